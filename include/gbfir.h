@@ -1,0 +1,205 @@
+/*
+ * gbfir.h — C ABI of the GB300 (sm_103a) direct-FIR library.
+ *
+ * This is the drop-in boundary for MatX's direct-FIR operators.  Each entry
+ * point replaces the CUDA branch of one MatX transform (the L4 dispatcher
+ * plus its L5 kernel) and keeps that transform's argument meaning, shape
+ * rules and error classes:
+ *
+ *   gbfir_conv1d           include/matx/transforms/conv.h:467-532 (conv1d_impl)
+ *                          include/matx/transforms/conv.h:402-451 (operand swap)
+ *                          include/matx/transforms/conv.h:175-224 (direct CUDA path)
+ *                          include/matx/transforms/corr.h:60-69   (corr = conv with reverse(conj(h)))
+ *   gbfir_resample_poly    include/matx/transforms/resample_poly.h:299-354 (resample_poly_impl)
+ *                          include/matx/transforms/resample_poly.h:64-210  (CUDA dispatcher)
+ *   gbfir_channelize_poly  include/matx/transforms/channelize_poly.h:724-849 (CUDA impl incl. the
+ *                          cuFFT ifft(FFTNorm::FORWARD) pass at :846, fused here)
+ *
+ * Entry points with no MatX counterpart (adjoints, ragged batches, plans) say
+ * so in their comment.
+ *
+ * Conventions
+ *  - Plain C.  No exception crosses the boundary; every function returns a
+ *    gbfir_status.  gbfir_last_error() gives a human-readable message for the
+ *    most recent failure on the calling thread.
+ *  - All device pointers are caller-owned and must stay valid until the work
+ *    enqueued on `stream` has completed.  Nothing here allocates device memory
+ *    unless an entry point says so.
+ *  - Every launch is enqueued on the given stream and returns asynchronously,
+ *    exactly like MatX's cudaExecutor path.
+ *  - A gbfir_buf describes a batch of 1-D rows: `batch` rows of `len`
+ *    elements, row r starting at ptr + r*batch_stride elements.  A row count of
+ *    1 or a batch_stride of 0 broadcasts one row over the batch (MatX's
+ *    clone<>() of a lower-rank operand, conv.h:467-532).  The innermost
+ *    dimension is always unit-stride; MatX's shim materialises other layouts
+ *    before calling in.
+ */
+#ifndef GBFIR_H_
+#define GBFIR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* CUDA stream handle; identical to cudaStream_t (struct CUstream_st*). */
+typedef struct CUstream_st *gbfir_stream_t;
+
+/* Status codes.  The first block mirrors matxError_t (include/matx/core/error.h:55-75)
+ * so the MatX shim can rethrow with the same class. */
+typedef enum gbfir_status {
+  GBFIR_SUCCESS = 0,
+  GBFIR_ERR_INVALID_PARAMETER = 1, /* matxInvalidParameter */
+  GBFIR_ERR_INVALID_DIM = 2,       /* matxInvalidDim */
+  GBFIR_ERR_INVALID_SIZE = 3,      /* matxInvalidSize */
+  GBFIR_ERR_INVALID_TYPE = 4,      /* matxInvalidType */
+  GBFIR_ERR_NOT_SUPPORTED = 5,     /* matxNotSupported */
+  GBFIR_ERR_CUDA = 6,              /* matxCudaError */
+  GBFIR_ERR_NULL_POINTER = 7,      /* a required pointer was NULL */
+  GBFIR_ERR_ALIGNMENT = 8,         /* pointer/stride not aligned to its element type */
+  GBFIR_ERR_WORKSPACE = 9,         /* workspace missing or too small */
+  GBFIR_ERR_TIMEOUT = 10           /* a bounded device-side wait gave up */
+} gbfir_status;
+
+typedef enum gbfir_dtype {
+  GBFIR_F32 = 0,  /* float                         */
+  GBFIR_C64 = 1,  /* cuda::std::complex<float>     */
+  GBFIR_F64 = 2,  /* double                        */
+  GBFIR_C128 = 3  /* cuda::std::complex<double>    */
+} gbfir_dtype;
+
+/* Same order as matxConvCorrMode_t (include/matx/core/operator_options.h:51-55). */
+typedef enum gbfir_conv_mode {
+  GBFIR_MODE_FULL = 0,
+  GBFIR_MODE_SAME = 1,
+  GBFIR_MODE_VALID = 2
+} gbfir_conv_mode;
+
+/* Arithmetic form of the tap contraction. */
+typedef enum gbfir_precision {
+  GBFIR_PREC_FP32 = 0,   /* CUDA-core FP32 (FP64 for F64/C128 operands)                 */
+  GBFIR_PREC_BF16 = 1,   /* tcgen05 tensor cores, bf16 operands, FP32 accumulate        */
+  GBFIR_PREC_FP16 = 2,   /* tcgen05 tensor cores, fp16 operands, FP32 accumulate        */
+  GBFIR_PREC_BF16X3 = 3  /* tcgen05, each operand split into three bf16 terms; the six
+                            cross products of order <= 2 are accumulated in FP32        */
+} gbfir_precision;
+
+typedef struct gbfir_buf {
+  void *ptr;            /* device pointer to row 0 element 0                 */
+  int64_t batch;        /* number of rows (>= 1)                             */
+  int64_t len;          /* elements per row                                  */
+  int64_t batch_stride; /* elements between rows; 0 broadcasts row 0         */
+  int32_t dtype;        /* gbfir_dtype                                       */
+} gbfir_buf;
+
+/* ---- forward operators ------------------------------------------------- */
+
+/* Direct 1-D convolution or correlation of every row of `in` with `h`.
+ *  out.len must be N+L-1 (FULL), max(N,L) (SAME) or max(N,L)-min(N,L)+1 (VALID),
+ *  matching Conv1DOp's output shape (include/matx/operators/conv.h:109-133).
+ *  The longer operand is treated as the signal (conv.h:427-450); SAME starts
+ *  at (Lmin-1)/2 for odd Lmin and Lmin/2-1 for even Lmin (kernels/conv.cuh:155-168).
+ *  is_corr != 0 computes corr(in, h) = conv1d(in, reverse(conj(h))) (corr.h:67).
+ *  `in` and `h` may each be batched (same row count as out) or broadcast.
+ *  out is complex if either operand is complex. */
+int gbfir_conv1d(gbfir_buf out, gbfir_buf in, gbfir_buf h, int32_t mode,
+                 int32_t is_corr, int32_t precision, gbfir_stream_t stream);
+
+/* Polyphase resampler: out[b] = up * (upsample-by-up, filter with h,
+ * downsample-by-down)(in[b]), with the scipy centring of
+ * include/matx/transforms/resample_poly.h:212-281 (even h gets a leading zero).
+ *  out.len must equal ceil(in.len*up/down) with the UNREDUCED up/down
+ *  (resample_poly.h:318-320); up/down are then divided by their gcd; up==down
+ *  copies the input and ignores h (resample_poly.h:333-336).
+ *  h is one row (broadcast); real or complex. */
+int gbfir_resample_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t up,
+                        int64_t down, int32_t precision, gbfir_stream_t stream);
+
+/* Polyphase channelizer, maximally decimated (D == M) or oversampled (D < M),
+ * fused FIR branch filtering + unnormalised positive-sign M-point DFT
+ * (include/matx/transforms/channelize_poly.h:724-849, host semantics :858-1029).
+ *  out is [batch][T][M] complex with T = ceil(in.len/D): out.len == T*M.
+ *  h is one row of any length L; it is zero-padded to P*M with P = ceil(L/M). */
+int gbfir_channelize_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t M,
+                          int64_t D, int32_t precision, gbfir_stream_t stream);
+
+/* ---- adjoints (no MatX counterpart) --------------------------------------
+ * For y = resample_poly(x, h, up, down) and the upstream gradient gy:
+ *   dx = transposed resampler of gy (correlation with the taps, up/down swapped),
+ *   dh = sum over the batch of the cross-correlation of gy with x,
+ *        reduced across blocks in FP64 in `workspace`.
+ * Either dx.ptr or dh.ptr may be NULL to skip that gradient.  up==down after
+ * the gcd gives dx = gy and dh = 0, matching the forward identity copy.
+ * Real FP32 operands only. */
+size_t gbfir_resample_poly_bwd_workspace_size(int64_t batch, int64_t in_len,
+                                              int64_t h_len, int64_t up,
+                                              int64_t down);
+int gbfir_resample_poly_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy,
+                            gbfir_buf x, gbfir_buf h, int64_t up, int64_t down,
+                            void *workspace, size_t workspace_bytes,
+                            gbfir_stream_t stream);
+
+/* Adjoint of gbfir_conv1d (is_corr == 0, real FP32, h broadcast):
+ *   dx = corr(gy, h) cropped to the signal, dh = sum_b corr(gy_b, x_b) cropped to L. */
+size_t gbfir_conv1d_bwd_workspace_size(int64_t batch, int64_t in_len,
+                                       int64_t h_len, int32_t mode);
+int gbfir_conv1d_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x,
+                     gbfir_buf h, int32_t mode, void *workspace,
+                     size_t workspace_bytes, gbfir_stream_t stream);
+
+/* ---- ragged batches (no MatX counterpart) --------------------------------
+ * One persistent launch resamples `count` independent complex64 signals of
+ * uneven length, tap count and up/down ratio.  Descriptors live in device
+ * memory (an array of gbfir_ragged_desc).  The launch is stream-ordered and
+ * contains no host synchronisation, so it can be captured in a CUDA graph. */
+typedef struct gbfir_ragged_desc {
+  const void *in;   /* complex64 input row                      */
+  void *out;        /* complex64 output row                     */
+  const float *h;   /* real taps                                */
+  int64_t in_len;
+  int64_t out_len;  /* must be ceil(in_len*up/down)             */
+  int32_t h_len;
+  int32_t up;       /* already reduced by gcd; up==down==1 copies */
+  int32_t down;
+  int32_t pad_;
+} gbfir_ragged_desc;
+
+/* Bytes of device workspace gbfir_ragged_resample needs for `count` signals
+ * and a tile plan of `num_tiles` tiles (from gbfir_ragged_plan). */
+size_t gbfir_ragged_workspace_size(int64_t count, int64_t num_tiles);
+
+/* Host-side planner: fills `tile_table` (host memory, num_tiles entries of 2
+ * int64 each: signal index and first output row) and returns the number of
+ * tiles, or a negative gbfir_status.  With tile_table == NULL only counts. */
+int64_t gbfir_ragged_plan(const gbfir_ragged_desc *host_descs, int64_t count,
+                          int32_t rows_per_tile, int64_t *tile_table);
+
+int gbfir_ragged_resample(const gbfir_ragged_desc *device_descs, int64_t count,
+                          const int64_t *device_tile_table, int64_t num_tiles,
+                          int32_t rows_per_tile, int32_t precision,
+                          void *workspace, size_t workspace_bytes,
+                          gbfir_stream_t stream);
+
+/* ---- tuning and diagnostics ---------------------------------------------- */
+
+/* Override the tile shape the dispatcher picks for resample_poly (autotuner
+ * hook; no MatX counterpart).  rows_per_thread in {1,2,4}, col_warps in
+ * {1,2,4,8}, group (outputs per row = group*up) >= 1.  Passing zeros restores
+ * the built-in heuristic. */
+int gbfir_set_resample_tile(int32_t rows_per_thread, int32_t col_warps,
+                            int32_t group);
+
+/* Number of device kernels this library has launched in this process. */
+uint64_t gbfir_launch_count(void);
+
+const char *gbfir_status_string(int status);
+const char *gbfir_last_error(void);
+int gbfir_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBFIR_H_ */

@@ -1,0 +1,221 @@
+"""Pins the CPU oracle to the reference: its golden vectors, its known-answer
+tests, and (where MatX compiles here) MatX's HostExecutor on the same inputs."""
+import numpy as np
+import pytest
+
+from conftest import load_cases, rel_l2
+
+MODES = {"conv_full": 0, "conv_same": 1, "conv_valid": 2}
+
+
+def test_conv_known_answer(oracle_mod):
+    # test/00_transform/ConvCorr.cu:250-288 — in {1,2,3,4}, h {2,1,-1}
+    x = np.array([1, 2, 3, 4], dtype=np.float64)
+    h = np.array([2, 1, -1], dtype=np.float64)
+    assert np.array_equal(oracle_mod.conv1d(x, h, 0)[0], [2, 5, 7, 9, 1, -4])
+    assert np.array_equal(oracle_mod.conv1d(x, h, 1)[0], [5, 7, 9, 1])
+    assert np.array_equal(oracle_mod.conv1d(x, h, 2)[0], [7, 9])
+
+
+@pytest.mark.parametrize("case", sorted(load_cases("conv.npz")))
+def test_conv_golden(oracle_mod, case):
+    c = load_cases("conv.npz")[case]
+    a, b = c["a_op"], c["b_op"]
+    for key, mode in MODES.items():
+        y = oracle_mod.conv1d(a, b, mode)[0]
+        assert y.shape == c[key].shape, key
+        assert rel_l2(y, c[key]) < 1e-6, key
+    assert rel_l2(oracle_mod.conv1d(a, b, 0, is_corr=True)[0], c["corr"]) < 1e-6
+    assert rel_l2(oracle_mod.conv1d(b, a, 0, is_corr=True)[0], c["corr_swap"]) < 1e-6
+
+
+@pytest.mark.parametrize("case", sorted(load_cases("resample.npz")))
+def test_resample_golden(oracle_mod, case):
+    c = load_cases("resample.npz")[case]
+    up, down = (int(v) for v in c["updown"])
+    y = oracle_mod.resample_poly(c["a"], c["h"], up, down)[0]
+    assert y.shape == c["y"].shape
+    tol = 1e-12 if c["a"].dtype == np.float64 else 1e-6
+    assert rel_l2(y, c["y"]) < tol
+
+
+@pytest.mark.parametrize("case", sorted(load_cases("channelize.npz")))
+def test_channelize_golden(oracle_mod, case):
+    c = load_cases("channelize.npz")[case]
+    M, D = (int(v) for v in c["md"])
+    a = c["a"]
+    batch_shape = a.shape[:-1]
+    y = oracle_mod.channelize_poly(a.reshape(-1, a.shape[-1]), c["h"], M, D)
+    y = y.reshape(*batch_shape, y.shape[-2], M) if batch_shape else y[0]
+    tol = 1e-10 if a.dtype == np.complex128 else 1e-5
+    assert y.shape == c["y"].shape
+    assert rel_l2(y, c["y"]) < tol
+    if "y_hreal" in c:
+        yr = oracle_mod.channelize_poly(a.reshape(-1, a.shape[-1]), np.real(c["h"]), M, D)
+        yr = yr.reshape(c["y_hreal"].shape)
+        assert rel_l2(yr, c["y_hreal"]) < tol
+
+
+def test_harris2003_known_answer(oracle_mod):
+    # ChannelizePoly.cu:820-1100, double, thresh 1e-12 absolute per component
+    import os
+    from conftest import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "harris2003.npz"))
+    M = int(z["M"][0])
+    y = oracle_mod.channelize_poly(z["x"], z["h"], M, M)[0]
+    assert np.max(np.abs(y.real - z["y"].real)) < 1e-12
+    assert np.max(np.abs(y.imag - z["y"].imag)) < 1e-12
+
+
+def test_harris2003_oversampled(oracle_mod):
+    # ChannelizePoly.cu:1104-1132, M=40, D=28, golden from the reference's .bin
+    import os
+    from conftest import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "harris2003_oversampled.npz"))
+    M, D = (int(v) for v in z["MD"])
+    y = oracle_mod.channelize_poly(z["x"], z["h"], M, D)[0]
+    assert y.shape == z["y"].shape
+    assert np.max(np.abs(y - z["y"])) < 1e-10
+
+
+def test_float_oracle_close_to_double(oracle_mod):
+    rng = np.random.default_rng(5)
+    x = (rng.standard_normal((3, 4000)) + 1j * rng.standard_normal((3, 4000))).astype(np.complex64)
+    h = rng.standard_normal(61).astype(np.float32)
+    assert rel_l2(oracle_mod.resample_poly(x, h, 3, 2, double=False),
+                  oracle_mod.resample_poly(x, h, 3, 2)) < 1e-6
+    assert rel_l2(oracle_mod.channelize_poly(x, h, 16, 16, double=False),
+                  oracle_mod.channelize_poly(x, h, 16, 16)) < 1e-5
+
+
+def test_threads_do_not_change_results(oracle_mod):
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal((8, 3000)).astype(np.float32)
+    h = rng.standard_normal(63).astype(np.float32)
+    a = oracle_mod.conv1d(x, h, 0, double=False, nthreads=1)
+    b = oracle_mod.conv1d(x, h, 0, double=False, nthreads=4)
+    assert np.array_equal(a, b)
+    a = oracle_mod.resample_poly(x, h, 4, 5, double=False, nthreads=1)
+    b = oracle_mod.resample_poly(x, h, 4, 5, double=False, nthreads=4)
+    assert np.array_equal(a, b)
+
+
+# ---- pin against MatX's own HostExecutor (only where MatX was compiled) ------
+
+def _need_ref(oracle_mod):
+    if oracle_mod.ref_lib() is None:
+        pytest.skip("MatX HostExecutor library (oracle/_ref) not built on this host")
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("is_corr", [0, 1])
+@pytest.mark.parametrize("shape", [(3, 200, 17), (2, 64, 64), (2, 30, 100), (1, 1000, 16)])
+@pytest.mark.parametrize("cplx", ["real", "cx_rh", "cx_ch"])
+def test_conv_matches_matx_host(oracle_mod, mode, is_corr, shape, cplx):
+    _need_ref(oracle_mod)
+    B, N, L = shape
+    rng = np.random.default_rng(hash((mode, is_corr, shape, cplx)) % 2**32)
+    x = rng.standard_normal((B, N))
+    h = rng.standard_normal(L)
+    if cplx != "real":
+        x = x + 1j * rng.standard_normal((B, N))
+    if cplx == "cx_ch":
+        h = h + 1j * rng.standard_normal(L)
+    for double in (True, False):
+        r = oracle_mod.ref_conv1d(x, h, mode, bool(is_corr), double=double)
+        o = oracle_mod.conv1d(x, h, mode, bool(is_corr), double=double)
+        assert r.shape == o.shape
+        assert rel_l2(o, r) < (1e-13 if double else 1e-6)
+
+
+@pytest.mark.parametrize("updown", [(3, 2), (4, 5), (160, 147), (1, 3), (2, 1), (6, 4), (5, 5)])
+@pytest.mark.parametrize("L", [31, 30, 5, 401])
+@pytest.mark.parametrize("cplx", ["real", "cx_rh", "cx_ch"])
+def test_resample_matches_matx_host(oracle_mod, updown, L, cplx):
+    _need_ref(oracle_mod)
+    up, down = updown
+    rng = np.random.default_rng(hash((updown, L, cplx)) % 2**32)
+    x = rng.standard_normal((2, 777))
+    h = rng.standard_normal(L)
+    if cplx != "real":
+        x = x + 1j * rng.standard_normal((2, 777))
+    if cplx == "cx_ch":
+        h = h + 1j * rng.standard_normal(L)
+    for double in (True, False):
+        r = oracle_mod.ref_resample_poly(x, h, up, down, double=double)
+        if r is None:
+            continue
+        o = oracle_mod.resample_poly(x, h, up, down, double=double)
+        assert rel_l2(o, r) < (1e-13 if double else 1e-6)
+
+
+@pytest.mark.parametrize("MD", [(8, 8), (10, 10), (13, 13), (16, 12), (40, 28), (9, 4), (1, 1), (64, 64)])
+@pytest.mark.parametrize("L", [100, 64, 7])
+@pytest.mark.parametrize("cplx", ["cx_rh", "cx_ch", "real"])
+def test_channelize_matches_matx_host(oracle_mod, MD, L, cplx):
+    _need_ref(oracle_mod)
+    M, D = MD
+    rng = np.random.default_rng(hash((MD, L, cplx)) % 2**32)
+    x = rng.standard_normal((2, 1001))
+    h = rng.standard_normal(L)
+    if cplx != "real":
+        x = x + 1j * rng.standard_normal((2, 1001))
+    if cplx == "cx_ch":
+        h = h + 1j * rng.standard_normal(L)
+    for double in (True, False):
+        r = oracle_mod.ref_channelize_poly(x, h, M, D, double=double)
+        if r is None:
+            continue
+        o = oracle_mod.channelize_poly(x, h, M, D, double=double)
+        assert rel_l2(o, r) < (1e-12 if double else 1e-5)
+
+
+# ---- adjoint oracle against FP64 central finite differences ------------------
+
+@pytest.mark.parametrize("updown", [(3, 2), (1, 1), (4, 5), (2, 3)])
+@pytest.mark.parametrize("L", [13, 12])
+def test_resample_adjoint_oracle_fd(oracle_mod, updown, L):
+    up, down = updown
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal((2, 60))
+    h = rng.standard_normal(L)
+    ny = oracle_mod.resample_poly(x, h, up, down).shape[1]
+    gy = rng.standard_normal((2, ny))
+    dx, dh = oracle_mod.resample_poly_bwd(gy, x, h, up, down)
+    f = lambda xx, hh: float(np.sum(gy * oracle_mod.resample_poly(xx, hh, up, down)))
+    eps = 1e-6
+    for _ in range(8):
+        b, i = rng.integers(2), rng.integers(60)
+        xp, xm = x.copy(), x.copy()
+        xp[b, i] += eps
+        xm[b, i] -= eps
+        assert abs((f(xp, h) - f(xm, h)) / (2 * eps) - dx[b, i]) < 1e-6
+        k = rng.integers(L)
+        hp, hm = h.copy(), h.copy()
+        hp[k] += eps
+        hm[k] -= eps
+        assert abs((f(x, hp) - f(x, hm)) / (2 * eps) - dh[k]) < 1e-6
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("L", [9, 8])
+def test_conv_adjoint_oracle_fd(oracle_mod, mode, L):
+    rng = np.random.default_rng(12)
+    x = rng.standard_normal((2, 50))
+    h = rng.standard_normal(L)
+    ny = oracle_mod.conv1d(x, h, mode).shape[1]
+    gy = rng.standard_normal((2, ny))
+    dx, dh = oracle_mod.conv1d_bwd(gy, x, h, mode)
+    f = lambda xx, hh: float(np.sum(gy * oracle_mod.conv1d(xx, hh, mode)))
+    eps = 1e-6
+    for _ in range(8):
+        b, i = rng.integers(2), rng.integers(50)
+        xp, xm = x.copy(), x.copy()
+        xp[b, i] += eps
+        xm[b, i] -= eps
+        assert abs((f(xp, h) - f(xm, h)) / (2 * eps) - dx[b, i]) < 1e-6
+        k = rng.integers(L)
+        hp, hm = h.copy(), h.copy()
+        hp[k] += eps
+        hm[k] -= eps
+        assert abs((f(x, hp) - f(x, hm)) / (2 * eps) - dh[k]) < 1e-6
