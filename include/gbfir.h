@@ -40,6 +40,12 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#if defined(__GNUC__)
+#define GBFIR_API __attribute__((visibility("default")))
+#else
+#define GBFIR_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -104,7 +110,7 @@ typedef struct gbfir_buf {
  *  is_corr != 0 computes corr(in, h) = conv1d(in, reverse(conj(h))) (corr.h:67).
  *  `in` and `h` may each be batched (same row count as out) or broadcast.
  *  out is complex if either operand is complex. */
-int gbfir_conv1d(gbfir_buf out, gbfir_buf in, gbfir_buf h, int32_t mode,
+GBFIR_API int gbfir_conv1d(gbfir_buf out, gbfir_buf in, gbfir_buf h, int32_t mode,
                  int32_t is_corr, int32_t precision, gbfir_stream_t stream);
 
 /* Polyphase resampler: out[b] = up * (upsample-by-up, filter with h,
@@ -114,7 +120,7 @@ int gbfir_conv1d(gbfir_buf out, gbfir_buf in, gbfir_buf h, int32_t mode,
  *  (resample_poly.h:318-320); up/down are then divided by their gcd; up==down
  *  copies the input and ignores h (resample_poly.h:333-336).
  *  h is one row (broadcast); real or complex. */
-int gbfir_resample_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t up,
+GBFIR_API int gbfir_resample_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t up,
                         int64_t down, int32_t precision, gbfir_stream_t stream);
 
 /* Polyphase channelizer, maximally decimated (D == M) or oversampled (D < M),
@@ -122,7 +128,7 @@ int gbfir_resample_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t up,
  * (include/matx/transforms/channelize_poly.h:724-849, host semantics :858-1029).
  *  out is [batch][T][M] complex with T = ceil(in.len/D): out.len == T*M.
  *  h is one row of any length L; it is zero-padded to P*M with P = ceil(L/M). */
-int gbfir_channelize_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t M,
+GBFIR_API int gbfir_channelize_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t M,
                           int64_t D, int32_t precision, gbfir_stream_t stream);
 
 /* ---- adjoints (no MatX counterpart) --------------------------------------
@@ -133,19 +139,19 @@ int gbfir_channelize_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t M,
  * Either dx.ptr or dh.ptr may be NULL to skip that gradient.  up==down after
  * the gcd gives dx = gy and dh = 0, matching the forward identity copy.
  * Real FP32 operands only. */
-size_t gbfir_resample_poly_bwd_workspace_size(int64_t batch, int64_t in_len,
+GBFIR_API size_t gbfir_resample_poly_bwd_workspace_size(int64_t batch, int64_t in_len,
                                               int64_t h_len, int64_t up,
                                               int64_t down);
-int gbfir_resample_poly_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy,
+GBFIR_API int gbfir_resample_poly_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy,
                             gbfir_buf x, gbfir_buf h, int64_t up, int64_t down,
                             void *workspace, size_t workspace_bytes,
                             gbfir_stream_t stream);
 
 /* Adjoint of gbfir_conv1d (is_corr == 0, real FP32, h broadcast):
  *   dx = corr(gy, h) cropped to the signal, dh = sum_b corr(gy_b, x_b) cropped to L. */
-size_t gbfir_conv1d_bwd_workspace_size(int64_t batch, int64_t in_len,
+GBFIR_API size_t gbfir_conv1d_bwd_workspace_size(int64_t batch, int64_t in_len,
                                        int64_t h_len, int32_t mode);
-int gbfir_conv1d_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x,
+GBFIR_API int gbfir_conv1d_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x,
                      gbfir_buf h, int32_t mode, void *workspace,
                      size_t workspace_bytes, gbfir_stream_t stream);
 
@@ -168,15 +174,15 @@ typedef struct gbfir_ragged_desc {
 
 /* Bytes of device workspace gbfir_ragged_resample needs for `count` signals
  * and a tile plan of `num_tiles` tiles (from gbfir_ragged_plan). */
-size_t gbfir_ragged_workspace_size(int64_t count, int64_t num_tiles);
+GBFIR_API size_t gbfir_ragged_workspace_size(int64_t count, int64_t num_tiles);
 
 /* Host-side planner: fills `tile_table` (host memory, num_tiles entries of 2
  * int64 each: signal index and first output row) and returns the number of
  * tiles, or a negative gbfir_status.  With tile_table == NULL only counts. */
-int64_t gbfir_ragged_plan(const gbfir_ragged_desc *host_descs, int64_t count,
+GBFIR_API int64_t gbfir_ragged_plan(const gbfir_ragged_desc *host_descs, int64_t count,
                           int32_t rows_per_tile, int64_t *tile_table);
 
-int gbfir_ragged_resample(const gbfir_ragged_desc *device_descs, int64_t count,
+GBFIR_API int gbfir_ragged_resample(const gbfir_ragged_desc *device_descs, int64_t count,
                           const int64_t *device_tile_table, int64_t num_tiles,
                           int32_t rows_per_tile, int32_t precision,
                           void *workspace, size_t workspace_bytes,
@@ -188,15 +194,15 @@ int gbfir_ragged_resample(const gbfir_ragged_desc *device_descs, int64_t count,
  * hook; no MatX counterpart).  rows_per_thread in {1,2,4}, col_warps in
  * {1,2,4,8}, group (outputs per row = group*up) >= 1.  Passing zeros restores
  * the built-in heuristic. */
-int gbfir_set_resample_tile(int32_t rows_per_thread, int32_t col_warps,
+GBFIR_API int gbfir_set_resample_tile(int32_t rows_per_thread, int32_t col_warps,
                             int32_t group);
 
 /* Number of device kernels this library has launched in this process. */
-uint64_t gbfir_launch_count(void);
+GBFIR_API uint64_t gbfir_launch_count(void);
 
-const char *gbfir_status_string(int status);
-const char *gbfir_last_error(void);
-int gbfir_version(void);
+GBFIR_API const char *gbfir_status_string(int status);
+GBFIR_API const char *gbfir_last_error(void);
+GBFIR_API int gbfir_version(void);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,199 @@
+"""matx_gb300 — GB300-native (sm_103a) direct-FIR operators behind MatX's operator API.
+
+Python host mirror of MatX's direct-FIR operators.  Each function keeps the MatX
+operator's name, argument meaning, output shape and error class, and runs the
+CUDA library libgbfir.so (include/gbfir.h) on torch's current CUDA stream:
+
+    conv1d(x, h, mode)                 include/matx/operators/conv.h:243-274
+    corr(x, h, mode)                   include/matx/operators/corr.h:224-253
+    resample_poly(x, h, up, down)      include/matx/operators/resample_poly.h:182-186
+    channelize_poly(x, h, M, D)        include/matx/operators/channelize_poly.h:275-278
+
+Tensors are torch CUDA tensors; the last dimension is the signal axis and every
+leading dimension is a batch dimension (MatX's BlockToIdx batch folding,
+core/operator_utils.h:244-267).  There is no CPU path: a CPU tensor or a missing
+library raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import torch
+
+from . import _lib
+from ._lib import GbfirError, PREC
+
+MATX_C_MODE_FULL, MATX_C_MODE_SAME, MATX_C_MODE_VALID = 0, 1, 2
+_MODE_NAMES = {"full": 0, "same": 1, "valid": 2}
+
+__all__ = ["conv1d", "corr", "resample_poly", "channelize_poly", "GbfirError",
+           "MATX_C_MODE_FULL", "MATX_C_MODE_SAME", "MATX_C_MODE_VALID", "launch_count",
+           "resample_out_len", "set_resample_tile"]
+
+_DT = {torch.float32: _lib.GBFIR_F32, torch.complex64: _lib.GBFIR_C64,
+       torch.float64: _lib.GBFIR_F64, torch.complex128: _lib.GBFIR_C128}
+
+
+def _mode(mode) -> int:
+    if isinstance(mode, str):
+        return _MODE_NAMES[mode.lower()]
+    return int(mode)
+
+
+def _prec(precision) -> int:
+    if isinstance(precision, str):
+        return PREC[precision.lower()]
+    return int(precision)
+
+
+def _stream() -> ctypes.c_void_p:
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _rows(t: torch.Tensor, name: str) -> torch.Tensor:
+    if not t.is_cuda:
+        raise ValueError(f"{name}: matx_gb300 runs on CUDA tensors only (got {t.device})")
+    if t.dtype not in _DT:
+        raise TypeError(f"{name}: unsupported dtype {t.dtype}")
+    if t.dim() == 0:
+        raise ValueError(f"{name}: needs at least one dimension")
+    return t
+
+
+def _buf(t: torch.Tensor, name: str) -> _lib.Buf:
+    """Describe a tensor as rows of its last dimension (materialises other layouts)."""
+    t = _rows(t, name)
+    if t.stride(-1) != 1:
+        raise ValueError(f"{name}: last dimension must be unit-stride")
+    n = t.shape[-1]
+    batch = t.numel() // n if n else 0
+    if t.dim() == 1:
+        bstride = 0
+    else:
+        flat = t.reshape(-1, n)
+        if flat.data_ptr() != t.data_ptr() or (batch > 1 and flat.stride(0) < n):
+            raise ValueError(f"{name}: leading dimensions must fold into one batch dimension")
+        bstride = flat.stride(0) if batch > 1 else 0
+    return _lib.Buf(t.data_ptr(), max(batch, 1), n, bstride, _DT[t.dtype])
+
+
+def _prep_in(t: torch.Tensor, name: str) -> torch.Tensor:
+    t = _rows(t, name)
+    if t.stride(-1) != 1 or (t.dim() > 1 and not t.is_contiguous()):
+        t = t.contiguous()  # MatX's shim materialises strided views the same way
+    return t
+
+
+def _out_dtype(*ts) -> torch.dtype:
+    cplx = any(t.is_complex() for t in ts)
+    dbl = any(t.dtype in (torch.float64, torch.complex128) for t in ts)
+    if cplx:
+        return torch.complex128 if dbl else torch.complex64
+    return torch.float64 if dbl else torch.float32
+
+
+def _cast(t: torch.Tensor, double: bool) -> torch.Tensor:
+    if t.is_complex():
+        want = torch.complex128 if double else torch.complex64
+    else:
+        want = torch.float64 if double else torch.float32
+    return t if t.dtype == want else t.to(want)
+
+
+def launch_count() -> int:
+    """Kernels libgbfir has launched in this process."""
+    return int(_lib.load().gbfir_launch_count())
+
+
+def set_resample_tile(rows_per_thread: int = 0, col_warps: int = 0, group: int = 0):
+    """Force a resample_poly tile shape (0, 0, 0 restores the heuristic)."""
+    _lib.check(_lib.load().gbfir_set_resample_tile(rows_per_thread, col_warps, group))
+
+
+def conv1d(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torch.Tensor | None = None,
+           _corr: bool = False) -> torch.Tensor:
+    """Direct 1-D convolution (MatX conv1d with MATX_C_METHOD_DIRECT).
+
+    Output length: N+L-1 (FULL), max(N,L) (SAME), max(N,L)-min(N,L)+1 (VALID).
+    The operand with more dimensions sets the batch shape; a 1-D operand is
+    broadcast across the other's batch (conv.h:467-532).
+    """
+    lib = _lib.load()
+    m = _mode(mode)
+    double = _out_dtype(x, h) in (torch.float64, torch.complex128)
+    x = _prep_in(_cast(x, double), "conv1d x")
+    h = _prep_in(_cast(h, double), "conv1d h")
+    N, L = x.shape[-1], h.shape[-1]
+    if m == 0:
+        olen = N + L - 1
+    elif m == 1:
+        olen = max(N, L)
+    else:
+        olen = max(N, L) - min(N, L) + 1
+    batch_shape = x.shape[:-1] if x.dim() >= h.dim() else h.shape[:-1]
+    if x.dim() > 1 and h.dim() > 1 and x.shape[:-1] != h.shape[:-1]:
+        raise GbfirError(2, "conv1d: batched operands must have the same batch shape")
+    odt = _out_dtype(x, h)
+    if out is None:
+        out = torch.empty(*batch_shape, olen, dtype=odt, device=x.device)
+    _lib.check(lib.gbfir_conv1d(_buf(out, "conv1d out"), _buf(x, "conv1d x"), _buf(h, "conv1d h"),
+                                m, int(_corr), 0, _stream()))
+    return out
+
+
+def corr(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torch.Tensor | None = None):
+    """Direct correlation: corr(x, h) = conv1d(x, reverse(conj(h))) (corr.h:67)."""
+    return conv1d(x, h, mode, out=out, _corr=True)
+
+
+def resample_out_len(n: int, up: int, down: int) -> int:
+    """ceil(n*up/down) with the unreduced up/down (resample_poly.h:67-79)."""
+    s = n * up
+    return s // down + (1 if s % down else 0)
+
+
+def resample_poly(x: torch.Tensor, h: torch.Tensor, up: int, down: int, *, precision="fp32",
+                  out: torch.Tensor | None = None) -> torch.Tensor:
+    """Polyphase resampler (MatX resample_poly, scipy centring and gain).
+
+    ``precision`` selects the tap-contraction form: "fp32" (CUDA cores),
+    "bf16", "fp16" or "bf16x3" (tcgen05 tensor cores, FP32 accumulate).
+    """
+    lib = _lib.load()
+    double = _out_dtype(x, h) in (torch.float64, torch.complex128)
+    x = _prep_in(_cast(x, double), "resample_poly x")
+    h = _prep_in(_cast(h, double), "resample_poly h")
+    if h.dim() != 1:
+        raise GbfirError(2, "resample_poly: currently only support 1D filters")
+    if up <= 0 or down <= 0:
+        raise GbfirError(1, "resample_poly: up and down must be positive")
+    olen = resample_out_len(x.shape[-1], up, down)
+    if out is None:
+        out = torch.empty(*x.shape[:-1], olen, dtype=_out_dtype(x, h), device=x.device)
+    _lib.check(lib.gbfir_resample_poly(_buf(out, "resample_poly out"), _buf(x, "resample_poly x"),
+                                       _buf(h, "resample_poly h"), int(up), int(down), _prec(precision),
+                                       _stream()))
+    return out
+
+
+def channelize_poly(x: torch.Tensor, h: torch.Tensor, num_channels: int, decimation_factor: int, *,
+                    precision="fp32", out: torch.Tensor | None = None) -> torch.Tensor:
+    """Polyphase channelizer, output [..., ceil(N/D), M] complex (channelize_poly.h:81-88)."""
+    lib = _lib.load()
+    double = _out_dtype(x, h) in (torch.float64, torch.complex128)
+    x = _prep_in(_cast(x, double), "channelize_poly x")
+    h = _prep_in(_cast(h, double), "channelize_poly h")
+    M, D = int(num_channels), int(decimation_factor)
+    if h.dim() != 1:
+        raise GbfirError(2, "channelize_poly: currently only support 1D filters")
+    if M <= 0 or D <= 0 or D > M:
+        raise GbfirError(1, "channelize_poly: need 0 < decimation_factor <= num_channels")
+    T = (x.shape[-1] + D - 1) // D
+    odt = torch.complex128 if double else torch.complex64
+    if out is None:
+        out = torch.empty(*x.shape[:-1], T, M, dtype=odt, device=x.device)
+    flat = out.view(*out.shape[:-2], T * M)
+    _lib.check(lib.gbfir_channelize_poly(_buf(flat, "channelize_poly out"), _buf(x, "channelize_poly x"),
+                                         _buf(h, "channelize_poly h"), M, D, _prec(precision), _stream()))
+    return out

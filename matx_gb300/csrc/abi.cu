@@ -1,0 +1,232 @@
+// abi.cu — the extern "C" boundary of libgbfir (include/gbfir.h).
+//
+// Every entry point validates its arguments with the same rules (and the same
+// error classes) as the MatX transform it replaces, then enqueues kernels on the
+// caller's stream.  No exception crosses the boundary.
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <unordered_map>
+
+#include "common.cuh"
+
+namespace gbfir {
+
+int conv1d_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int mode, int is_corr, cudaStream_t s);
+int resample_poly_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t up, int64_t down,
+                     cudaStream_t s);
+int channelize_poly_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t M, int64_t D,
+                       cudaStream_t s);
+int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t up, int64_t down,
+                     int precision, cudaStream_t s);
+int set_resample_tile(int rq, int wc, int group);
+
+static thread_local std::string t_last_error;
+static std::atomic<uint64_t> g_launches{0};
+
+void set_error(const std::string &msg) { t_last_error = msg; }
+void count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+int num_sms() {
+  static std::mutex mu;
+  static std::unordered_map<int, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(dev);
+  if (it != cache.end()) return it->second;
+  int n = 0;
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  if (n <= 0) n = 1;
+  cache[dev] = n;
+  return n;
+}
+
+int ensure_smem(const void *func, size_t bytes, const char *what) {
+  static std::mutex mu;
+  static std::unordered_map<uint64_t, size_t> done;  // (device, func) -> bytes granted
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint64_t key = (reinterpret_cast<uint64_t>(func) << 4) ^ (uint64_t)dev;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = done.find(key);
+    if (it != done.end() && it->second >= bytes) return GBFIR_SUCCESS;
+  }
+  if (bytes > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) {
+      char buf[256];
+      snprintf(buf, sizeof(buf), "%s: cannot reserve %zu B of shared memory: %s", what, bytes, cudaGetErrorString(e));
+      set_error(buf);
+      return GBFIR_ERR_CUDA;
+    }
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  done[key] = bytes;
+  return GBFIR_SUCCESS;
+}
+
+int check_buf(const gbfir_buf &b, const char *name, bool allow_broadcast) {
+  if (b.ptr == nullptr) GBFIR_FAIL(GBFIR_ERR_NULL_POINTER, "%s: null pointer", name);
+  const size_t es = dtype_size(b.dtype);
+  if (es == 0) GBFIR_FAIL(GBFIR_ERR_INVALID_TYPE, "%s: unknown dtype %d", name, (int)b.dtype);
+  if (b.batch < 1) GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "%s: batch must be >= 1 (got %lld)", name, (long long)b.batch);
+  if (b.len < 1) GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "%s: length must be >= 1 (got %lld)", name, (long long)b.len);
+  const size_t align = (b.dtype == GBFIR_C128) ? 16 : es;
+  if (reinterpret_cast<uintptr_t>(b.ptr) % align)
+    GBFIR_FAIL(GBFIR_ERR_ALIGNMENT, "%s: pointer not aligned to %zu bytes", name, align);
+  if (b.batch > 1) {
+    if (b.batch_stride < 0) GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "%s: negative batch stride", name);
+    if (b.batch_stride == 0 && !allow_broadcast)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "%s: zero batch stride is only allowed for inputs", name);
+    if (b.batch_stride != 0 && b.batch_stride < b.len)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "%s: batch stride %lld shorter than a row (%lld)", name,
+                 (long long)b.batch_stride, (long long)b.len);
+  }
+  return GBFIR_SUCCESS;
+}
+
+// Output dtype rule: complex if either operand is complex, same precision as the inputs.
+static int check_types(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, const char *what,
+                       bool out_always_complex) {
+  if (dtype_double(in.dtype) != dtype_double(h.dtype) || dtype_double(in.dtype) != dtype_double(out.dtype))
+    GBFIR_FAIL(GBFIR_ERR_INVALID_TYPE, "%s: operands must all be single or all be double precision", what);
+  const bool oc = out_always_complex || dtype_complex(in.dtype) || dtype_complex(h.dtype);
+  if (dtype_complex(out.dtype) != oc)
+    GBFIR_FAIL(GBFIR_ERR_INVALID_TYPE, "%s: output must be %s", what, oc ? "complex" : "real");
+  return GBFIR_SUCCESS;
+}
+
+static int check_precision(int32_t precision, const char *what) {
+  if (precision < GBFIR_PREC_FP32 || precision > GBFIR_PREC_BF16X3)
+    GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "%s: unknown precision %d", what, (int)precision);
+  return GBFIR_SUCCESS;
+}
+
+}  // namespace gbfir
+
+using namespace gbfir;
+
+#define GBFIR_TRY(expr)        \
+  do {                         \
+    int _rc = (expr);          \
+    if (_rc) return _rc;       \
+  } while (0)
+
+extern "C" {
+
+int gbfir_conv1d(gbfir_buf out, gbfir_buf in, gbfir_buf h, int32_t mode, int32_t is_corr, int32_t precision,
+                 gbfir_stream_t stream) {
+  try {
+    GBFIR_TRY(check_buf(out, "conv1d out", false));
+    GBFIR_TRY(check_buf(in, "conv1d in", true));
+    GBFIR_TRY(check_buf(h, "conv1d h", true));
+    GBFIR_TRY(check_types(out, in, h, "conv1d", false));
+    GBFIR_TRY(check_precision(precision, "conv1d"));
+    if (mode < GBFIR_MODE_FULL || mode > GBFIR_MODE_VALID)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "conv1d: unknown mode %d", (int)mode);
+    // batch rule of conv1d_impl (conv.h:467-532): each operand is one row or out.batch rows
+    if ((in.batch != 1 && in.batch != out.batch) || (h.batch != 1 && h.batch != out.batch))
+      GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "conv1d: batch sizes do not match (out %lld, in %lld, h %lld)",
+                 (long long)out.batch, (long long)in.batch, (long long)h.batch);
+    const int64_t mx = std::max(in.len, h.len), mn = std::min(in.len, h.len);
+    const int64_t want = mode == GBFIR_MODE_FULL ? in.len + h.len - 1 : mode == GBFIR_MODE_SAME ? mx : mx - mn + 1;
+    if (out.len != want)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "conv1d: output length %lld, expected %lld", (long long)out.len,
+                 (long long)want);
+    if (precision != GBFIR_PREC_FP32)
+      GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "conv1d: only the FP32 form is available for conv1d");
+    return conv1d_fp(out, in, h, mode, is_corr != 0, reinterpret_cast<cudaStream_t>(stream));
+  } catch (...) {
+    GBFIR_FAIL(GBFIR_ERR_CUDA, "conv1d: internal exception");
+  }
+}
+
+int gbfir_resample_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t up, int64_t down, int32_t precision,
+                        gbfir_stream_t stream) {
+  try {
+    GBFIR_TRY(check_buf(out, "resample_poly out", false));
+    GBFIR_TRY(check_buf(in, "resample_poly in", false));
+    GBFIR_TRY(check_buf(h, "resample_poly h", false));
+    GBFIR_TRY(check_types(out, in, h, "resample_poly", false));
+    GBFIR_TRY(check_precision(precision, "resample_poly"));
+    if (up <= 0) GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "resample_poly: up must be positive");
+    if (down <= 0) GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "resample_poly: down must be positive");
+    if (h.batch != 1) GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "resample_poly: the filter must be one row");
+    if (out.batch != in.batch)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "resample_poly: input/output must have matched batch sizes");
+    const int64_t up_size = in.len * up;
+    const int64_t outlen = up_size / down + ((up_size % down) ? 1 : 0);
+    if (out.len != outlen)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "resample_poly: output size mismatch (%lld, expected %lld)",
+                 (long long)out.len, (long long)outlen);
+    const int64_t g = std::gcd(up, down);
+    up /= g;
+    down /= g;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (precision == GBFIR_PREC_FP32 || (up == 1 && down == 1)) return resample_poly_fp(out, in, h, up, down, s);
+    return resample_poly_tc(out, in, h, up, down, precision, s);
+  } catch (...) {
+    GBFIR_FAIL(GBFIR_ERR_CUDA, "resample_poly: internal exception");
+  }
+}
+
+int gbfir_channelize_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t M, int64_t D, int32_t precision,
+                          gbfir_stream_t stream) {
+  try {
+    GBFIR_TRY(check_buf(out, "channelize_poly out", false));
+    GBFIR_TRY(check_buf(in, "channelize_poly in", false));
+    GBFIR_TRY(check_buf(h, "channelize_poly h", false));
+    GBFIR_TRY(check_types(out, in, h, "channelize_poly", true));
+    GBFIR_TRY(check_precision(precision, "channelize_poly"));
+    if (M <= 0) GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "channelize_poly: num_channels must be positive");
+    if (D <= 0) GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "channelize_poly: decimation_factor must be positive");
+    if (D > M) GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "channelize_poly: decimation_factor must be <= num_channels");
+    if (h.batch != 1) GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "channelize_poly: currently only support 1D filters");
+    if (out.batch != in.batch)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "channelize_poly: input/output must have matched batch sizes");
+    const int64_t T = (in.len + D - 1) / D;
+    if (out.len != T * M)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "channelize_poly: output row must hold T*M = %lld elements (got %lld)",
+                 (long long)(T * M), (long long)out.len);
+    if (precision != GBFIR_PREC_FP32)
+      GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "channelize_poly: only the FP32 form is available");
+    return channelize_poly_fp(out, in, h, M, D, reinterpret_cast<cudaStream_t>(stream));
+  } catch (...) {
+    GBFIR_FAIL(GBFIR_ERR_CUDA, "channelize_poly: internal exception");
+  }
+}
+
+int gbfir_set_resample_tile(int32_t rows_per_thread, int32_t col_warps, int32_t group) {
+  int rc = set_resample_tile(rows_per_thread, col_warps, group);
+  if (rc) GBFIR_FAIL(rc, "set_resample_tile: invalid tile (%d, %d, %d)", rows_per_thread, col_warps, group);
+  return rc;
+}
+
+uint64_t gbfir_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+const char *gbfir_status_string(int status) {
+  switch (status) {
+    case GBFIR_SUCCESS: return "success";
+    case GBFIR_ERR_INVALID_PARAMETER: return "invalid parameter";
+    case GBFIR_ERR_INVALID_DIM: return "invalid dimension";
+    case GBFIR_ERR_INVALID_SIZE: return "invalid size";
+    case GBFIR_ERR_INVALID_TYPE: return "invalid type";
+    case GBFIR_ERR_NOT_SUPPORTED: return "not supported";
+    case GBFIR_ERR_CUDA: return "CUDA error";
+    case GBFIR_ERR_NULL_POINTER: return "null pointer";
+    case GBFIR_ERR_ALIGNMENT: return "misaligned pointer";
+    case GBFIR_ERR_WORKSPACE: return "workspace missing or too small";
+    case GBFIR_ERR_TIMEOUT: return "device wait timed out";
+    default: return "unknown status";
+  }
+}
+
+const char *gbfir_last_error(void) { return t_last_error.c_str(); }
+
+int gbfir_version(void) { return 100; }
+
+}  // extern "C"

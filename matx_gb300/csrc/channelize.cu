@@ -1,0 +1,438 @@
+// channelize.cu — fused polyphase channelizer (FIR branches + M-point DFT) for sm_103a.
+//
+// Semantics are MatX's channelize_poly (include/matx/transforms/channelize_poly.h:724-849
+// CUDA path, :858-1029 host path, include/matx/kernels/channelize_poly.cuh:134-310):
+//   D == M:  F[t][c] = sum_p h[p*M + c] * x[(t - p)*M + (M-1-c)]
+//   D <  M:  r' = (c + M - D) mod M, s = M-1-r', last = t*D + D - 1, A = last - s,
+//            newest = last - (A mod M), causal = A/M + 1, phase = (c + t*D) mod M,
+//            F[t][c] = sum_{p < min(P, causal)} h[phase + p*M] * x[newest - p*M]
+//   with h zero-padded to P*M (P = ceil(L/M)) and x zero outside [0, N), then
+//   Y[t][k] = sum_c F[t][c] * exp(+2*pi*i*c*k/M)  (unnormalised; MatX runs this
+//   as a separate in-place cuFFT ifft(FFTNorm::FORWARD) pass, channelize_poly.h:846).
+//
+// Schedule (no MatX counterpart).  One CTA owns TT consecutive output steps of
+// one row and all M channels, so the DFT never leaves shared memory: the input
+// window is staged once (cp.async, zero-filled), the branch filters write F into
+// shared memory, the DFT runs in shared memory/registers, and each output row
+// is stored once.  HBM traffic is 8 B in + 8 B out per output sample, against
+// 32 B for FIR-then-FFT.
+//   * FIR, D == M: a thread owns one channel and 8 consecutive steps; taps in
+//     blocks of 8 with a 16-sample register window (64 FMAs per 8 loads).
+//   * FIR, D <  M: one (step, channel) per thread iteration (phases rotate).
+//   * DFT, M = M1*M2 <= 256 (powers of two): four-step FFT, radix-M1 and radix-M2
+//     passes in registers, twiddle W_M^(c2*k1) between them, padded layouts so both
+//     passes are bank-conflict free.  Other M: direct DFT with a twiddle table.
+#include "common.cuh"
+
+namespace gbfir {
+
+constexpr int kChThreads = 256;
+constexpr int kChE = 8;
+
+struct ChParams {
+  const void *x;
+  int64_t x_bstride, N;
+  const void *h;
+  int64_t L;
+  void *out;
+  int64_t out_bstride;
+  int64_t M, D, P, Ppad, T;
+  int32_t TT;
+  int64_t tiles_per_row, ntiles;
+  int32_t W;           // window samples
+  int32_t tap_stride;  // D==M: row stride of the [c][p] tap table
+  int32_t Mf, Mp;      // F/Y row stride, A row stride
+  int32_t r2_elems;    // elements in region 2 (window / A / generic Y)
+};
+
+// W_16^k = exp(+2*pi*i*k/16), k = 0..7 (cos/sin of multiples of pi/8).
+template <typename T>
+__device__ __forceinline__ void w16(int k, T &c, T &s) {
+  const T a = T(0.92387953251128675613), b = T(0.38268343236508977173), r = T(0.70710678118654752440);
+  switch (k & 7) {
+    case 0: c = 1; s = 0; break;
+    case 1: c = a; s = b; break;
+    case 2: c = r; s = r; break;
+    case 3: c = b; s = a; break;
+    case 4: c = 0; s = 1; break;
+    case 5: c = -b; s = a; break;
+    case 6: c = -r; s = r; break;
+    default: c = -a; s = b; break;
+  }
+}
+
+template <int R>
+__host__ __device__ constexpr int bitrev(int i) {
+  int r = 0;
+  for (int b = 1; b < R; b <<= 1) {
+    r = (r << 1) | (i & 1);
+    i >>= 1;
+  }
+  return r;
+}
+
+// In-register radix-2 FFT, positive exponent: v[k] <- sum_n v[n] exp(+2*pi*i*n*k/R).
+template <typename T, int R>
+__device__ __forceinline__ void fft_reg(T (&re)[R], T (&im)[R]) {
+  if constexpr (R > 1) {
+#pragma unroll
+  for (int i = 0; i < R; i++) {
+    const int j = bitrev<R>(i);
+    if (j > i) {
+      T t = re[i]; re[i] = re[j]; re[j] = t;
+      t = im[i]; im[i] = im[j]; im[j] = t;
+    }
+  }
+#pragma unroll
+  for (int len = 2; len <= R; len <<= 1) {
+#pragma unroll
+    for (int i = 0; i < R; i += len) {
+#pragma unroll
+      for (int k = 0; k < len / 2; k++) {
+        T wc, ws;
+        w16<T>(k * (16 / len), wc, ws);
+        const int a = i + k, b = i + k + len / 2;
+        const T br = re[b] * wc - im[b] * ws;
+        const T bi = re[b] * ws + im[b] * wc;
+        re[b] = re[a] - br;
+        im[b] = im[a] - bi;
+        re[a] = re[a] + br;
+        im[a] = im[a] + bi;
+      }
+    }
+  }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void twiddle_of(int64_t m, int64_t M, T &c, T &s);
+template <>
+__device__ __forceinline__ void twiddle_of<float>(int64_t m, int64_t M, float &c, float &s) {
+  // exp(+2*pi*i*m/M); the argument 2m/M is reduced to [0, 2) exactly in integers first.
+  sincospif((float)(2 * m) / (float)M, &s, &c);
+}
+template <>
+__device__ __forceinline__ void twiddle_of<double>(int64_t m, int64_t M, double &c, double &s) {
+  sincospi((double)(2 * m) / (double)M, &s, &c);
+}
+
+// DFT kind: (M1, M2) with M = M1*M2; M1 == 0 selects the direct DFT.
+template <typename T, bool XC, bool HC, int M1, int M2>
+__global__ void __launch_bounds__(kChThreads) channelize_fused(const ChParams p) {
+  using XT = typename val_of<T, XC>::type;
+  using HT = typename val_of<T, HC>::type;
+  using CT = typename cplx_of<T>::type;
+  constexpr bool FC = XC || HC;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int M = (int)p.M;
+  const bool md = p.D == p.M;
+  // layout: [taps][twiddles][region 1: F / Y][region 2: window / A / generic Y]
+  const size_t tap_elems = md ? (size_t)M * p.tap_stride : (size_t)p.Ppad * M;
+  size_t off = (tap_elems * sizeof(HT) + 15) & ~(size_t)15;
+  HT *taps = reinterpret_cast<HT *>(smem_raw);
+  CT *tw = reinterpret_cast<CT *>(smem_raw + off);
+  off += ((size_t)M * sizeof(CT) + 15) & ~(size_t)15;
+  CT *r1 = reinterpret_cast<CT *>(smem_raw + off);
+  off += ((size_t)p.TT * p.Mf * sizeof(CT) + 15) & ~(size_t)15;
+  unsigned char *r2raw = smem_raw + off;
+  XT *win = reinterpret_cast<XT *>(r2raw);
+  CT *r2 = reinterpret_cast<CT *>(r2raw);
+
+  const int tid = threadIdx.x;
+  const HT *hp = reinterpret_cast<const HT *>(p.h);
+  const XT *xp = reinterpret_cast<const XT *>(p.x);
+  CT *op = reinterpret_cast<CT *>(p.out);
+
+  // taps: D==M -> [c][p] rows of tap_stride; D<M -> natural zero-padded P*M
+  for (size_t e = tid; e < tap_elems; e += kChThreads) {
+    HT v = zero_val<HT>();
+    if (md) {
+      const int c = (int)(e / p.tap_stride), pp = (int)(e - (size_t)c * p.tap_stride);
+      const int64_t idx = (int64_t)pp * M + c;
+      if (pp < p.P && idx < p.L) v = hp[idx];
+    } else if ((int64_t)e < p.L) {
+      v = hp[e];
+    }
+    taps[e] = v;
+  }
+  for (int m = tid; m < M; m += kChThreads) {
+    T c, s;
+    twiddle_of<T>(m, p.M, c, s);
+    tw[m].x = c;
+    tw[m].y = s;
+  }
+
+  for (int64_t tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x) {
+    const int64_t b = tile / p.tiles_per_row;
+    const int64_t t0 = (tile - b * p.tiles_per_row) * p.TT;
+    const XT *row = xp + b * p.x_bstride;
+    const int64_t w0 = t0 * p.D + p.D - (p.Ppad + 1) * p.M;
+    __syncthreads();  // previous tile fully stored, tables written
+    for (int e = tid; e < p.W; e += kChThreads) {
+      const int64_t gi = w0 + e;
+      const bool ok = gi >= 0 && gi < p.N;
+      cp_async_zfill<sizeof(XT)>(&win[e], ok ? (const void *)(row + gi) : (const void *)row, ok);
+    }
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+
+    // ---- FIR branch filters -> F in r1 ([TT][Mf]) ----
+    if (md) {
+      constexpr int E = kChE;
+      const int nitems = M * (p.TT / E);
+      const int Pp = (int)p.Ppad;
+      for (int w = tid; w < nitems; w += kChThreads) {
+        const int c = w % M, r = w / M;
+        const int sc = M - 1 - c;
+        Acc<T, FC> acc[E];
+#pragma unroll
+        for (int e = 0; e < E; e++) acc[e].zero();
+        const HT *th = taps + (size_t)c * p.tap_stride;
+        XT cur[E], prv[E];
+        int rowi = r * E + Pp;  // window row of (t = t0 + r*E, p = 0)
+#pragma unroll
+        for (int e = 0; e < E; e++) cur[e] = win[(rowi + e) * M + sc];
+        for (int kb = 0; kb < Pp; kb += E) {
+          rowi -= E;
+#pragma unroll
+          for (int e = 0; e < E; e++) prv[e] = win[(rowi + e) * M + sc];
+          HT t[E];
+#pragma unroll
+          for (int kk = 0; kk < E; kk++) t[kk] = th[kb + kk];
+#pragma unroll
+          for (int kk = 0; kk < E; kk++) {
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+              const XT xv = (e >= kk) ? cur[e - kk] : prv[E + e - kk];
+              mac<T, XC, HC>(acc[e], xv, t[kk]);
+            }
+          }
+#pragma unroll
+          for (int e = 0; e < E; e++) cur[e] = prv[e];
+        }
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+          CT v;
+          v.x = acc[e].re;
+          if constexpr (FC) v.y = acc[e].im;
+          else v.y = 0;
+          r1[(r * E + e) * p.Mf + c] = v;
+        }
+      }
+    } else {
+      const int nitems = M * p.TT;
+      for (int w = tid; w < nitems; w += kChThreads) {
+        const int c = w % M, tl = w / M;
+        const int64_t t = t0 + tl;
+        const int64_t rr = (c + p.M - p.D) % p.M;
+        const int64_t s = p.M - 1 - rr;
+        const int64_t last = t * p.D + p.D - 1;
+        Acc<T, FC> acc;
+        acc.zero();
+        if (last >= s) {
+          const int64_t A = last - s;
+          const int64_t newest = last - (A % p.M);
+          const int64_t causal = A / p.M + 1;
+          const int64_t phase = (c + t * p.D) % p.M;
+          const int64_t niter = min(p.P, causal);
+          int widx = (int)(newest - w0);
+          int hidx = (int)phase;
+          for (int64_t i = 0; i < niter; i++) {
+            mac<T, XC, HC>(acc, win[widx], taps[hidx]);
+            widx -= M;
+            hidx += M;
+          }
+        }
+        CT v;
+        v.x = acc.re;
+        if constexpr (FC) v.y = acc.im;
+        else v.y = 0;
+        r1[tl * p.Mf + c] = v;
+      }
+    }
+    __syncthreads();
+
+    // ---- M-point DFT ----
+    CT *ybuf = r1;
+    if constexpr (M1 > 0) {
+      // step 1: radix-M1 over c1 for each (t, c2); twiddle; A[t][k1*(M2+1) + c2]
+      const int n1 = p.TT * M2;
+      for (int w = tid; w < n1; w += kChThreads) {
+        const int c2 = w % M2, tl = w / M2;
+        T re[M1], im[M1];
+#pragma unroll
+        for (int c1 = 0; c1 < M1; c1++) {
+          const CT v = r1[tl * p.Mf + M2 * c1 + c2];
+          re[c1] = v.x;
+          im[c1] = v.y;
+        }
+        fft_reg<T, M1>(re, im);
+#pragma unroll
+        for (int k1 = 0; k1 < M1; k1++) {
+          CT v;
+          if (M2 > 1 && k1 > 0 && c2 > 0) {
+            const CT wv = tw[c2 * k1];
+            v.x = re[k1] * wv.x - im[k1] * wv.y;
+            v.y = re[k1] * wv.y + im[k1] * wv.x;
+          } else {
+            v.x = re[k1];
+            v.y = im[k1];
+          }
+          r2[tl * p.Mp + k1 * (M2 + 1) + c2] = v;
+        }
+      }
+      __syncthreads();
+      // step 2: radix-M2 over c2 for each (t, k1); Y[t][k1 + M1*k2] into r1
+      const int n2 = p.TT * M1;
+      for (int w = tid; w < n2; w += kChThreads) {
+        const int k1 = w % M1, tl = w / M1;
+        T re[M2], im[M2];
+#pragma unroll
+        for (int c2 = 0; c2 < M2; c2++) {
+          const CT v = r2[tl * p.Mp + k1 * (M2 + 1) + c2];
+          re[c2] = v.x;
+          im[c2] = v.y;
+        }
+        fft_reg<T, M2>(re, im);
+#pragma unroll
+        for (int k2 = 0; k2 < M2; k2++) {
+          CT v;
+          v.x = re[k2];
+          v.y = im[k2];
+          r1[tl * p.Mf + k1 + M1 * k2] = v;
+        }
+      }
+    } else {
+      // direct DFT: Y[t][k] = sum_c F[t][c] * tw[(c*k) mod M], into r2
+      const int n2 = p.TT * M;
+      for (int w = tid; w < n2; w += kChThreads) {
+        const int k = w % M, tl = w / M;
+        T ar = 0, ai = 0;
+        int idx = 0;
+        for (int c = 0; c < M; c++) {
+          const CT f = r1[tl * p.Mf + c];
+          const CT wv = tw[idx];
+          ar = fma(f.x, wv.x, ar);
+          ar = fma(-f.y, wv.y, ar);
+          ai = fma(f.x, wv.y, ai);
+          ai = fma(f.y, wv.x, ai);
+          idx += k;
+          if (idx >= M) idx -= M;
+        }
+        CT v;
+        v.x = ar;
+        v.y = ai;
+        r2[tl * p.Mf + k] = v;
+      }
+      ybuf = r2;
+    }
+    __syncthreads();
+
+    // ---- store rows t0 .. t0+TT-1 (contiguous [TT][M] block of the output row) ----
+    const int64_t nrows = min((int64_t)p.TT, p.T - t0);
+    CT *orow = op + b * p.out_bstride + t0 * p.M;
+    const int64_t nel = nrows * p.M;
+    for (int64_t e = tid; e < nel; e += kChThreads) {
+      const int64_t tl = e / M, k = e - tl * M;
+      orow[e] = ybuf[tl * p.Mf + k];
+    }
+  }
+}
+
+template <typename T, bool XC, bool HC, int M1, int M2>
+static int launch_ch(ChParams &p, int64_t batch, cudaStream_t s) {
+  using XT = typename val_of<T, XC>::type;
+  using HT = typename val_of<T, HC>::type;
+  using CT = typename cplx_of<T>::type;
+  const bool md = p.D == p.M;
+  const int M = (int)p.M;
+  p.Mf = (M1 > 0 && M2 < 16) ? M + M2 : M;
+  if (M1 == 0) p.Mf = M;
+  p.Mp = M1 > 0 ? M1 * (M2 + 1) : 0;
+  p.tap_stride = md ? (int)(p.Ppad + ((p.Ppad % 8) == 0 ? 4 : 0)) : 0;
+  const size_t tap_elems = md ? (size_t)M * p.tap_stride : (size_t)p.Ppad * M;
+  auto smem_for = [&](int TT, int32_t &W, int32_t &r2e) -> size_t {
+    W = (int32_t)((TT - 1) * p.D + (p.Ppad + 1) * p.M);
+    size_t r2b = (size_t)W * sizeof(XT);
+    const size_t ab = (size_t)TT * (M1 > 0 ? p.Mp : p.Mf) * sizeof(CT);
+    if (ab > r2b) r2b = ab;
+    r2e = (int32_t)(r2b / sizeof(XT));
+    size_t sz = ((tap_elems * sizeof(HT) + 15) & ~(size_t)15) + (((size_t)M * sizeof(CT) + 15) & ~(size_t)15) +
+                (((size_t)TT * p.Mf * sizeof(CT) + 15) & ~(size_t)15) + r2b;
+    return sz;
+  };
+  int TT = 64;
+  int32_t W = 0, r2e = 0;
+  size_t smem = smem_for(TT, W, r2e);
+  while (TT > kChE && smem > 100 * 1024) {
+    TT -= kChE;
+    smem = smem_for(TT, W, r2e);
+  }
+  if (smem > 220 * 1024)
+    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "channelize_poly: M=%lld, P=%lld needs %zu B of shared memory per tile",
+               (long long)p.M, (long long)p.P, smem);
+  p.TT = TT;
+  p.W = W;
+  p.r2_elems = r2e;
+  p.tiles_per_row = (p.T + TT - 1) / TT;
+  p.ntiles = p.tiles_per_row * batch;
+  auto fn = channelize_fused<T, XC, HC, M1, M2>;
+  int rc = ensure_smem((const void *)fn, smem, "channelize_poly");
+  if (rc) return rc;
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kChThreads, smem);
+  if (occ < 1) occ = 1;
+  int64_t grid = (int64_t)num_sms() * occ;
+  if (grid > p.ntiles) grid = p.ntiles;
+  fn<<<(unsigned)grid, kChThreads, smem, s>>>(p);
+  return check_launch("channelize_poly");
+}
+
+template <typename T, bool XC, bool HC>
+static int dispatch_ch(ChParams &p, int64_t batch, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    switch (p.M) {
+      case 2: return launch_ch<T, XC, HC, 2, 1>(p, batch, s);
+      case 4: return launch_ch<T, XC, HC, 4, 1>(p, batch, s);
+      case 8: return launch_ch<T, XC, HC, 8, 1>(p, batch, s);
+      case 16: return launch_ch<T, XC, HC, 16, 1>(p, batch, s);
+      case 32: return launch_ch<T, XC, HC, 8, 4>(p, batch, s);
+      case 64: return launch_ch<T, XC, HC, 8, 8>(p, batch, s);
+      case 128: return launch_ch<T, XC, HC, 16, 8>(p, batch, s);
+      case 256: return launch_ch<T, XC, HC, 16, 16>(p, batch, s);
+      default: break;
+    }
+  }
+  return launch_ch<T, XC, HC, 0, 0>(p, batch, s);
+}
+
+int channelize_poly_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t M, int64_t D,
+                       cudaStream_t s) {
+  ChParams p{};
+  p.x = in.ptr;
+  p.x_bstride = in.batch > 1 ? in.batch_stride : 0;
+  p.N = in.len;
+  p.h = h.ptr;
+  p.L = h.len;
+  p.out = out.ptr;
+  p.out_bstride = out.batch_stride;
+  p.M = M;
+  p.D = D;
+  p.P = (h.len + M - 1) / M;
+  p.Ppad = (p.P + kChE - 1) / kChE * kChE;
+  p.T = (in.len + D - 1) / D;
+  const bool xc = dtype_complex(in.dtype), hc = dtype_complex(h.dtype);
+  if (dtype_double(in.dtype)) {
+    if (xc && hc) return dispatch_ch<double, true, true>(p, out.batch, s);
+    if (xc) return dispatch_ch<double, true, false>(p, out.batch, s);
+    if (hc) return dispatch_ch<double, false, true>(p, out.batch, s);
+    return dispatch_ch<double, false, false>(p, out.batch, s);
+  }
+  if (xc && hc) return dispatch_ch<float, true, true>(p, out.batch, s);
+  if (xc) return dispatch_ch<float, true, false>(p, out.batch, s);
+  if (hc) return dispatch_ch<float, false, true>(p, out.batch, s);
+  return dispatch_ch<float, false, false>(p, out.batch, s);
+}
+
+}  // namespace gbfir

@@ -1,0 +1,118 @@
+"""CPU-side checks of the C-ABI library: it loads, exports every symbol the
+header declares, and its host-side validation returns the MatX error classes
+before any device work (fake, never-dereferenced pointers)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import __graft_entry__ as g
+    from matx_gb300 import build
+    build.build()
+    from matx_gb300 import _lib
+    return _lib.load()
+
+
+def header_functions():
+    names = []
+    for fn in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if not fn.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", fn)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"\b(gbfir_[a-z0-9_]+)\s*\(", text)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = header_functions()
+    for must in ("gbfir_conv1d", "gbfir_resample_poly", "gbfir_channelize_poly"):
+        assert must in names
+
+
+def test_every_header_symbol_is_exported(lib):
+    from matx_gb300 import _lib
+    bound = {n for n, _, _ in _lib.SIGNATURES}
+    for name in header_functions():
+        assert hasattr(lib, name), f"{name} not exported"
+        assert name in bound, f"{name} has no ctypes signature"
+
+
+def test_status_strings(lib):
+    assert lib.gbfir_status_string(0) == b"success"
+    assert lib.gbfir_status_string(2) == b"invalid dimension"
+    assert lib.gbfir_version() >= 100
+
+
+FAKE = 0x100000  # aligned, never dereferenced: validation fails first
+
+
+def buf(n, batch=1, dtype=1, stride=None, ptr=FAKE):
+    from matx_gb300._lib import Buf
+    return Buf(ptr, batch, n, n if stride is None else stride, dtype)
+
+
+def last(lib):
+    return lib.gbfir_last_error().decode()
+
+
+def test_resample_validation(lib):
+    # output length must be ceil(N*up/down) with unreduced up/down (resample_poly.h:318-320)
+    assert lib.gbfir_resample_poly(buf(100), buf(67), buf(61, dtype=0), 3, 2, 0, None) == 2
+    assert "output size mismatch" in last(lib)
+    assert lib.gbfir_resample_poly(buf(101), buf(67), buf(61, dtype=0), 0, 2, 0, None) == 1
+    assert lib.gbfir_resample_poly(buf(101), buf(67), buf(61, dtype=0), 3, -1, 0, None) == 1
+    # batch mismatch
+    assert lib.gbfir_resample_poly(buf(101, batch=2), buf(67, batch=3), buf(61, dtype=0), 3, 2, 0, None) == 2
+    # null pointer
+    assert lib.gbfir_resample_poly(buf(101, ptr=0), buf(67), buf(61, dtype=0), 3, 2, 0, None) == 7
+    # complex input needs complex output
+    assert lib.gbfir_resample_poly(buf(101, dtype=0), buf(67), buf(61, dtype=0), 3, 2, 0, None) == 4
+    # misaligned complex pointer
+    assert lib.gbfir_resample_poly(buf(101, ptr=FAKE + 4), buf(67), buf(61, dtype=0), 3, 2, 0, None) == 8
+    # unknown precision
+    assert lib.gbfir_resample_poly(buf(101), buf(67), buf(61, dtype=0), 3, 2, 9, None) == 1
+    # filter must be one row
+    assert lib.gbfir_resample_poly(buf(101), buf(67), buf(61, batch=2, dtype=0), 3, 2, 0, None) == 2
+
+
+def test_conv_validation(lib):
+    assert lib.gbfir_conv1d(buf(100, dtype=0), buf(64, dtype=0), buf(16, dtype=0), 0, 0, 0, None) == 3
+    assert lib.gbfir_conv1d(buf(79, dtype=0), buf(64, dtype=0), buf(16, dtype=0), 3, 0, 0, None) == 1
+    # SAME is max(N, L), VALID is max-min+1 — wrong sizes rejected
+    assert lib.gbfir_conv1d(buf(63, dtype=0), buf(64, dtype=0), buf(16, dtype=0), 1, 0, 0, None) == 3
+    assert lib.gbfir_conv1d(buf(48, dtype=0), buf(64, dtype=0), buf(16, dtype=0), 2, 0, 0, None) == 3
+    # batch mismatch between operands and output
+    assert lib.gbfir_conv1d(buf(79, batch=4, dtype=0), buf(64, batch=3, dtype=0), buf(16, dtype=0),
+                            0, 0, 0, None) == 2
+    # mixed precision operands
+    assert lib.gbfir_conv1d(buf(79, dtype=0), buf(64, dtype=2), buf(16, dtype=0), 0, 0, 0, None) == 4
+
+
+def test_channelize_validation(lib):
+    # D > M
+    assert lib.gbfir_channelize_poly(buf(16 * 8), buf(128), buf(64, dtype=0), 8, 9, 0, None) == 1
+    # output row must hold T*M
+    assert lib.gbfir_channelize_poly(buf(16 * 8 + 1), buf(128), buf(64, dtype=0), 8, 8, 0, None) == 2
+    # output must be complex even for real inputs
+    assert lib.gbfir_channelize_poly(buf(128, dtype=0), buf(128, dtype=0), buf(64, dtype=0), 8, 8, 0, None) == 4
+    assert lib.gbfir_channelize_poly(buf(128), buf(128), buf(64, dtype=0), 0, 1, 0, None) == 1
+
+
+def test_resample_tile_hook(lib):
+    assert lib.gbfir_set_resample_tile(3, 1, 1) == 1
+    assert lib.gbfir_set_resample_tile(2, 4, 1) == 0
+    assert lib.gbfir_set_resample_tile(0, 0, 0) == 0
+
+
+def test_package_refuses_cpu_tensors():
+    import torch
+    import matx_gb300 as mx
+    with pytest.raises(ValueError):
+        mx.resample_poly(torch.zeros(10, dtype=torch.complex64), torch.zeros(5), 3, 2)
