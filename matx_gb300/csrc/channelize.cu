@@ -340,6 +340,114 @@ __global__ void __launch_bounds__(kChThreads) channelize_fused(const ChParams p)
   }
 }
 
+// ---- split path for large M*P: FIR into the output, then an in-place row DFT ----
+// Used when the fused tile does not fit in shared memory.  The FIR reads x and h
+// through L1 (lanes over channels read consecutive samples), writes F[t][c] into
+// the output buffer, and a second kernel replaces each row by its M-point DFT.
+template <typename T, bool XC, bool HC>
+__global__ void __launch_bounds__(kChThreads) channelize_fir_split(const ChParams p) {
+  using XT = typename val_of<T, XC>::type;
+  using HT = typename val_of<T, HC>::type;
+  using CT = typename cplx_of<T>::type;
+  constexpr bool FC = XC || HC;
+  const XT *xp = reinterpret_cast<const XT *>(p.x);
+  const HT *hp = reinterpret_cast<const HT *>(p.h);
+  CT *op = reinterpret_cast<CT *>(p.out);
+  const int64_t per_row = p.T * p.M;
+  const int64_t total = per_row * p.ntiles;  // ntiles == batch on this path
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / per_row, r = e - b * per_row;
+    const int64_t t = r / p.M, c = r - t * p.M;
+    const XT *row = xp + b * p.x_bstride;
+    const int64_t rr = (c + p.M - p.D) % p.M;
+    const int64_t s = p.M - 1 - rr;
+    const int64_t last = t * p.D + p.D - 1;
+    Acc<T, FC> acc;
+    acc.zero();
+    if (last >= s) {
+      const int64_t A = last - s;
+      int64_t idx = last - (A % p.M);
+      const int64_t causal = A / p.M + 1;
+      int64_t hidx = (p.D == p.M) ? c : (c + t * p.D) % p.M;
+      const int64_t niter = min(p.P, causal);
+      for (int64_t i = 0; i < niter; i++, idx -= p.M, hidx += p.M) {
+        if (idx < p.N && hidx < p.L) mac<T, XC, HC>(acc, row[idx], hp[hidx]);
+      }
+    }
+    CT v;
+    v.x = acc.re;
+    if constexpr (FC) v.y = acc.im;
+    else v.y = 0;
+    op[b * p.out_bstride + r] = v;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kChThreads) dft_rows_inplace(void *out, int64_t out_bstride, int64_t T_rows,
+                                                               int64_t M, int64_t batch) {
+  using CT = typename cplx_of<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  CT *tw = reinterpret_cast<CT *>(smem_raw);
+  CT *rowbuf = tw + M;
+  for (int m = threadIdx.x; m < M; m += kChThreads) {
+    T c, s;
+    twiddle_of<T>(m, M, c, s);
+    tw[m].x = c;
+    tw[m].y = s;
+  }
+  CT *op = reinterpret_cast<CT *>(out);
+  const int64_t nrows = T_rows * batch;
+  for (int64_t rix = blockIdx.x; rix < nrows; rix += gridDim.x) {
+    const int64_t b = rix / T_rows, t = rix - b * T_rows;
+    CT *row = op + b * out_bstride + t * M;
+    __syncthreads();
+    for (int m = threadIdx.x; m < M; m += kChThreads) rowbuf[m] = row[m];
+    __syncthreads();
+    for (int k = threadIdx.x; k < M; k += kChThreads) {
+      T ar = 0, ai = 0;
+      int idx = 0;
+      for (int c = 0; c < M; c++) {
+        const CT f = rowbuf[c];
+        const CT wv = tw[idx];
+        ar = fma(f.x, wv.x, ar);
+        ar = fma(-f.y, wv.y, ar);
+        ai = fma(f.x, wv.y, ai);
+        ai = fma(f.y, wv.x, ai);
+        idx += k;
+        if (idx >= M) idx -= M;
+      }
+      CT v;
+      v.x = ar;
+      v.y = ai;
+      row[k] = v;
+    }
+  }
+}
+
+template <typename T, bool XC, bool HC>
+static int launch_split(ChParams &p, int64_t batch, cudaStream_t s) {
+  using CT = typename cplx_of<T>::type;
+  p.ntiles = batch;
+  const int64_t total = p.T * p.M * batch;
+  int64_t grid = (total + kChThreads - 1) / kChThreads;
+  const int64_t cap = (int64_t)num_sms() * 8;
+  if (grid > cap) grid = cap;
+  channelize_fir_split<T, XC, HC><<<(unsigned)grid, kChThreads, 0, s>>>(p);
+  int rc = check_launch("channelize_poly (split FIR)");
+  if (rc) return rc;
+  const size_t smem = 2 * (size_t)p.M * sizeof(CT);
+  if (smem > 200 * 1024)
+    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "channelize_poly: M=%lld is too large for the row DFT", (long long)p.M);
+  auto fn = dft_rows_inplace<T>;
+  rc = ensure_smem((const void *)fn, smem, "channelize_poly");
+  if (rc) return rc;
+  int64_t g2 = p.T * batch;
+  const int64_t cap2 = (int64_t)num_sms() * 4;
+  if (g2 > cap2) g2 = cap2;
+  fn<<<(unsigned)g2, kChThreads, smem, s>>>(p.out, p.out_bstride, p.T, p.M, batch);
+  return check_launch("channelize_poly (row DFT)");
+}
+
 template <typename T, bool XC, bool HC, int M1, int M2>
 static int launch_ch(ChParams &p, int64_t batch, cudaStream_t s) {
   using XT = typename val_of<T, XC>::type;
@@ -369,9 +477,7 @@ static int launch_ch(ChParams &p, int64_t batch, cudaStream_t s) {
     TT -= kChE;
     smem = smem_for(TT, W, r2e);
   }
-  if (smem > 220 * 1024)
-    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "channelize_poly: M=%lld, P=%lld needs %zu B of shared memory per tile",
-               (long long)p.M, (long long)p.P, smem);
+  if (smem > 200 * 1024) return launch_split<T, XC, HC>(p, batch, s);
   p.TT = TT;
   p.W = W;
   p.r2_elems = r2e;
