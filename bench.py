@@ -193,6 +193,7 @@ def run_reference(args, rank, world):
 
 
 def main():
+    global BATCH
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -204,7 +205,6 @@ def main():
     ap.add_argument("--batch", type=int, default=BATCH, help="rows per GPU (profiling cases)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    global BATCH
     BATCH = args.batch
 
     rank = int(os.environ.get("RANK", "0"))
