@@ -19,6 +19,8 @@ Sources, all from the reference's own test suite:
 * harris2003.npz — the maximally decimated known-answer test whose filter,
   input and output are written inline in test/00_transform/ChannelizePoly.cu:820-1100
   (M = 10), parsed from that file as text.
+* grad_refs.npz — adjoints of conv1d (all modes) and resample_poly composed from MatX's
+  own HostExecutor corr / resample_poly in double (oracle/_ref), on seeded inputs.
 * harris2003_oversampled.npz — the M=40, D=28 oversampled case: input and golden
   output from test/test_vectors/channelize_poly/harris2003_oversampled_testvector.bin,
   filter from the generator's remez design (00_transforms.py:336-397).
@@ -184,7 +186,45 @@ def make_harris():
     return h.size, x.size, y.shape
 
 
+def make_grad_refs():
+    """Gradients composed from MatX's own host operators (oracle/_ref, FP64):
+    conv1d:   dx = corr(gy, h, FULL)[L-1-start : L-1-start+N]
+              dh[f] = sum_b corr(x_b, gy_b, FULL)[Ly-1+start-f]
+    resample: dx = (up/down) * resample_poly(gy, reverse(h), down, up)[:N]  (odd L)
+    for y = conv1d(x, h, mode) / resample_poly(x, h, up, down) and a seeded gy."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    import oracle
+    oracle.build(ref=True)
+    rng = np.random.default_rng(77)
+    B, N, L = 4, 1000, 127
+    x = rng.uniform(-1, 1, (B, N))
+    h = rng.standard_normal(L) / np.sqrt(L)
+    out = {"x": x, "h": h}
+    for mode, name in ((0, "full"), (1, "same"), (2, "valid")):
+        Ly = N + L - 1 if mode == 0 else (N if mode == 1 else N - L + 1)
+        start = 0 if mode == 0 else ((L - 1) // 2 if mode == 1 else L - 1)
+        gy = rng.standard_normal((B, Ly))
+        cf = oracle.ref_conv1d(gy, h, 0, is_corr=True, double=True)
+        dx = cf[:, L - 1 - start: L - 1 - start + N]
+        dh = np.zeros(L)
+        for b in range(B):
+            c2 = oracle.ref_conv1d(x[b], gy[b], 0, is_corr=True, double=True)[0]
+            dh += c2[Ly - 1 + start - np.arange(L)]
+        out[f"conv_{name}__gy"] = gy
+        out[f"conv_{name}__dx"] = dx
+        out[f"conv_{name}__dh"] = dh
+    for up, down in ((3, 2), (2, 3), (4, 5)):
+        Ly = (N * up + down - 1) // down
+        gy = rng.standard_normal((B, Ly))
+        t = oracle.ref_resample_poly(gy, h[::-1].copy(), down, up, double=True)
+        out[f"rs_{up}_{down}__gy"] = gy
+        out[f"rs_{up}_{down}__dx"] = (up / down) * t[:, :N]
+    np.savez_compressed(os.path.join(HERE, "grad_refs.npz"), **out)
+    return len(out)
+
+
 def main():
+    print("grad refs", make_grad_refs())
     T = _gen()
     print("conv cases", make_conv(T))
     print("resample cases", make_resample(T))

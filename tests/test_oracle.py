@@ -219,3 +219,18 @@ def test_conv_adjoint_oracle_fd(oracle_mod, mode, L):
         hp[k] += eps
         hm[k] -= eps
         assert abs((f(x, hp) - f(x, hm)) / (2 * eps) - dh[k]) < 1e-6
+
+
+def test_adjoint_oracle_matches_matx_built_gradients(oracle_mod):
+    # grad_refs.npz: gradients composed from MatX's own corr / resample_poly (FP64)
+    import os
+    from conftest import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "grad_refs.npz"))
+    x, h = z["x"], z["h"]
+    for mode, name in ((0, "full"), (1, "same"), (2, "valid")):
+        dx, dh = oracle_mod.conv1d_bwd(z[f"conv_{name}__gy"], x, h, mode)
+        assert rel_l2(dx, z[f"conv_{name}__dx"]) < 1e-12
+        assert rel_l2(dh, z[f"conv_{name}__dh"]) < 1e-12
+    for up, down in ((3, 2), (2, 3), (4, 5)):
+        dx, _ = oracle_mod.resample_poly_bwd(z[f"rs_{up}_{down}__gy"], x, h, up, down)
+        assert rel_l2(dx, z[f"rs_{up}_{down}__dx"]) < 1e-12
