@@ -71,37 +71,49 @@ def alg_bytes(n_in, L, up, down, batch):
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling (200 ms) around the timed region; only rows written after
+    mark() are summarised."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int, path: str | None):
+    def __init__(self, gpu_index: int):
+        import tempfile
         self.p = None
-        self.path = path
-        self.gpu = gpu_index
+        self.offset = 0
+        self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         try:
-            self.f = open(path, "w") if path else subprocess.PIPE
             self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.Q}",
                                        "--format=csv,noheader,nounits", "-lms", "200"],
-                                      stdout=self.f, stderr=subprocess.DEVNULL, text=True)
+                                      stdout=self.tmp, stderr=subprocess.DEVNULL, text=True)
+            t0 = time.time()
+            while time.time() - t0 < 10 and os.path.getsize(self.tmp.name) == 0:
+                time.sleep(0.05)
         except Exception:
             self.p = None
+
+    def mark(self):
+        self.tmp.flush()
+        self.offset = os.path.getsize(self.tmp.name)
 
     def stop(self):
         if self.p is None:
             return None
+        time.sleep(0.25)  # let the sampler write the last row of the timed region
         self.p.terminate()
         try:
-            out, _ = self.p.communicate(timeout=5)
+            self.p.wait(timeout=5)
         except Exception:
             self.p.kill()
-            out = ""
-        if self.path:
-            self.f.close()
-            out = open(self.path).read()
-        rows = [r.split(",") for r in (out or "").strip().splitlines() if r.strip()]
+        with open(self.tmp.name) as f:
+            f.seek(self.offset)
+            out = f.read()
+        try:
+            os.unlink(self.tmp.name)
+        except OSError:
+            pass
+        rows = [r.split(",") for r in out.strip().splitlines() if r.strip()]
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in rows:
@@ -196,7 +208,7 @@ def main():
     global BATCH
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp32")
@@ -246,11 +258,12 @@ def main():
     barrier()
 
     # ---- device-resident timed region -----------------------------------------------
-    clocks = Clocks(local, None)
+    clocks = Clocks(local)
     ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in RATIOS]
           for _ in range(args.steps)]
     e_start, e_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
+    clocks.mark()
     l0 = mx.launch_count()
     e_start.record(stream)
     for k in range(args.steps):

@@ -106,9 +106,9 @@ def launch_count() -> int:
     return int(_lib.load().gbfir_launch_count())
 
 
-def set_resample_tile(rows_per_thread: int = 0, col_warps: int = 0, group: int = 0):
-    """Force a resample_poly tile shape (0, 0, 0 restores the heuristic)."""
-    _lib.check(_lib.load().gbfir_set_resample_tile(rows_per_thread, col_warps, group))
+def set_resample_tile(rows_per_thread: int = 0, col_warps: int = 0, group: int = 0, buffers: int = 0):
+    """Force a resample_poly tile shape (zeros restore the heuristic)."""
+    _lib.check(_lib.load().gbfir_set_resample_tile(rows_per_thread, col_warps, group, buffers))
 
 
 def conv1d(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torch.Tensor | None = None,

@@ -55,7 +55,7 @@ SIGNATURES = [
     ("gbfir_ragged_workspace_size", _sz, [_i64, _i64]),
     ("gbfir_ragged_plan", _i64, [_p, _i64, _i32, _p]),
     ("gbfir_ragged_resample", ctypes.c_int, [_p, _i64, _p, _i64, _i32, _i32, _p, _sz, _p]),
-    ("gbfir_set_resample_tile", ctypes.c_int, [_i32, _i32, _i32]),
+    ("gbfir_set_resample_tile", ctypes.c_int, [_i32, _i32, _i32, _i32]),
     ("gbfir_launch_count", ctypes.c_uint64, []),
     ("gbfir_status_string", ctypes.c_char_p, [ctypes.c_int]),
     ("gbfir_last_error", ctypes.c_char_p, []),

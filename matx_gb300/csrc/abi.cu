@@ -21,7 +21,7 @@ int channelize_poly_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_bu
                        cudaStream_t s);
 int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t up, int64_t down,
                      int precision, cudaStream_t s);
-int set_resample_tile(int rq, int wc, int group);
+int set_resample_tile(int rq, int wc, int group, int nbuf);
 
 static thread_local std::string t_last_error;
 static std::atomic<uint64_t> g_launches{0};
@@ -200,9 +200,10 @@ int gbfir_channelize_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t M, i
   }
 }
 
-int gbfir_set_resample_tile(int32_t rows_per_thread, int32_t col_warps, int32_t group) {
-  int rc = set_resample_tile(rows_per_thread, col_warps, group);
-  if (rc) GBFIR_FAIL(rc, "set_resample_tile: invalid tile (%d, %d, %d)", rows_per_thread, col_warps, group);
+int gbfir_set_resample_tile(int32_t rows_per_thread, int32_t col_warps, int32_t group, int32_t buffers) {
+  int rc = set_resample_tile(rows_per_thread, col_warps, group, buffers);
+  if (rc)
+    GBFIR_FAIL(rc, "set_resample_tile: invalid tile (%d, %d, %d, %d)", rows_per_thread, col_warps, group, buffers);
   return rc;
 }
 

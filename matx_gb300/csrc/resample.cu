@@ -12,7 +12,7 @@
 namespace gbfir {
 
 // Resample tile override set by the autotuner hook.
-static int g_rq_override = 0, g_wc_override = 0, g_group_override = 0;
+static int g_rq_override = 0, g_wc_override = 0, g_group_override = 0, g_nbuf_override = 0;
 
 // Identity (up == down after the gcd): out = in, with real->complex widening.
 template <typename T, bool XC, bool OC>
@@ -46,6 +46,7 @@ static int run_resample(const gbfir_buf &out, const gbfir_buf &in, const gbfir_b
   tc.rq = g_rq_override;
   tc.wc = g_wc_override;
   tc.group = g_group_override;
+  tc.nbuf = g_nbuf_override;
   return resample_pass<T, XC, HC>(in.ptr, in.batch_stride, in.len, h.ptr, h.len, out.ptr, out.batch_stride, out.len,
                                   out.batch, up, down, -1, true, 0, (double)up, tc, s);
 }
@@ -87,13 +88,15 @@ int resample_poly_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf 
   return run_resample<float, false, false>(out, in, h, up, down, s);
 }
 
-int set_resample_tile(int rq, int wc, int group) {
+int set_resample_tile(int rq, int wc, int group, int nbuf) {
+  if (nbuf != 0 && nbuf != 1 && nbuf != 2) return GBFIR_ERR_INVALID_PARAMETER;
   if (rq != 0 && rq != 1 && rq != 2 && rq != 4) return GBFIR_ERR_INVALID_PARAMETER;
   if (wc != 0 && wc != 1 && wc != 2 && wc != 4 && wc != 8) return GBFIR_ERR_INVALID_PARAMETER;
   if (group < 0 || group > 64) return GBFIR_ERR_INVALID_PARAMETER;
   g_rq_override = rq;
   g_wc_override = wc;
   g_group_override = group;
+  g_nbuf_override = nbuf;
   return GBFIR_SUCCESS;
 }
 

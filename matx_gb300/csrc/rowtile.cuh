@@ -5,10 +5,13 @@
 // inputs from q*S + k with S = down*G, so every row sees the same tap matrix
 // B[k][j] = he[c + j*down - k*up].  The columns j are cut into groups of 4
 // adjacent phases; group g only needs the band k in [kl0(g), kl0(g)+span) (its
-// union band), stored in shared memory as one 4-vector of taps per k.  A warp's
-// 32 lanes take 32 different rows of the same column group, so the tap read is
-// a warp-wide broadcast and each input sample read from shared memory feeds
-// 4 phases x RQ rows of FMAs.  A persistent CTA walks tiles of QC rows; the next
+// union band), stored in shared memory as one 4-vector of taps per k.  A thread
+// owns 8 adjacent phases (two bands, the second starting d samples later) of RQ
+// rows and walks the union of the two bands in three ranges (A only, both, B
+// only), so each input sample read from shared memory feeds up to 8 phases x RQ
+// rows of FMAs with no multiply by a padding zero between the bands.  A warp's
+// 32 lanes take 32 different rows of the same phases, so tap reads are warp-wide
+// broadcasts.  A persistent CTA walks tiles of QC rows; with nbuf = 2 the next
 // tile's input window is prefetched with cp.async (zero-filled outside the
 // signal) while the current one is computed.
 //
@@ -40,6 +43,7 @@ struct RsParams {
   int32_t win_alloc; // shared elements per window buffer (with padding)
   double scale;      // output scale (up for resample_poly)
   int32_t rev;       // read taps reversed
+  int32_t nbuf;      // 2: prefetch the next tile's window while computing; 1: single buffer
 };
 
 template <typename T, bool HC>
@@ -105,6 +109,7 @@ __global__ void __launch_bounds__(256) resample_rowtile(const RsParams p) {
     }
   };
 
+  const bool dbuf = p.nbuf == 2;
   int64_t tile = blockIdx.x;
   if (tile < p.ntiles) issue_loads(tile, xbuf0);
   cp_async_commit();
@@ -112,14 +117,18 @@ __global__ void __launch_bounds__(256) resample_rowtile(const RsParams p) {
   const int wid = tid >> 5, lane = tid & 31;
   const int wr = wid / p.WC, wc = wid - wr * p.WC;
   const T scale = T(p.scale);
+  const int nsg = (p.ncg + 1) / 2;  // super-groups of 8 phases = two 4-phase bands
 
   for (int it = 0; tile < p.ntiles; tile += gridDim.x, ++it) {
-    XT *cur = (it & 1) ? xbuf1 : xbuf0;
-    XT *nxt = (it & 1) ? xbuf0 : xbuf1;
+    XT *cur = (dbuf && (it & 1)) ? xbuf1 : xbuf0;
     const int64_t next = tile + gridDim.x;
-    if (next < p.ntiles) issue_loads(next, nxt);
-    cp_async_commit();
-    cp_async_wait<1>();
+    if (dbuf) {
+      if (next < p.ntiles) issue_loads(next, (it & 1) ? xbuf0 : xbuf1);
+      cp_async_commit();
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
     __syncthreads();
 
     const int64_t b = tile / p.tiles_per_row;
@@ -127,21 +136,27 @@ __global__ void __launch_bounds__(256) resample_rowtile(const RsParams p) {
     OT *orow = op + b * p.out_bstride;
     const int rbase = wr * 32 * RQ + lane;  // local row of slice i is rbase + 32*i
 
-    for (int g = wc; g < p.ncg; g += p.WC) {
-      const int64_t kl0 = ceil_div(p.c + 4 * (int64_t)g * p.down - p.Lo + 1, p.up);
-      const int kb = (int)(kl0 - p.kmin);
+    for (int sg = wc; sg < nsg; sg += p.WC) {
+      const int gA = 2 * sg, gB = 2 * sg + 1;
+      const bool hasB = gB < p.ncg;
+      const int oA = (int)(ceil_div(p.c + 4 * (int64_t)gA * p.down - p.Lo + 1, p.up) - p.kmin);
+      const int oB = hasB ? (int)(ceil_div(p.c + 4 * (int64_t)gB * p.down - p.Lo + 1, p.up) - p.kmin) : oA;
+      const int d = oB - oA;  // band B starts d samples after band A
       int base[RQ];
 #pragma unroll
-      for (int i = 0; i < RQ; i++) base[i] = (rbase + 32 * i) * (int)p.S + kb;
-      Acc<T, OC> acc[RQ][4];
+      for (int i = 0; i < RQ; i++) base[i] = (rbase + 32 * i) * (int)p.S + oA;
+      Acc<T, OC> acc[RQ][8];
 #pragma unroll
       for (int i = 0; i < RQ; i++)
 #pragma unroll
-        for (int jj = 0; jj < 4; jj++) acc[i][jj].zero();
-      const TapVec<T, HC> *tg = table + g * p.span;
+        for (int jj = 0; jj < 8; jj++) acc[i][jj].zero();
+      const TapVec<T, HC> *tA = table + gA * p.span;
+      const TapVec<T, HC> *tB = table + (hasB ? gB : gA) * p.span;
+      // range 1: band A only
+      const int e1 = hasB ? min(d, p.span) : p.span;
 #pragma unroll 2
-      for (int kk = 0; kk < p.span; kk++) {
-        const TapVec<T, HC> t = tg[kk];
+      for (int kk = 0; kk < e1; kk++) {
+        const TapVec<T, HC> t = tA[kk];
 #pragma unroll
         for (int i = 0; i < RQ; i++) {
           const XT xv = cur[smem_idx<PAD>(base[i] + kk)];
@@ -149,18 +164,49 @@ __global__ void __launch_bounds__(256) resample_rowtile(const RsParams p) {
           for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][jj], xv, t.v[jj]);
         }
       }
+      if (hasB) {
+        // range 2: both bands
+#pragma unroll 2
+        for (int kk = d; kk < p.span; kk++) {
+          const TapVec<T, HC> ta = tA[kk];
+          const TapVec<T, HC> tb = tB[kk - d];
+#pragma unroll
+          for (int i = 0; i < RQ; i++) {
+            const XT xv = cur[smem_idx<PAD>(base[i] + kk)];
+#pragma unroll
+            for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][jj], xv, ta.v[jj]);
+#pragma unroll
+            for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][4 + jj], xv, tb.v[jj]);
+          }
+        }
+        // range 3: band B only
+#pragma unroll 2
+        for (int kk = max(p.span, d); kk < d + p.span; kk++) {
+          const TapVec<T, HC> tb = tB[kk - d];
+#pragma unroll
+          for (int i = 0; i < RQ; i++) {
+            const XT xv = cur[smem_idx<PAD>(base[i] + kk)];
+#pragma unroll
+            for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][4 + jj], xv, tb.v[jj]);
+          }
+        }
+      }
 #pragma unroll
       for (int i = 0; i < RQ; i++) {
         const int64_t q = q0 + rbase + 32 * i;
 #pragma unroll
-        for (int jj = 0; jj < 4; jj++) {
-          const int64_t j = 4 * (int64_t)g + jj;
+        for (int jj = 0; jj < 8; jj++) {
+          const int64_t j = 8 * (int64_t)sg + jj;
           const int64_t n = q * p.Nt + j;
           if (j < p.Nt && n < p.out_len) orow[n] = pack<T, OC>(acc[i][jj], scale);
         }
       }
     }
     __syncthreads();
+    if (!dbuf && next < p.ntiles) {
+      issue_loads(next, xbuf0);
+      cp_async_commit();
+    }
   }
   cp_async_wait<0>();
 }
@@ -276,7 +322,7 @@ inline int dispatch_rq(RsParams &p, int rq, bool pad, size_t smem, cudaStream_t 
 // Tile shape knobs: rq rows per thread (1, 2, 4), wc column warps (1..8), G row
 // grouping.  Zero picks the built-in heuristic.
 struct TileChoice {
-  int rq = 0, wc = 0;
+  int rq = 0, wc = 0, nbuf = 0;
   int64_t group = 0;
 };
 
@@ -290,27 +336,35 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
                          int64_t c_override, bool odd_extend, int rev, double scale, TileChoice tc, cudaStream_t s) {
   using XT = typename val_of<T, XC>::type;
   using HT = typename val_of<T, HC>::type;
-  const int64_t G = tc.group > 0 ? tc.group : 4 / gcd64(upk, 4);
+  const int64_t G = tc.group > 0 ? tc.group : 8 / gcd64(upk, 8);
   RsGeom geo = plan_geometry(upk, dn, L, out_len, G, c_override, odd_extend);
+  const int nsg = (geo.ncg + 1) / 2;
   int wc = 1;
   if (tc.wc > 0) {
     wc = tc.wc;
   } else {
-    while (wc < 8 && wc * 2 <= geo.ncg) wc *= 2;
+    // the largest power of two <= 8 that divides the super-group count (balanced warps)
+    while (wc < 8 && nsg % (wc * 2) == 0) wc *= 2;
   }
-  if (wc > geo.ncg) wc = 1;
+  if (wc > nsg) wc = 1;
   const bool pad = (geo.S % 2) == 0;
-  auto smem_for = [&](int rq) -> size_t {
+  auto smem_for = [&](int rq, int nbuf) -> size_t {
     const int64_t QC = 32LL * rq * (8 / wc);
     const int64_t win = (QC - 1) * geo.S + (geo.kmax - geo.kmin) + 1;
     const int64_t alloc = pad ? win + (win >> 4) + 1 : win;
     const size_t table = ((size_t)geo.ncg * geo.span * 4 * sizeof(HT) + 15) & ~(size_t)15;
-    return table + 2 * (size_t)alloc * sizeof(XT);
+    return table + (size_t)nbuf * (size_t)alloc * sizeof(XT);
   };
   int rq = tc.rq > 0 ? tc.rq : 2;
   if (sizeof(T) == 8) rq = 1;
-  while (rq > 1 && smem_for(rq) > 110 * 1024) rq /= 2;
-  const size_t smem = smem_for(rq);
+  int nbuf = tc.nbuf > 0 ? tc.nbuf : 2;
+  // two CTAs per SM: prefer double buffering, then fewer rows, then a single buffer
+  while (smem_for(rq, nbuf) > 110 * 1024 && (rq > 1 || nbuf > 1)) {
+    if (nbuf == 2 && rq == 1) nbuf = 1;
+    else if (rq > 1) rq /= 2;
+    else nbuf = 1;
+  }
+  const size_t smem = smem_for(rq, nbuf);
 
   RsParams p{};
   p.x = in;
@@ -327,6 +381,7 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
   p.down = dn;
   p.scale = scale;
   p.rev = rev;
+  p.nbuf = nbuf;
   if (smem <= 200 * 1024) {
     p.Nt = geo.Nt;
     p.S = geo.S;

@@ -106,9 +106,10 @@ def test_channelize_validation(lib):
 
 
 def test_resample_tile_hook(lib):
-    assert lib.gbfir_set_resample_tile(3, 1, 1) == 1
-    assert lib.gbfir_set_resample_tile(2, 4, 1) == 0
-    assert lib.gbfir_set_resample_tile(0, 0, 0) == 0
+    assert lib.gbfir_set_resample_tile(3, 1, 1, 0) == 1
+    assert lib.gbfir_set_resample_tile(2, 4, 1, 3) == 1
+    assert lib.gbfir_set_resample_tile(2, 4, 1, 1) == 0
+    assert lib.gbfir_set_resample_tile(0, 0, 0, 0) == 0
 
 
 def test_package_refuses_cpu_tensors():

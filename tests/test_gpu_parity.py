@@ -209,12 +209,13 @@ def test_resample_tile_overrides_agree(mx, orc):
         h = kaiser_filter(up, down).astype(np.float32)
         r = orc.resample_poly(x, h, up, down)
         try:
-            for rq, wc, g in ((1, 1, 0), (4, 1, 0), (2, 2, 0), (1, 8, 0), (2, 1, 2)):
-                mx.set_resample_tile(rq, wc, g)
+            for rq, wc, g, nb in ((1, 1, 0, 0), (4, 1, 0, 1), (2, 2, 0, 2), (1, 8, 0, 1), (2, 1, 2, 0),
+                                  (1, 4, 4, 2), (4, 2, 16, 1)):
+                mx.set_resample_tile(rq, wc, g, nb)
                 y = host(mx.resample_poly(dev(x), dev(h), up, down))
-                assert rel_l2(y, r) < FP32_TOL, (up, down, rq, wc, g)
+                assert rel_l2(y, r) < FP32_TOL, (up, down, rq, wc, g, nb)
         finally:
-            mx.set_resample_tile(0, 0, 0)
+            mx.set_resample_tile(0, 0, 0, 0)
 
 
 @pytest.mark.parametrize("updown", [(3, 2), (4, 5), (160, 147)])
