@@ -204,6 +204,97 @@ def run_reference(args, rank, world):
     return 0
 
 
+RAGGED_RATIOS = [(1, 2), (2, 3), (3, 4), (5, 4), (160, 147)]
+
+
+def run_ragged(args, rank, world, dev):
+    """4096 complex64 signals, log-uniform lengths in [1e3, 1e6], odd taps uniform in
+    [15, 511], (up, down) drawn from RAGGED_RATIOS, Kaiser sinc filters: one persistent
+    launch vs one plain launch per signal."""
+    import torch
+    from scipy import signal
+    import matx_gb300 as mx
+    from matx_gb300.ragged import RaggedPlan
+    rng = np.random.default_rng(5 + rank)
+    n_sig = 4096
+    lens = np.exp(rng.uniform(np.log(1e3), np.log(1e6), n_sig)).astype(np.int64)
+    taps = rng.integers(7, 256, n_sig) * 2 + 1
+    rsel = rng.integers(len(RAGGED_RATIOS), size=n_sig)
+    g = torch.Generator(device=dev).manual_seed(11 + rank)
+    sigs = []
+    macs = 0
+    outs_total = 0
+    for i in range(n_sig):
+        up, down = RAGGED_RATIOS[rsel[i]]
+        x = torch.randn(int(lens[i]), dtype=torch.complex64, device=dev, generator=g)
+        h = torch.from_numpy(signal.firwin(int(taps[i]), 1.0 / max(up, down), window=("kaiser", 5.0))
+                             .astype(np.float32)).to(dev)
+        sigs.append((x, h, up, down))
+        macs += mac_count(int(lens[i]), int(taps[i]), up, down)
+        outs_total += out_len(int(lens[i]), up, down)
+    plan = RaggedPlan(sigs)
+    for _ in range(args.warmup):
+        plan.run()
+    torch.cuda.synchronize()
+    steps = max(3, min(args.steps, 50))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = mx.launch_count()
+    e0.record()
+    for _ in range(steps):
+        plan.run()
+    e1.record()
+    torch.cuda.synchronize()
+    launches = mx.launch_count() - l0
+    ms_ragged = e0.elapsed_time(e1) / steps
+    # CUDA graph of the same launch
+    sg = torch.cuda.Stream()
+    sg.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(sg):
+        plan.run()
+    torch.cuda.current_stream().wait_stream(sg)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        plan.run()
+    graph.replay()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(steps):
+        graph.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_graph = e0.elapsed_time(e1) / steps
+    # one plain launch per signal
+    outs = plan.outputs
+    for (x, h, up, down), y in zip(sigs, outs):
+        mx.resample_poly(x, h, up, down, out=y)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(max(1, steps // 10)):
+        for (x, h, up, down), y in zip(sigs, outs):
+            mx.resample_poly(x, h, up, down, out=y)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_single = e0.elapsed_time(e1) / max(1, steps // 10)
+    in_bytes = int(lens.sum()) * 8
+    line = {
+        "metric": "FIR GMAC/s (ragged resample_poly c64, one persistent launch)",
+        "value": macs / (ms_graph * 1e-3) / 1e9, "unit": "GMAC/s", "n_gpus": world, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": ms_graph, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded complex Gaussian; Kaiser sinc taps)",
+        "config": {"workload": "ragged resample_poly: 4096 c64 signals, lengths log-uniform [1e3, 1e6], "
+                               "odd taps uniform [15, 511], (up,down) in {(1,2),(2,3),(3,4),(5,4),(160,147)}",
+                   "samples": int(lens.sum()), "outputs": int(outs_total), "tiles": plan.num_tiles},
+        "ragged_ms": ms_ragged, "ragged_graph_ms": ms_graph, "per_signal_launches_ms": ms_single,
+        "speedup_vs_per_signal": ms_single / ms_graph,
+        "output_samples_per_s": outs_total / (ms_graph * 1e-3),
+        "hbm_gbs": (in_bytes + outs_total * 8) / (ms_graph * 1e-3) / 1e9,
+        "gpu_launches": launches,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     global BATCH
     ap = argparse.ArgumentParser()
@@ -215,6 +306,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     ap.add_argument("--batch", type=int, default=BATCH, help="rows per GPU (profiling cases)")
+    ap.add_argument("--no-tune", action="store_true", help="use the built-in tile heuristic")
+    ap.add_argument("--workload", default="resample", choices=["resample", "ragged"],
+                    help="ragged: 4096 uneven signals in one persistent launch (separate JSON line)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     BATCH = args.batch
@@ -234,6 +328,8 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
+    if args.workload == "ragged":
+        return run_ragged(args, rank, world, dev)
 
     xh = make_inputs(1234 + rank)
     taps_np = [kaiser_taps(u, d) for u, d in RATIOS]
@@ -252,6 +348,15 @@ def main():
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
+
+    # ---- tile autotuning (before the timed region) ----------------------------------------
+    tiles = {}
+    if not args.no_tune and prec == "fp32":
+        from matx_gb300 import autotune
+        for (u, d), h, o in zip(RATIOS, taps, outs):
+            r = autotune.tune_resample(x, h, u, d, out=o, use_cache=False)
+            tiles[f"{u}/{d}"] = {"rows_per_thread": r.best[0], "col_warps": r.best[1], "group": r.best[2],
+                                 "buffers": r.best[3], "ms": r.best_ms, "heuristic_ms": r.default_ms}
 
     for _ in range(args.warmup):
         step()
@@ -368,6 +473,7 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": f"resample_rowtile ({u}/{d})", "alg_bytes_per_launch": bytes_dom},
             "per_ratio": per_ratio,
+            "tiles": tiles,
             "error_vs_fp64_rel_l2": err,
             "e2e": {"value": e2e_val, "unit": "GMAC/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "cpu_baseline": cpu,

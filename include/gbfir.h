@@ -167,24 +167,38 @@ typedef struct gbfir_ragged_desc {
   int64_t in_len;
   int64_t out_len;  /* must be ceil(in_len*up/down)             */
   int32_t h_len;
-  int32_t up;       /* already reduced by gcd; up==down==1 copies */
+  int32_t up;       /* reduced by gcd in the planner; up==down copies the input */
   int32_t down;
   int32_t pad_;
 } gbfir_ragged_desc;
 
-/* Bytes of device workspace gbfir_ragged_resample needs for `count` signals
- * and a tile plan of `num_tiles` tiles (from gbfir_ragged_plan). */
+/* Bytes of device workspace gbfir_ragged_resample needs (a work-queue counter). */
 GBFIR_API size_t gbfir_ragged_workspace_size(int64_t count, int64_t num_tiles);
 
-/* Host-side planner: fills `tile_table` (host memory, num_tiles entries of 2
- * int64 each: signal index and first output row) and returns the number of
- * tiles, or a negative gbfir_status.  With tile_table == NULL only counts. */
-GBFIR_API int64_t gbfir_ragged_plan(const gbfir_ragged_desc *host_descs, int64_t count,
-                          int32_t rows_per_tile, int64_t *tile_table);
+/* Launch geometry produced by the planner (host memory). */
+typedef struct gbfir_ragged_plan_info {
+  int64_t num_tiles;     /* entries in the tile table                         */
+  int64_t shared_bytes;  /* dynamic shared memory per CTA                     */
+  int64_t table_bytes;   /* of which the tap table (the window follows it)    */
+} gbfir_ragged_plan_info;
 
+/* Host-side planner.  Validates the descriptors (host copies), cuts every signal
+ * into row tiles of its own geometry and writes `tile_table` (host memory, two
+ * int64 per tile: signal index, first tile row), most expensive tiles first.
+ * Returns the number of tiles (with tile_table == NULL it only counts) or a
+ * negative gbfir_status, and fills *info.  Each signal's up/down are reduced by
+ * their gcd. */
+GBFIR_API int64_t gbfir_ragged_plan(const gbfir_ragged_desc *host_descs, int64_t count,
+                          int64_t *tile_table, gbfir_ragged_plan_info *info);
+
+/* One persistent launch over all tiles.  device_descs / device_tile_table are
+ * device copies of the descriptors and of the planner's table; info is the
+ * planner's host struct.  CTAs take tiles from an atomic counter in `workspace`
+ * (zeroed on the stream first), so the launch balances arbitrary length skew and
+ * contains no host synchronisation: it can be captured in a CUDA graph. */
 GBFIR_API int gbfir_ragged_resample(const gbfir_ragged_desc *device_descs, int64_t count,
-                          const int64_t *device_tile_table, int64_t num_tiles,
-                          int32_t rows_per_tile, int32_t precision,
+                          const int64_t *device_tile_table,
+                          const gbfir_ragged_plan_info *info, int32_t precision,
                           void *workspace, size_t workspace_bytes,
                           gbfir_stream_t stream);
 
@@ -197,6 +211,15 @@ GBFIR_API int gbfir_ragged_resample(const gbfir_ragged_desc *device_descs, int64
  * the built-in heuristic for it.  Process-wide setting, not thread-safe. */
 GBFIR_API int gbfir_set_resample_tile(int32_t rows_per_thread, int32_t col_warps,
                             int32_t group, int32_t buffers);
+
+/* Register the tile shape resample_poly uses for one (up, down, filter length)
+ * (autotuner output; no MatX counterpart).  up/down are reduced by their gcd.
+ * Same field meaning as gbfir_set_resample_tile; the global override wins over
+ * a registered entry, a registered entry over the built-in heuristic. */
+GBFIR_API int gbfir_resample_tile_register(int64_t up, int64_t down, int64_t h_len,
+                                 int32_t rows_per_thread, int32_t col_warps,
+                                 int32_t group, int32_t buffers);
+GBFIR_API int gbfir_resample_tile_clear(void);
 
 /* Number of device kernels this library has launched in this process. */
 GBFIR_API uint64_t gbfir_launch_count(void);

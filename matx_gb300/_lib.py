@@ -41,6 +41,10 @@ class RaggedDesc(ctypes.Structure):
                 ("up", ctypes.c_int32), ("down", ctypes.c_int32), ("pad_", ctypes.c_int32)]
 
 
+class RaggedPlanInfo(ctypes.Structure):
+    _fields_ = [("num_tiles", ctypes.c_int64), ("shared_bytes", ctypes.c_int64), ("table_bytes", ctypes.c_int64)]
+
+
 # (name, restype, argtypes) of every symbol include/gbfir.h declares
 _B = Buf
 _i32, _i64, _p, _sz = ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p, ctypes.c_size_t
@@ -53,9 +57,11 @@ SIGNATURES = [
     ("gbfir_conv1d_bwd_workspace_size", _sz, [_i64, _i64, _i64, _i32]),
     ("gbfir_conv1d_bwd", ctypes.c_int, [_B, _B, _B, _B, _B, _i32, _p, _sz, _p]),
     ("gbfir_ragged_workspace_size", _sz, [_i64, _i64]),
-    ("gbfir_ragged_plan", _i64, [_p, _i64, _i32, _p]),
-    ("gbfir_ragged_resample", ctypes.c_int, [_p, _i64, _p, _i64, _i32, _i32, _p, _sz, _p]),
+    ("gbfir_ragged_plan", _i64, [_p, _i64, _p, _p]),
+    ("gbfir_ragged_resample", ctypes.c_int, [_p, _i64, _p, _p, _i32, _p, _sz, _p]),
     ("gbfir_set_resample_tile", ctypes.c_int, [_i32, _i32, _i32, _i32]),
+    ("gbfir_resample_tile_register", ctypes.c_int, [_i64, _i64, _i64, _i32, _i32, _i32, _i32]),
+    ("gbfir_resample_tile_clear", ctypes.c_int, []),
     ("gbfir_launch_count", ctypes.c_uint64, []),
     ("gbfir_status_string", ctypes.c_char_p, [ctypes.c_int]),
     ("gbfir_last_error", ctypes.c_char_p, []),

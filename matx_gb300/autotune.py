@@ -1,0 +1,134 @@
+"""Tile autotuner for resample_poly (no MatX counterpart).
+
+For one workload (input rows, filter, up/down) the tuner times every candidate
+row-tile shape of the resample kernel on the device with CUDA events and keeps
+the fastest:
+
+  rows_per_thread (outputs per thread along the row direction)  1, 2, 4
+  col_warps       (phases per CTA = 8 * col_warps per pass)     1, 2, 4, 8
+  group           (outputs per tile row = group * up)           multiples giving up*group % 4 == 0
+  buffers         (prefetch the next input window or not)       1, 2
+
+The winner is registered in the library (gbfir_resample_tile_register), so every
+later call with the same reduced (up, down) and filter length uses it, and it is
+stored in a JSON cache keyed by device name, dtype, rates, filter length and the
+row-length bucket, so a later process can register it without re-timing.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+from dataclasses import dataclass, field
+
+import torch
+
+from . import _lib
+from . import resample_poly, set_resample_tile
+
+CACHE = os.environ.get("MATX_GB300_TUNE_CACHE",
+                       os.path.join(os.path.expanduser("~"), ".cache", "matx_gb300", "resample_tiles.json"))
+
+
+@dataclass
+class TuneResult:
+    key: str
+    best: tuple
+    best_ms: float
+    default_ms: float
+    table: list = field(default_factory=list)
+
+
+def _key(x: torch.Tensor, h: torch.Tensor, up: int, down: int) -> str:
+    g = math.gcd(up, down)
+    name = torch.cuda.get_device_name(x.device).replace(" ", "_")
+    nbucket = 1 << max(0, int(math.log2(max(1, x.shape[-1]))))
+    return f"{name}|{x.dtype}|{h.dtype}|{up // g}/{down // g}|L{h.shape[-1]}|N{nbucket}|B{x.numel() // x.shape[-1]}"
+
+
+def candidates(up: int, down: int):
+    g = math.gcd(up, down)
+    u = up // g
+    g0 = 4 // math.gcd(u, 4)
+    groups = sorted({g0 * m for m in (1, 2, 4, 8) if g0 * m <= 64})
+    for rq in (1, 2, 4):
+        for wc in (1, 2, 4, 8):
+            for grp in groups:
+                nsg = (u * grp + 7) // 8
+                if wc > max(1, nsg):
+                    continue
+                for nb in (1, 2):
+                    yield (rq, wc, grp, nb)
+
+
+def _time(fn, reps: int) -> float:
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        start.record()
+        fn()
+        stop.record()
+        stop.synchronize()
+        ts.append(start.elapsed_time(stop))
+    ts.sort()
+    return ts[len(ts) // 2]
+
+
+def register(up: int, down: int, h_len: int, tile) -> None:
+    rq, wc, grp, nb = tile
+    _lib.check(_lib.load().gbfir_resample_tile_register(up, down, h_len, rq, wc, grp, nb))
+
+
+def load_cache() -> dict:
+    try:
+        with open(CACHE) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _save_cache(d: dict) -> None:
+    try:
+        os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+        tmp = CACHE + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(d, f, indent=1, sort_keys=True)
+        os.replace(tmp, CACHE)
+    except OSError:
+        pass
+
+
+def tune_resample(x: torch.Tensor, h: torch.Tensor, up: int, down: int, *, reps: int = 5,
+                  out: torch.Tensor | None = None, use_cache: bool = True) -> TuneResult:
+    """Time all candidate tiles on (x, h) and register the fastest."""
+    key = _key(x, h, up, down)
+    cache = load_cache() if use_cache else {}
+    if key in cache:
+        ent = cache[key]
+        tile = tuple(ent["best"])
+        register(up, down, h.shape[-1], tile)
+        return TuneResult(key, tile, ent["best_ms"], ent["default_ms"], [])
+    if out is None:
+        out = resample_poly(x, h, up, down)
+    run = lambda: resample_poly(x, h, up, down, out=out)
+    set_resample_tile(0, 0, 0, 0)
+    default_ms = _time(run, reps)
+    table = []
+    try:
+        for tile in candidates(up, down):
+            set_resample_tile(*tile)
+            try:
+                ms = _time(run, reps)
+            except _lib.GbfirError:
+                continue
+            table.append((tile, ms))
+    finally:
+        set_resample_tile(0, 0, 0, 0)
+    best, best_ms = min(table, key=lambda t: t[1])
+    register(up, down, h.shape[-1], best)
+    if use_cache:
+        cache[key] = {"best": list(best), "best_ms": best_ms, "default_ms": default_ms}
+        _save_cache(cache)
+    return TuneResult(key, best, best_ms, default_ms, table)

@@ -22,6 +22,8 @@ int channelize_poly_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_bu
 int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t up, int64_t down,
                      int precision, cudaStream_t s);
 int set_resample_tile(int rq, int wc, int group, int nbuf);
+int register_resample_tile(int64_t up, int64_t down, int64_t L, int rq, int wc, int group, int nbuf);
+int clear_resample_tiles();
 
 static thread_local std::string t_last_error;
 static std::atomic<uint64_t> g_launches{0};
@@ -206,6 +208,15 @@ int gbfir_set_resample_tile(int32_t rows_per_thread, int32_t col_warps, int32_t 
     GBFIR_FAIL(rc, "set_resample_tile: invalid tile (%d, %d, %d, %d)", rows_per_thread, col_warps, group, buffers);
   return rc;
 }
+
+int gbfir_resample_tile_register(int64_t up, int64_t down, int64_t h_len, int32_t rows_per_thread, int32_t col_warps,
+                                 int32_t group, int32_t buffers) {
+  int rc = register_resample_tile(up, down, h_len, rows_per_thread, col_warps, group, buffers);
+  if (rc) GBFIR_FAIL(rc, "resample_tile_register: invalid tile");
+  return rc;
+}
+
+int gbfir_resample_tile_clear(void) { return clear_resample_tiles(); }
 
 uint64_t gbfir_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 

@@ -7,12 +7,33 @@
 //
 // Schedule (no MatX counterpart): the row-tile kernel of rowtile.cuh, with a
 // direct per-output kernel for rates whose tiles do not fit in shared memory.
+#include <mutex>
+#include <unordered_map>
+
 #include "rowtile.cuh"
 
 namespace gbfir {
 
 // Resample tile override set by the autotuner hook.
 static int g_rq_override = 0, g_wc_override = 0, g_group_override = 0, g_nbuf_override = 0;
+
+// Autotuned tiles per (reduced up, reduced down, filter length).
+struct TileKey {
+  int64_t up, down, L;
+  bool operator==(const TileKey &o) const { return up == o.up && down == o.down && L == o.L; }
+};
+struct TileKeyHash {
+  size_t operator()(const TileKey &k) const {
+    return std::hash<int64_t>()(k.up * 1000003 + k.down * 7919 + k.L);
+  }
+};
+static std::mutex g_tile_mu;
+static std::unordered_map<TileKey, TileChoice, TileKeyHash> g_tiles;
+
+static bool valid_tile(int rq, int wc, int group, int nbuf) {
+  return (rq == 0 || rq == 1 || rq == 2 || rq == 4) && (wc == 0 || wc == 1 || wc == 2 || wc == 4 || wc == 8) &&
+         group >= 0 && group <= 64 && (nbuf == 0 || nbuf == 1 || nbuf == 2);
+}
 
 // Identity (up == down after the gcd): out = in, with real->complex widening.
 template <typename T, bool XC, bool OC>
@@ -43,10 +64,15 @@ template <typename T, bool XC, bool HC>
 static int run_resample(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t up, int64_t down,
                         cudaStream_t s) {
   TileChoice tc;
-  tc.rq = g_rq_override;
-  tc.wc = g_wc_override;
-  tc.group = g_group_override;
-  tc.nbuf = g_nbuf_override;
+  {
+    std::lock_guard<std::mutex> lk(g_tile_mu);
+    auto it = g_tiles.find(TileKey{up, down, h.len});
+    if (it != g_tiles.end()) tc = it->second;
+  }
+  if (g_rq_override) tc.rq = g_rq_override;
+  if (g_wc_override) tc.wc = g_wc_override;
+  if (g_group_override) tc.group = g_group_override;
+  if (g_nbuf_override) tc.nbuf = g_nbuf_override;
   return resample_pass<T, XC, HC>(in.ptr, in.batch_stride, in.len, h.ptr, h.len, out.ptr, out.batch_stride, out.len,
                                   out.batch, up, down, -1, true, 0, (double)up, tc, s);
 }
@@ -88,11 +114,27 @@ int resample_poly_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf 
   return run_resample<float, false, false>(out, in, h, up, down, s);
 }
 
+int register_resample_tile(int64_t up, int64_t down, int64_t L, int rq, int wc, int group, int nbuf) {
+  if (!valid_tile(rq, wc, group, nbuf) || up <= 0 || down <= 0 || L <= 0) return GBFIR_ERR_INVALID_PARAMETER;
+  const int64_t g = gcd64(up, down);
+  TileChoice tc;
+  tc.rq = rq;
+  tc.wc = wc;
+  tc.group = group;
+  tc.nbuf = nbuf;
+  std::lock_guard<std::mutex> lk(g_tile_mu);
+  g_tiles[TileKey{up / g, down / g, L}] = tc;
+  return GBFIR_SUCCESS;
+}
+
+int clear_resample_tiles() {
+  std::lock_guard<std::mutex> lk(g_tile_mu);
+  g_tiles.clear();
+  return GBFIR_SUCCESS;
+}
+
 int set_resample_tile(int rq, int wc, int group, int nbuf) {
-  if (nbuf != 0 && nbuf != 1 && nbuf != 2) return GBFIR_ERR_INVALID_PARAMETER;
-  if (rq != 0 && rq != 1 && rq != 2 && rq != 4) return GBFIR_ERR_INVALID_PARAMETER;
-  if (wc != 0 && wc != 1 && wc != 2 && wc != 4 && wc != 8) return GBFIR_ERR_INVALID_PARAMETER;
-  if (group < 0 || group > 64) return GBFIR_ERR_INVALID_PARAMETER;
+  if (!valid_tile(rq, wc, group, nbuf)) return GBFIR_ERR_INVALID_PARAMETER;
   g_rq_override = rq;
   g_wc_override = wc;
   g_group_override = group;

@@ -63,6 +63,106 @@ __device__ __forceinline__ int smem_idx(int p) {
   else return p;
 }
 
+// table[g*span + kk].v[jj] = he[c + (4g+jj)*down - (kl0(g)+kk)*up] (reversed when rev), 0 outside.
+template <typename T, bool HC>
+__device__ __forceinline__ void build_tap_table(const RsParams &p, const typename val_of<T, HC>::type *hp,
+                                                TapVec<T, HC> *table, int tid, int nthreads) {
+  using HT = typename val_of<T, HC>::type;
+  const int nent = p.ncg * p.span * 4;
+  for (int e = tid; e < nent; e += nthreads) {
+    const int g = e / (p.span * 4);
+    const int rem = e - g * (p.span * 4);
+    const int kk = rem >> 2, jj = rem & 3;
+    const int64_t j = 4 * (int64_t)g + jj;
+    const int64_t kl0 = ceil_div(p.c + 4 * (int64_t)g * p.down - p.Lo + 1, p.up);
+    const int64_t tp = p.c + j * p.down - (kl0 + kk) * p.up;
+    HT v = zero_val<HT>();
+    if (j < p.Nt && tp >= 0 && tp < p.Lo) {
+      const int64_t te = p.rev ? p.Lo - 1 - tp : tp;  // index into he
+      if (!(p.even && te == 0)) v = hp[te - p.even];
+    }
+    table[g * p.span + kk].v[jj] = v;
+  }
+}
+
+// One tile of QC rows starting at row q0: every warp (wr, wc) accumulates its 8-phase
+// super-groups for RQ rows per lane and stores them (masked by Nt and out_len).
+template <typename T, bool XC, bool HC, int RQ, bool PAD>
+__device__ __forceinline__ void rowtile_compute(const RsParams &p, const typename val_of<T, XC>::type *cur,
+                                                const TapVec<T, HC> *table, typename val_of<T, XC || HC>::type *orow,
+                                                int64_t q0, int wr, int wc, int lane, T scale) {
+  using XT = typename val_of<T, XC>::type;
+  constexpr bool OC = XC || HC;
+  const int nsg = (p.ncg + 1) / 2;
+  const int rbase = wr * 32 * RQ + lane;  // local row of slice i is rbase + 32*i
+  for (int sg = wc; sg < nsg; sg += p.WC) {
+    const int gA = 2 * sg, gB = 2 * sg + 1;
+    const bool hasB = gB < p.ncg;
+    const int oA = (int)(ceil_div(p.c + 4 * (int64_t)gA * p.down - p.Lo + 1, p.up) - p.kmin);
+    const int oB = hasB ? (int)(ceil_div(p.c + 4 * (int64_t)gB * p.down - p.Lo + 1, p.up) - p.kmin) : oA;
+    const int d = oB - oA;  // band B starts d samples after band A
+    int base[RQ];
+#pragma unroll
+    for (int i = 0; i < RQ; i++) base[i] = (rbase + 32 * i) * (int)p.S + oA;
+    Acc<T, OC> acc[RQ][8];
+#pragma unroll
+    for (int i = 0; i < RQ; i++)
+#pragma unroll
+      for (int jj = 0; jj < 8; jj++) acc[i][jj].zero();
+    const TapVec<T, HC> *tA = table + gA * p.span;
+    const TapVec<T, HC> *tB = table + (hasB ? gB : gA) * p.span;
+    // range 1: band A only
+    const int e1 = hasB ? min(d, p.span) : p.span;
+#pragma unroll 2
+    for (int kk = 0; kk < e1; kk++) {
+      const TapVec<T, HC> t = tA[kk];
+#pragma unroll
+      for (int i = 0; i < RQ; i++) {
+        const XT xv = cur[smem_idx<PAD>(base[i] + kk)];
+#pragma unroll
+        for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][jj], xv, t.v[jj]);
+      }
+    }
+    if (hasB) {
+      // range 2: both bands
+#pragma unroll 2
+      for (int kk = d; kk < p.span; kk++) {
+        const TapVec<T, HC> ta = tA[kk];
+        const TapVec<T, HC> tb = tB[kk - d];
+#pragma unroll
+        for (int i = 0; i < RQ; i++) {
+          const XT xv = cur[smem_idx<PAD>(base[i] + kk)];
+#pragma unroll
+          for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][jj], xv, ta.v[jj]);
+#pragma unroll
+          for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][4 + jj], xv, tb.v[jj]);
+        }
+      }
+      // range 3: band B only
+#pragma unroll 2
+      for (int kk = max(p.span, d); kk < d + p.span; kk++) {
+        const TapVec<T, HC> tb = tB[kk - d];
+#pragma unroll
+        for (int i = 0; i < RQ; i++) {
+          const XT xv = cur[smem_idx<PAD>(base[i] + kk)];
+#pragma unroll
+          for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][4 + jj], xv, tb.v[jj]);
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < RQ; i++) {
+      const int64_t q = q0 + rbase + 32 * i;
+#pragma unroll
+      for (int jj = 0; jj < 8; jj++) {
+        const int64_t j = 8 * (int64_t)sg + jj;
+        const int64_t n = q * p.Nt + j;
+        if (j < p.Nt && n < p.out_len) orow[n] = pack<T, OC>(acc[i][jj], scale);
+      }
+    }
+  }
+}
+
 template <typename T, bool XC, bool HC, int RQ, bool PAD>
 __global__ void __launch_bounds__(256) resample_rowtile(const RsParams p) {
   using XT = typename val_of<T, XC>::type;
@@ -80,22 +180,7 @@ __global__ void __launch_bounds__(256) resample_rowtile(const RsParams p) {
   const XT *xp = reinterpret_cast<const XT *>(p.x);
   OT *op = reinterpret_cast<OT *>(p.out);
 
-  // ---- tap table: table[g*span + kk].v[jj] = he[c + (4g+jj)*down - (kl0(g)+kk)*up]
-  const int nent = p.ncg * p.span * 4;
-  for (int e = tid; e < nent; e += blockDim.x) {
-    const int g = e / (p.span * 4);
-    const int rem = e - g * (p.span * 4);
-    const int kk = rem >> 2, jj = rem & 3;
-    const int64_t j = 4 * (int64_t)g + jj;
-    const int64_t kl0 = ceil_div(p.c + 4 * (int64_t)g * p.down - p.Lo + 1, p.up);
-    const int64_t tp = p.c + j * p.down - (kl0 + kk) * p.up;
-    HT v = zero_val<HT>();
-    if (j < p.Nt && tp >= 0 && tp < p.Lo) {
-      const int64_t te = p.rev ? p.Lo - 1 - tp : tp;  // index into he
-      if (!(p.even && te == 0)) v = hp[te - p.even];
-    }
-    table[g * p.span + kk].v[jj] = v;
-  }
+  build_tap_table<T, HC>(p, hp, table, tid, blockDim.x);
 
   auto issue_loads = [&](int64_t tile, XT *buf) {
     const int64_t b = tile / p.tiles_per_row;
@@ -117,7 +202,6 @@ __global__ void __launch_bounds__(256) resample_rowtile(const RsParams p) {
   const int wid = tid >> 5, lane = tid & 31;
   const int wr = wid / p.WC, wc = wid - wr * p.WC;
   const T scale = T(p.scale);
-  const int nsg = (p.ncg + 1) / 2;  // super-groups of 8 phases = two 4-phase bands
 
   for (int it = 0; tile < p.ntiles; tile += gridDim.x, ++it) {
     XT *cur = (dbuf && (it & 1)) ? xbuf1 : xbuf0;
@@ -134,74 +218,7 @@ __global__ void __launch_bounds__(256) resample_rowtile(const RsParams p) {
     const int64_t b = tile / p.tiles_per_row;
     const int64_t q0 = (tile - b * p.tiles_per_row) * p.QC;
     OT *orow = op + b * p.out_bstride;
-    const int rbase = wr * 32 * RQ + lane;  // local row of slice i is rbase + 32*i
-
-    for (int sg = wc; sg < nsg; sg += p.WC) {
-      const int gA = 2 * sg, gB = 2 * sg + 1;
-      const bool hasB = gB < p.ncg;
-      const int oA = (int)(ceil_div(p.c + 4 * (int64_t)gA * p.down - p.Lo + 1, p.up) - p.kmin);
-      const int oB = hasB ? (int)(ceil_div(p.c + 4 * (int64_t)gB * p.down - p.Lo + 1, p.up) - p.kmin) : oA;
-      const int d = oB - oA;  // band B starts d samples after band A
-      int base[RQ];
-#pragma unroll
-      for (int i = 0; i < RQ; i++) base[i] = (rbase + 32 * i) * (int)p.S + oA;
-      Acc<T, OC> acc[RQ][8];
-#pragma unroll
-      for (int i = 0; i < RQ; i++)
-#pragma unroll
-        for (int jj = 0; jj < 8; jj++) acc[i][jj].zero();
-      const TapVec<T, HC> *tA = table + gA * p.span;
-      const TapVec<T, HC> *tB = table + (hasB ? gB : gA) * p.span;
-      // range 1: band A only
-      const int e1 = hasB ? min(d, p.span) : p.span;
-#pragma unroll 2
-      for (int kk = 0; kk < e1; kk++) {
-        const TapVec<T, HC> t = tA[kk];
-#pragma unroll
-        for (int i = 0; i < RQ; i++) {
-          const XT xv = cur[smem_idx<PAD>(base[i] + kk)];
-#pragma unroll
-          for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][jj], xv, t.v[jj]);
-        }
-      }
-      if (hasB) {
-        // range 2: both bands
-#pragma unroll 2
-        for (int kk = d; kk < p.span; kk++) {
-          const TapVec<T, HC> ta = tA[kk];
-          const TapVec<T, HC> tb = tB[kk - d];
-#pragma unroll
-          for (int i = 0; i < RQ; i++) {
-            const XT xv = cur[smem_idx<PAD>(base[i] + kk)];
-#pragma unroll
-            for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][jj], xv, ta.v[jj]);
-#pragma unroll
-            for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][4 + jj], xv, tb.v[jj]);
-          }
-        }
-        // range 3: band B only
-#pragma unroll 2
-        for (int kk = max(p.span, d); kk < d + p.span; kk++) {
-          const TapVec<T, HC> tb = tB[kk - d];
-#pragma unroll
-          for (int i = 0; i < RQ; i++) {
-            const XT xv = cur[smem_idx<PAD>(base[i] + kk)];
-#pragma unroll
-            for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][4 + jj], xv, tb.v[jj]);
-          }
-        }
-      }
-#pragma unroll
-      for (int i = 0; i < RQ; i++) {
-        const int64_t q = q0 + rbase + 32 * i;
-#pragma unroll
-        for (int jj = 0; jj < 8; jj++) {
-          const int64_t j = 8 * (int64_t)sg + jj;
-          const int64_t n = q * p.Nt + j;
-          if (j < p.Nt && n < p.out_len) orow[n] = pack<T, OC>(acc[i][jj], scale);
-        }
-      }
-    }
+    rowtile_compute<T, XC, HC, RQ, PAD>(p, cur, table, orow, q0, wr, wc, lane, scale);
     __syncthreads();
     if (!dbuf && next < p.ntiles) {
       issue_loads(next, xbuf0);
@@ -336,7 +353,7 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
                          int64_t c_override, bool odd_extend, int rev, double scale, TileChoice tc, cudaStream_t s) {
   using XT = typename val_of<T, XC>::type;
   using HT = typename val_of<T, HC>::type;
-  const int64_t G = tc.group > 0 ? tc.group : 8 / gcd64(upk, 8);
+  const int64_t G = tc.group > 0 ? tc.group : 4 / gcd64(upk, 4);
   RsGeom geo = plan_geometry(upk, dn, L, out_len, G, c_override, odd_extend);
   const int nsg = (geo.ncg + 1) / 2;
   int wc = 1;

@@ -117,3 +117,29 @@ def test_package_refuses_cpu_tensors():
     import matx_gb300 as mx
     with pytest.raises(ValueError):
         mx.resample_poly(torch.zeros(10, dtype=torch.complex64), torch.zeros(5), 3, 2)
+
+
+def test_ragged_plan_validation(lib):
+    from matx_gb300._lib import RaggedDesc, RaggedPlanInfo
+    d = (RaggedDesc * 2)()
+    d[0] = RaggedDesc(FAKE, FAKE, FAKE, 1000, 1500, 61, 3, 2, 0)
+    d[1] = RaggedDesc(FAKE, FAKE, FAKE, 1000, 800, 101, 4, 5, 0)
+    info = RaggedPlanInfo()
+    n = lib.gbfir_ragged_plan(d, 2, None, ctypes.byref(info))
+    assert n > 0 and info.num_tiles == n and info.shared_bytes > info.table_bytes >= 0
+    d[1] = RaggedDesc(FAKE, FAKE, FAKE, 1000, 801, 101, 4, 5, 0)  # wrong out_len
+    assert lib.gbfir_ragged_plan(d, 2, None, ctypes.byref(info)) == -2
+    d[1] = RaggedDesc(FAKE, 0, FAKE, 1000, 800, 101, 4, 5, 0)  # null output
+    assert lib.gbfir_ragged_plan(d, 2, None, ctypes.byref(info)) == -7
+    d[1] = RaggedDesc(FAKE + 4, FAKE, FAKE, 1000, 800, 101, 4, 5, 0)  # misaligned complex input
+    assert lib.gbfir_ragged_plan(d, 2, None, ctypes.byref(info)) == -8
+    # tiles are ordered most expensive first and cover every row tile
+    d[1] = RaggedDesc(FAKE, FAKE, FAKE, 100000, 80000, 101, 4, 5, 0)
+    n = lib.gbfir_ragged_plan(d, 2, None, ctypes.byref(info))
+    import numpy as np
+    t = np.empty((n, 2), dtype=np.int64)
+    assert lib.gbfir_ragged_plan(d, 2, t.ctypes.data_as(ctypes.c_void_p), ctypes.byref(info)) == n
+    assert set(t[:, 0].tolist()) == {0, 1}
+    # launch refuses a plan that does not come from the planner (before touching the device)
+    bad = RaggedPlanInfo(n, 300 * 1024, 0)
+    assert lib.gbfir_ragged_resample(FAKE, 2, FAKE, ctypes.byref(bad), 0, FAKE, 256, None) == 1
