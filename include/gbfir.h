@@ -221,6 +221,16 @@ GBFIR_API int gbfir_resample_tile_register(int64_t up, int64_t down, int64_t h_l
                                  int32_t group, int32_t buffers);
 GBFIR_API int gbfir_resample_tile_clear(void);
 
+/* Diagnostic: C[M][N] = A[M][K] * B[N][K]^T on the tcgen05 tensor cores (no MatX
+ * counterpart).  FP32 in/out; operands rounded to bf16 (terms = 1) or split into three
+ * bf16 terms with the six products of order <= 2 accumulated in FP32 (terms = 3).
+ * M % 128 == 0, N in [16, 256] step 16, K in {16, 32, 48, 64}.  swap_offsets exchanges
+ * the two shared-memory descriptor offsets (layout check).  *status (device int) is set
+ * to 1 if a bounded wait in the kernel gave up. */
+GBFIR_API int gbfir_tc_gemm_selftest(const float *A, const float *B, float *C, int32_t M,
+                           int32_t N, int32_t K, int32_t terms, int32_t swap_offsets,
+                           int32_t *status, gbfir_stream_t stream);
+
 /* Number of device kernels this library has launched in this process. */
 GBFIR_API uint64_t gbfir_launch_count(void);
 

@@ -1,0 +1,145 @@
+// tc.cuh — tcgen05 (5th-generation tensor core) building blocks for sm_103a, in inline PTX.
+//
+// Conventions used by every tensor-core kernel of this library:
+//  * One CTA, cta_group::1, MMA shape M = 128 (TMEM lane m = row m), N = 16..256, K = 16
+//    (kind::f16, bf16 or fp16 operands, FP32 accumulate).
+//  * Operands live in shared memory in the no-swizzle K-major canonical layout: 8-row x
+//    16-byte core matrices (8 rows x 8 bf16 along K, 128 contiguous bytes); the core
+//    matrix (row group i, K group j) sits at  base + i * SBO + j * LBO.
+//  * One elected thread issues the MMAs and a tcgen05.commit that arrives on an mbarrier;
+//    every wait on an mbarrier is bounded: after kSpinLimit failed polls the waiter sets
+//    an error flag and the kernel skips the work that depended on it, so a fault in the
+//    pipeline becomes a status code, never a hung GPU.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+namespace gbfir {
+namespace tc {
+
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// ---- mbarrier ---------------------------------------------------------------------
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Bounded wait; returns false (and leaves the barrier untouched) if it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kSpinLimit; i++) {
+    if (mbar_try_wait(bar, parity)) return true;
+  }
+  return false;
+}
+
+// ---- proxy / tcgen05 ordering fences ---------------------------------------------------
+// generic-proxy shared-memory writes -> visible to the tensor core (async proxy)
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// ---- tensor memory ---------------------------------------------------------------------
+// Executed by one full warp.  ncols is a power of two in [32, 512].
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// ---- descriptors ---------------------------------------------------------------------
+// Shared-memory matrix descriptor, no swizzle: start, leading (K-direction core matrix)
+// and stride (row-group direction) byte offsets, all multiples of 16 bytes.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version for this architecture
+  return d;                // base offset 0, relative LBO, layout type 0 (no swizzle)
+}
+
+// Instruction descriptor for kind::f16 with FP32 accumulate, both operands K-major.
+// ab_bf16: 1 = bf16 operands, 0 = fp16.
+__host__ __device__ constexpr uint32_t idesc_f16(uint32_t M, uint32_t N, uint32_t ab_bf16) {
+  return (1u << 4)                  // D format: F32
+         | (ab_bf16 << 7)           // A format
+         | (ab_bf16 << 10)          // B format
+         | ((N >> 3) << 17)         // N / 8
+         | ((M >> 4) << 24);        // M / 16
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T ; issued by one thread.
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// Arrive on `bar` once every MMA this thread issued so far has completed.
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// Warp w (0..3) reads its 32 TMEM lanes, 16 consecutive FP32 columns starting at `col`.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// ---- operand packing ----------------------------------------------------------------------
+// Byte offset of element (row, k) in the K-major no-swizzle layout with K-adjacent core
+// matrices contiguous: core (row/8, k/8) at ((row/8) * (K/8) + k/8) * 128.
+__device__ __forceinline__ uint32_t kmajor_offset(uint32_t row, uint32_t k, uint32_t K) {
+  return (((row >> 3) * (K >> 3) + (k >> 3)) << 7) + ((row & 7) << 4) + ((k & 7) << 1);
+}
+
+// Split an FP32 value into three bf16 terms a0 + a1 + a2 (24 significant bits).
+__device__ __forceinline__ void split3_bf16(float a, __nv_bfloat16 &a0, __nv_bfloat16 &a1, __nv_bfloat16 &a2) {
+  a0 = __float2bfloat16_rn(a);
+  const float r1 = a - __bfloat162float(a0);
+  a1 = __float2bfloat16_rn(r1);
+  const float r2 = r1 - __bfloat162float(a1);
+  a2 = __float2bfloat16_rn(r2);
+}
+
+}  // namespace tc
+}  // namespace gbfir
