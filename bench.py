@@ -448,6 +448,39 @@ def main():
     except Exception as e:  # the error statement is informative, never the measurement
         err = {"unavailable": str(e)[:200]}
 
+    # ---- tensor-core forms on the same inputs (untimed by the headline; per-ratio CUDA events) ----
+    forms = {}
+    if not args.no_e2e and prec == "fp32":
+        try:
+            import oracle
+            for form in ("bf16x3", "bf16", "fp16"):
+                fr = {}
+                for i, ((u2, d2), hh, oo) in enumerate(zip(RATIOS, taps, outs)):
+                    try:
+                        mx.resample_poly(x, hh, u2, d2, precision=form, out=oo)
+                    except mx.GbfirError as ge:
+                        fr[f"{u2}/{d2}"] = {"unavailable": str(ge)[:160]}
+                        continue
+                    torch.cuda.synchronize()
+                    reps = 20
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    for _ in range(reps):
+                        mx.resample_poly(x, hh, u2, d2, precision=form, out=oo)
+                    e1.record(stream)
+                    torch.cuda.synchronize()
+                    ms = e0.elapsed_time(e1) / reps
+                    row = 17
+                    r64 = oracle.resample_poly(xh[row], taps_np[i], u2, d2, double=True, nthreads=4)[0]
+                    err_f = float(np.linalg.norm(oo[row].cpu().numpy() - r64) / np.linalg.norm(r64))
+                    b2 = alg_bytes(NSAMP, len(taps_np[i]), u2, d2, BATCH)
+                    fr[f"{u2}/{d2}"] = {"ms": ms, "gmacs": macs[i] / (ms * 1e-3) / 1e9,
+                                        "vs_fp32": per_ms[i] / ms, "hbm_frac": b2 / (ms * 1e-3) / 1e9 / peak,
+                                        "rel_l2_vs_fp64": err_f}
+                forms[form] = fr
+        except Exception as fe:  # noqa: BLE001
+            forms = {"unavailable": str(fe)[:200]}
+
     # ---- CPU baseline on this host (rank 0, N = 1 only) ----------------------------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -474,6 +507,7 @@ def main():
                          "kernel": f"resample_rowtile ({u}/{d})", "alg_bytes_per_launch": bytes_dom},
             "per_ratio": per_ratio,
             "tiles": tiles,
+            "forms": forms,
             "error_vs_fp64_rel_l2": err,
             "e2e": {"value": e2e_val, "unit": "GMAC/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "cpu_baseline": cpu,

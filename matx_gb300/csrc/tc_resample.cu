@@ -1,0 +1,371 @@
+// tc_resample.cu — resample_poly as Toeplitz MMAs on the tcgen05 tensor cores
+// (bf16, fp16 and bf16x3 split precision, FP32 accumulate in TMEM).  No MatX counterpart.
+//
+// Math.  With gcd-reduced rates, y[n] = up * sum_i x[i] * he[c + n*down - i*up].
+// The kernel groups outputs into rows whose inputs advance by exactly 8 samples of a
+// linear array xs, so that the Hankel operand A[q][k] = xs[8q + k] is a plain
+// K-major shared-memory matrix with overlapping rows: its 8-row x 16-byte core
+// matrices are 16 bytes apart along K (LBO = 16) and 128 bytes apart along rows
+// (SBO = 128), and no Hankel matrix is ever materialised.
+//   path A (down divides 8): xs[u] = x[u + k0]; a row holds Nt = 8*up/down outputs and
+//     D[q][j] = sum_k xs[8q + k] * W[j][k],  W[j][k] = up*he[c + j*down - (k + k0)*up].
+//   path B (other down): x is split into its `down` polyphase components
+//     xs_b[a] = x[down*a + b]; each is an interpolator (rate up) and a row holds
+//     Nt = 8*up outputs:  D[q][j] = sum_b sum_k xs_b[8q + k + k0] * W_b[j][k],
+//     W_b[j][k] = up*he[c + down*j - up*(b + down*(k + k0))].
+// The tap matrices W (N = Nt rounded up to 16 columns, Kp = band rounded to 16) are
+// built once per CTA.  Complex x runs as two M = 128 MMAs (real, imaginary rows) on the
+// same W.  bf16x3 splits both operands into three bf16 terms and accumulates the six
+// products of order <= 2 (smallest first) — 24 significant bits, FP32-class accuracy.
+//
+// Pipeline (persistent CTA, 256 threads).  An iteration covers MT M-tiles of 128 rows.
+// Threads convert the next iteration's input samples into the bf16 term arrays of the
+// other shared buffer while one thread's MMAs for the current iteration run into one
+// of two TMEM accumulator sets; after a bounded mbarrier wait every warp reads its TMEM
+// lanes back and stores the outputs.
+#include "rowtile.cuh"
+#include "tc.cuh"
+
+namespace gbfir {
+
+constexpr int kTcThreads = 256;
+
+struct TcParams {
+  const void *x;
+  int64_t x_bstride, N;
+  const float *h;
+  int64_t Lo, c;
+  int32_t even, rev;
+  void *out;
+  int64_t out_bstride, out_len;
+  int64_t up, down;
+  int32_t path;     // 0: A, 1: B
+  int32_t P;        // arrays per term (1 or down)
+  int32_t Nt, Nmma; // useful outputs per row, MMA N
+  int32_t Kp;       // K band (multiple of 16)
+  int64_t k0;       // aligned band start (multiple of 8)
+  int32_t MT;       // M-tiles (128 rows) per iteration
+  int32_t LA;       // elements per xs array per buffer = 8*128*MT + Kp
+  int32_t terms;    // 1 or 3
+  int32_t fp16;     // 1: fp16 operands (single term), 0: bf16
+  int64_t rows;     // rows per signal row = ceil(out_len / Nt)
+  int64_t iters_per_row, niters;
+  double scale;     // up
+  int32_t tmem_cols;
+};
+
+// Bounded-wait status of the tensor-core kernels (1 = a wait gave up); read and
+// cleared by gbfir_tc_status().
+__device__ int32_t g_tc_status;
+
+__device__ __forceinline__ float tap_value(const TcParams &p, int64_t tp) {
+  if (tp < 0 || tp >= p.Lo) return 0.f;
+  const int64_t te = p.rev ? p.Lo - 1 - tp : tp;
+  if (p.even && te == 0) return 0.f;
+  return p.h[te - p.even];
+}
+
+template <bool XC>
+__global__ void __launch_bounds__(kTcThreads) tc_resample_kernel(const TcParams p) {
+  using XT = typename val_of<float, XC>::type;
+  constexpr int NPARTS = XC ? 2 : 1;  // real / imaginary operand rows
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t bars[2];
+  __shared__ uint32_t tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  // shared layout: W [P][terms][Nmma x Kp] ; xs [2 bufs][NPARTS][terms][P][LA]
+  const uint32_t wbytes = (uint32_t)p.Nmma * p.Kp * 2u;
+  unsigned char *wbase = smem;
+  unsigned char *xbase = smem + ((size_t)p.P * p.terms * wbytes + 127) / 128 * 128;
+  const size_t xarr = ((size_t)p.LA * 2 + 127) / 128 * 128;  // bytes per xs array
+  auto warr = [&](int pp, int t) { return wbase + ((size_t)pp * p.terms + t) * wbytes; };
+  auto xarrp = [&](int buf, int part, int t, int pp) {
+    return xbase + ((((size_t)buf * NPARTS + part) * p.terms + t) * p.P + pp) * xarr;
+  };
+
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, (uint32_t)p.tmem_cols);
+  if (tid == 0) {
+    tc::mbar_init(&bars[0], 1);
+    tc::mbar_init(&bars[1], 1);
+    tc::mbar_fence_init();
+  }
+  // ---- tap matrices W_p[j][k] (K-major core layout), split into terms ----
+  const int wel = p.Nmma * p.Kp;
+  for (int e = tid; e < p.P * wel; e += kTcThreads) {
+    const int pp = e / wel, r = e - pp * wel;
+    const int j = r / p.Kp, k = r - j * p.Kp;
+    float v = 0.f;
+    if (j < p.Nt) {
+      const int64_t kk = k + p.k0;
+      const int64_t tp = p.path == 0 ? p.c + (int64_t)j * p.down - kk * p.up
+                                     : p.c + p.down * (int64_t)j - p.up * (pp + p.down * kk);
+      v = tap_value(p, tp) * (float)p.scale;
+    }
+    const uint32_t off = tc::kmajor_offset(j, k, p.Kp);
+    if (p.fp16) {
+      *reinterpret_cast<__half *>(warr(pp, 0) + off) = __float2half_rn(v);
+    } else {
+      __nv_bfloat16 t0, t1, t2;
+      tc::split3_bf16(v, t0, t1, t2);
+      *reinterpret_cast<__nv_bfloat16 *>(warr(pp, 0) + off) = t0;
+      if (p.terms == 3) {
+        *reinterpret_cast<__nv_bfloat16 *>(warr(pp, 1) + off) = t1;
+        *reinterpret_cast<__nv_bfloat16 *>(warr(pp, 2) + off) = t2;
+      }
+    }
+  }
+
+  // ---- input conversion of one iteration into buffer `buf` ----
+  const XT *xp = reinterpret_cast<const XT *>(p.x);
+  auto convert = [&](int64_t it, int buf) {
+    const int64_t b = it / p.iters_per_row;
+    const int64_t q0 = (it - b * p.iters_per_row) * (int64_t)(128 * p.MT);
+    const XT *row = xp + b * p.x_bstride;
+    // path A: xs[u] = x[8*q0 + k0 + u]; path B: xs_b[u] = x[down*(8*q0 + k0 + u) + b]
+    const int64_t base = p.path == 0 ? 8 * q0 + p.k0 : p.down * (8 * q0 + p.k0);
+    for (int pp = 0; pp < p.P; pp++) {
+    for (int u = tid; u < p.LA; u += kTcThreads) {
+      const int64_t gi = base + (int64_t)u * p.P + pp;  // path A: P == 1, pp == 0
+      XT xv = zero_val<XT>();
+      if (gi >= 0 && gi < p.N) xv = row[gi];
+#pragma unroll
+      for (int part = 0; part < NPARTS; part++) {
+        const float f = part == 0 ? re_of(xv) : im_of(xv);
+        if (p.fp16) {
+          reinterpret_cast<__half *>(xarrp(buf, part, 0, pp))[u] = __float2half_rn(f);
+        } else {
+          __nv_bfloat16 t0, t1, t2;
+          tc::split3_bf16(f, t0, t1, t2);
+          reinterpret_cast<__nv_bfloat16 *>(xarrp(buf, part, 0, pp))[u] = t0;
+          if (p.terms == 3) {
+            reinterpret_cast<__nv_bfloat16 *>(xarrp(buf, part, 1, pp))[u] = t1;
+            reinterpret_cast<__nv_bfloat16 *>(xarrp(buf, part, 2, pp))[u] = t2;
+          }
+        }
+      }
+    }
+    }
+  };
+
+  int64_t it = blockIdx.x;
+  if (it < p.niters) convert(it, 0);
+  tc::fence_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t set_cols = (uint32_t)(p.MT * NPARTS * p.Nmma);
+  const uint32_t idesc = tc::idesc_f16(128, (uint32_t)p.Nmma, p.fp16 ? 0u : 1u);
+  const int pa3[6] = {2, 1, 0, 1, 0, 0}, pb3[6] = {0, 1, 2, 0, 1, 0};
+  const int npairs = p.terms == 3 ? 6 : 1;
+  bool ok = true;
+  uint32_t phase[2] = {0, 0};
+
+  for (int k = 0; it < p.niters; it += gridDim.x, ++k) {
+    const int buf = k & 1;
+    const uint32_t dset = tmem + (uint32_t)buf * set_cols;
+    if (tid == 0) {
+      // A: xs_p + (8*128*m + 16*ks) elements, LBO 16 B, SBO 128 B;  W: K-major, LBO 128 B, SBO Kp/8*128 B
+      const uint32_t wsbo = (uint32_t)(p.Kp / 8) * 128u;
+      for (int m = 0; m < p.MT; m++) {
+        for (int part = 0; part < NPARTS; part++) {
+          const uint32_t d = dset + (uint32_t)((m * NPARTS + part) * p.Nmma);
+          uint32_t acc = 0;
+          for (int pi = 0; pi < npairs; pi++) {
+            const int ta = p.terms == 3 ? pa3[pi] : 0, tb = p.terms == 3 ? pb3[pi] : 0;
+            for (int pp = 0; pp < p.P; pp++) {
+              const uint32_t xa = tc::smem_u32(xarrp(buf, part, ta, pp)) + (uint32_t)(8 * 128 * m) * 2u;
+              const uint32_t wa = tc::smem_u32(warr(pp, tb));
+              for (int ks = 0; ks < p.Kp / 16; ks++) {
+                const uint64_t ad = tc::smem_desc(xa + ks * 32u, 16u, 128u);
+                const uint64_t bd = tc::smem_desc(wa + ks * 256u, 128u, wsbo);
+                tc::mma_f16(d, ad, bd, idesc, acc);
+                acc = 1;
+              }
+            }
+          }
+        }
+      }
+      tc::mma_commit(&bars[buf]);
+    }
+    // convert the next iteration into the other buffer while the MMAs run
+    const int64_t nxt = it + gridDim.x;
+    if (nxt < p.niters) convert(nxt, buf ^ 1);
+    tc::fence_async_smem();
+    const bool got = tc::mbar_wait(&bars[buf], phase[buf]);
+    phase[buf] ^= 1u;
+    if (!got) {
+      ok = false;
+      if (tid == 0) atomicExch(&g_tc_status, 1);
+    }
+    tc::tc_fence_after();
+    // ---- epilogue: warp quarter w%4 owns TMEM lanes 32*(w%4) .. +32 (rows); warps 0-3 take
+    // even M-tiles, 4-7 odd ones ----
+    if (got) {
+      const int64_t b = it / p.iters_per_row;
+      const int64_t q0 = (it - b * p.iters_per_row) * (int64_t)(128 * p.MT);
+      XT *orow = reinterpret_cast<XT *>(p.out) + b * p.out_bstride;
+      for (int m = warp >> 2; m < p.MT; m += 2) {
+        const int64_t q = q0 + 128 * m + 32 * (warp & 3) + lane;
+        for (int col = 0; col < p.Nmma; col += 16) {
+          uint32_t rr[16], ri[16];
+          const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
+          tc::tmem_ld16(dset + lane_base + (uint32_t)((m * NPARTS) * p.Nmma + col), rr);
+          if constexpr (XC) tc::tmem_ld16(dset + lane_base + (uint32_t)((m * NPARTS + 1) * p.Nmma + col), ri);
+          tc::tmem_ld_wait();
+#pragma unroll
+          for (int i = 0; i < 16; i++) {
+            const int j = col + i;
+            const int64_t n = q * p.Nt + j;
+            if (j < p.Nt && n < p.out_len) {
+              if constexpr (XC) {
+                float2 v;
+                v.x = __uint_as_float(rr[i]);
+                v.y = __uint_as_float(ri[i]);
+                orow[n] = v;
+              } else {
+                orow[n] = __uint_as_float(rr[i]);
+              }
+            }
+          }
+        }
+      }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    if (!ok) break;
+  }
+  // drain: a timed-out wait above leaves MMAs possibly in flight; wait once more (bounded)
+  if (!ok && tid == 0) {
+    (void)tc::mbar_wait(&bars[0], phase[0]);
+    (void)tc::mbar_wait(&bars[1], phase[1]);
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, (uint32_t)p.tmem_cols);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+struct TcPlan {
+  TcParams p;
+  size_t smem;
+  bool ok;
+  char why[160];
+};
+
+static TcPlan plan_tc(int64_t up, int64_t down, int64_t L, int64_t N_in, int64_t out_len, int64_t batch, int xc,
+                      int precision, int rev) {
+  TcPlan pl{};
+  TcParams &p = pl.p;
+  p.even = (L % 2) == 0;
+  p.Lo = L + p.even;
+  p.c = (p.Lo - 1) / 2;
+  p.rev = rev;
+  p.up = up;
+  p.down = down;
+  p.N = N_in;
+  p.out_len = out_len;
+  p.scale = (double)up;
+  p.fp16 = precision == GBFIR_PREC_FP16;
+  p.terms = precision == GBFIR_PREC_BF16X3 ? 3 : 1;
+  p.path = (8 % down == 0) ? 0 : 1;
+  p.P = p.path == 0 ? 1 : (int32_t)down;
+  int64_t kmin, kmax;
+  if (p.path == 0) {
+    p.Nt = (int32_t)(up * (8 / down));
+    kmin = ceil_div(p.c - p.Lo + 1, up);
+    kmax = floor_div(p.c + (int64_t)(p.Nt - 1) * down, up);
+  } else {
+    p.Nt = (int32_t)(8 * up);
+    kmin = INT64_MAX;
+    kmax = INT64_MIN;
+    for (int64_t b = 0; b < down; b++) {
+      kmin = std::min(kmin, ceil_div(p.c - up * b - p.Lo + 1, up * down));
+      kmax = std::max(kmax, floor_div(p.c + down * (int64_t)(p.Nt - 1) - up * b, up * down));
+    }
+  }
+  p.Nmma = (p.Nt + 15) / 16 * 16;
+  p.k0 = floor_div(kmin, 8) * 8;
+  p.Kp = (int32_t)((kmax - p.k0 + 1 + 15) / 16 * 16);
+  if (p.Nmma > 256) {
+    snprintf(pl.why, sizeof(pl.why), "a row of %d outputs exceeds the MMA N limit of 256", p.Nt);
+    return pl;
+  }
+  if (p.P > 16) {
+    snprintf(pl.why, sizeof(pl.why), "down = %lld polyphase components are too many", (long long)down);
+    return pl;
+  }
+  const int nparts = xc ? 2 : 1;
+  auto smem_for = [&](int MT) -> size_t {
+    const size_t w = (size_t)p.P * p.terms * p.Nmma * p.Kp * 2;
+    const size_t la = (size_t)8 * 128 * MT + p.Kp;
+    const size_t xa = (la * 2 + 127) / 128 * 128;
+    return (w + 127) / 128 * 128 + 2 * (size_t)nparts * p.terms * p.P * xa;
+  };
+  int MT = 4;
+  while (MT > 1 && (smem_for(MT) > 200 * 1024 || 2 * MT * nparts * p.Nmma > 512)) MT /= 2;
+  if (2 * MT * nparts * p.Nmma > 512 || smem_for(MT) > 200 * 1024) {
+    snprintf(pl.why, sizeof(pl.why), "tile needs %zu B of shared memory", smem_for(MT));
+    return pl;
+  }
+  p.MT = MT;
+  p.LA = 8 * 128 * MT + p.Kp;
+  uint32_t cols = 32;
+  while (cols < (uint32_t)(2 * MT * nparts * p.Nmma)) cols <<= 1;
+  p.tmem_cols = (int32_t)cols;
+  p.rows = (out_len + p.Nt - 1) / p.Nt;
+  p.iters_per_row = (p.rows + 128 * MT - 1) / (128 * MT);
+  p.niters = p.iters_per_row * batch;
+  pl.smem = smem_for(MT);
+  pl.ok = true;
+  return pl;
+}
+
+int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t up, int64_t down,
+                     int precision, cudaStream_t s) {
+  if (dtype_double(in.dtype) || dtype_complex(h.dtype))
+    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly: tensor-core forms take float32/complex64 signals and real "
+                                        "float32 taps");
+  const bool xc = dtype_complex(in.dtype);
+  TcPlan pl = plan_tc(up, down, h.len, in.len, out.len, out.batch, xc, precision, 0);
+  if (!pl.ok)
+    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly: tensor-core form unavailable for up=%lld down=%lld: %s",
+               (long long)up, (long long)down, pl.why);
+  TcParams &p = pl.p;
+  p.x = in.ptr;
+  p.x_bstride = out.batch > 1 ? in.batch_stride : 0;
+  p.h = reinterpret_cast<const float *>(h.ptr);
+  p.out = out.ptr;
+  p.out_bstride = out.batch_stride;
+  const void *fn = xc ? (const void *)tc_resample_kernel<true> : (const void *)tc_resample_kernel<false>;
+  int rc = ensure_smem(fn, pl.smem, "resample_poly (tensor cores)");
+  if (rc) return rc;
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kTcThreads, pl.smem);
+  if (occ < 1) occ = 1;
+  // each CTA holds tmem_cols of the SM's 512 TMEM columns
+  occ = std::min(occ, 512 / p.tmem_cols);
+  int64_t grid = (int64_t)num_sms() * occ;
+  if (grid > p.niters) grid = p.niters;
+  void *args[] = {&p};
+  cudaError_t e = cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kTcThreads), args, pl.smem, s);
+  if (e != cudaSuccess) GBFIR_FAIL(GBFIR_ERR_CUDA, "resample_poly (tensor cores): %s", cudaGetErrorString(e));
+  count_launch();
+  return GBFIR_SUCCESS;
+}
+
+int tc_status_read_and_clear() {
+  int32_t v = 0, zero = 0;
+  if (cudaMemcpyFromSymbol(&v, g_tc_status, sizeof(v)) != cudaSuccess) return -1;
+  cudaMemcpyToSymbol(g_tc_status, &zero, sizeof(zero));
+  return v;
+}
+
+}  // namespace gbfir
+
+extern "C" int gbfir_tc_status(void) { return gbfir::tc_status_read_and_clear(); }
