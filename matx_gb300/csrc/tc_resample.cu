@@ -52,6 +52,7 @@ struct TcParams {
   int64_t iters_per_row, niters;
   double scale;     // up
   int32_t tmem_cols;
+  int32_t nbuf;     // 2: convert the next iteration during the MMAs; 1: after them
 };
 
 // Bounded-wait status of the tensor-core kernels (1 = a wait gave up); read and
@@ -162,9 +163,11 @@ __global__ void __launch_bounds__(kTcThreads) tc_resample_kernel(const TcParams 
   bool ok = true;
   uint32_t phase[2] = {0, 0};
 
+  const bool dbuf = p.nbuf == 2;
   for (int k = 0; it < p.niters; it += gridDim.x, ++k) {
-    const int buf = k & 1;
-    const uint32_t dset = tmem + (uint32_t)buf * set_cols;
+    const int buf = dbuf ? (k & 1) : 0;  // shared operand buffer
+    const int ts = k & 1;                // TMEM accumulator set and mbarrier
+    const uint32_t dset = tmem + (uint32_t)ts * set_cols;
     if (tid == 0) {
       // A: xs_p + (8*128*m + 16*ks) elements, LBO 16 B, SBO 128 B;  W: K-major, LBO 128 B, SBO Kp/8*128 B
       const uint32_t wsbo = (uint32_t)(p.Kp / 8) * 128u;
@@ -187,14 +190,14 @@ __global__ void __launch_bounds__(kTcThreads) tc_resample_kernel(const TcParams 
           }
         }
       }
-      tc::mma_commit(&bars[buf]);
+      tc::mma_commit(&bars[ts]);
     }
     // convert the next iteration into the other buffer while the MMAs run
     const int64_t nxt = it + gridDim.x;
-    if (nxt < p.niters) convert(nxt, buf ^ 1);
+    if (dbuf && nxt < p.niters) convert(nxt, buf ^ 1);
     tc::fence_async_smem();
-    const bool got = tc::mbar_wait(&bars[buf], phase[buf]);
-    phase[buf] ^= 1u;
+    const bool got = tc::mbar_wait(&bars[ts], phase[ts]);
+    phase[ts] ^= 1u;
     if (!got) {
       ok = false;
       if (tid == 0) atomicExch(&g_tc_status, 1);
@@ -236,6 +239,13 @@ __global__ void __launch_bounds__(kTcThreads) tc_resample_kernel(const TcParams 
     __syncthreads();
     tc::tc_fence_after();
     if (!ok) break;
+    if (!dbuf && nxt < p.niters) {
+      convert(nxt, 0);
+      tc::fence_async_smem();
+      tc::tc_fence_before();
+      __syncthreads();
+      tc::tc_fence_after();
+    }
   }
   // drain: a timed-out wait above leaves MMAs possibly in flight; wait once more (bounded)
   if (!ok && tid == 0) {
@@ -301,19 +311,21 @@ static TcPlan plan_tc(int64_t up, int64_t down, int64_t L, int64_t N_in, int64_t
     return pl;
   }
   const int nparts = xc ? 2 : 1;
-  auto smem_for = [&](int MT) -> size_t {
+  auto smem_for = [&](int MT, int nbuf) -> size_t {
     const size_t w = (size_t)p.P * p.terms * p.Nmma * p.Kp * 2;
     const size_t la = (size_t)8 * 128 * MT + p.Kp;
     const size_t xa = (la * 2 + 127) / 128 * 128;
-    return (w + 127) / 128 * 128 + 2 * (size_t)nparts * p.terms * p.P * xa;
+    return (w + 127) / 128 * 128 + (size_t)nbuf * nparts * p.terms * p.P * xa;
   };
-  int MT = 4;
-  while (MT > 1 && (smem_for(MT) > 200 * 1024 || 2 * MT * nparts * p.Nmma > 512)) MT /= 2;
-  if (2 * MT * nparts * p.Nmma > 512 || smem_for(MT) > 200 * 1024) {
-    snprintf(pl.why, sizeof(pl.why), "tile needs %zu B of shared memory", smem_for(MT));
+  int MT = 4, nbuf = 2;
+  while (MT > 1 && (smem_for(MT, nbuf) > 200 * 1024 || 2 * MT * nparts * p.Nmma > 512)) MT /= 2;
+  if (smem_for(MT, nbuf) > 200 * 1024) nbuf = 1;
+  if (2 * MT * nparts * p.Nmma > 512 || smem_for(MT, nbuf) > 200 * 1024) {
+    snprintf(pl.why, sizeof(pl.why), "tile needs %zu B of shared memory", smem_for(MT, nbuf));
     return pl;
   }
   p.MT = MT;
+  p.nbuf = nbuf;
   p.LA = 8 * 128 * MT + p.Kp;
   uint32_t cols = 32;
   while (cols < (uint32_t)(2 * MT * nparts * p.Nmma)) cols <<= 1;
@@ -321,7 +333,7 @@ static TcPlan plan_tc(int64_t up, int64_t down, int64_t L, int64_t N_in, int64_t
   p.rows = (out_len + p.Nt - 1) / p.Nt;
   p.iters_per_row = (p.rows + 128 * MT - 1) / (128 * MT);
   p.niters = p.iters_per_row * batch;
-  pl.smem = smem_for(MT);
+  pl.smem = smem_for(MT, nbuf);
   pl.ok = true;
   return pl;
 }
