@@ -296,7 +296,7 @@ def run_ragged(args, rank, world, dev):
 
 
 def main():
-    global BATCH
+    global BATCH, RATIOS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=400)
@@ -307,11 +307,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     ap.add_argument("--batch", type=int, default=BATCH, help="rows per GPU (profiling cases)")
     ap.add_argument("--no-tune", action="store_true", help="use the built-in tile heuristic")
+    ap.add_argument("--ratios", default="3/2,4/5,160/147", help="comma-separated up/down list (profiling cases)")
     ap.add_argument("--workload", default="resample", choices=["resample", "ragged"],
                     help="ragged: 4096 uneven signals in one persistent launch (separate JSON line)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     BATCH = args.batch
+    RATIOS = [tuple(int(v) for v in r.split("/")) for r in args.ratios.split(",")]
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -84,6 +84,10 @@ __global__ void __launch_bounds__(kTcThreads) tc_resample_kernel(const TcParams 
   auto xarrp = [&](int buf, int part, int t, int pp) {
     return xbase + ((((size_t)buf * NPARTS + part) * p.terms + t) * p.P + pp) * xarr;
   };
+  // raw input ring: two slots of P*LA samples (x as stored in HBM), filled by cp.async
+  const size_t raw_elems = (size_t)p.P * p.LA;
+  XT *raw0 = reinterpret_cast<XT *>(xbase + (size_t)p.nbuf * NPARTS * p.terms * p.P * xarr);
+  auto rawp = [&](int slot) { return raw0 + (size_t)slot * raw_elems; };
 
   if (warp == 0) tc::tmem_alloc(&tmem_slot, (uint32_t)p.tmem_cols);
   if (tid == 0) {
@@ -117,40 +121,62 @@ __global__ void __launch_bounds__(kTcThreads) tc_resample_kernel(const TcParams 
     }
   }
 
-  // ---- input conversion of one iteration into buffer `buf` ----
+  // ---- input staging: raw samples of one iteration into a ring slot (cp.async, zero-filled) ----
   const XT *xp = reinterpret_cast<const XT *>(p.x);
-  auto convert = [&](int64_t it, int buf) {
-    const int64_t b = it / p.iters_per_row;
-    const int64_t q0 = (it - b * p.iters_per_row) * (int64_t)(128 * p.MT);
+  auto fetch = [&](int64_t itx, int slot) {
+    const int64_t b = itx / p.iters_per_row;
+    const int64_t q0 = (itx - b * p.iters_per_row) * (int64_t)(128 * p.MT);
     const XT *row = xp + b * p.x_bstride;
-    // path A: xs[u] = x[8*q0 + k0 + u]; path B: xs_b[u] = x[down*(8*q0 + k0 + u) + b]
+    // path A: raw[v] = x[8*q0 + k0 + v]; path B: raw[v] = x[down*(8*q0 + k0) + v], v = P*u + b
     const int64_t base = p.path == 0 ? 8 * q0 + p.k0 : p.down * (8 * q0 + p.k0);
-    for (int pp = 0; pp < p.P; pp++) {
-    for (int u = tid; u < p.LA; u += kTcThreads) {
-      const int64_t gi = base + (int64_t)u * p.P + pp;  // path A: P == 1, pp == 0
-      XT xv = zero_val<XT>();
-      if (gi >= 0 && gi < p.N) xv = row[gi];
+    XT *dst = rawp(slot);
+    for (int v = tid; v < (int)raw_elems; v += kTcThreads) {
+      const int64_t gi = base + v;
+      const bool okk = gi >= 0 && gi < p.N;
+      cp_async_zfill<sizeof(XT)>(dst + v, okk ? (const void *)(row + gi) : (const void *)row, okk);
+    }
+  };
+  // ---- conversion of a staged slot into the bf16/fp16 term arrays of buffer `buf` ----
+  // Each thread converts two consecutive samples of one component (4-byte stores).
+  auto convert = [&](int slot, int buf) {
+    const XT *src = rawp(slot);
+    const int half = (p.LA + 1) / 2;
+    for (int e = tid; e < p.P * half; e += kTcThreads) {
+      const int pp = e / half, u = 2 * (e - pp * half);
+      const XT v0 = src[(size_t)u * p.P + pp];
+      const XT v1 = (u + 1 < p.LA) ? src[(size_t)(u + 1) * p.P + pp] : zero_val<XT>();
 #pragma unroll
       for (int part = 0; part < NPARTS; part++) {
-        const float f = part == 0 ? re_of(xv) : im_of(xv);
+        const float f0 = part == 0 ? re_of(v0) : im_of(v0);
+        const float f1 = part == 0 ? re_of(v1) : im_of(v1);
         if (p.fp16) {
-          reinterpret_cast<__half *>(xarrp(buf, part, 0, pp))[u] = __float2half_rn(f);
+          *reinterpret_cast<__half2 *>(reinterpret_cast<__half *>(xarrp(buf, part, 0, pp)) + u) =
+              __floats2half2_rn(f0, f1);
         } else {
-          __nv_bfloat16 t0, t1, t2;
-          tc::split3_bf16(f, t0, t1, t2);
-          reinterpret_cast<__nv_bfloat16 *>(xarrp(buf, part, 0, pp))[u] = t0;
+          __nv_bfloat16 a0, a1, a2, b0, b1, b2;
+          tc::split3_bf16(f0, a0, a1, a2);
+          tc::split3_bf16(f1, b0, b1, b2);
+          *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<__nv_bfloat16 *>(xarrp(buf, part, 0, pp)) + u) =
+              __halves2bfloat162(a0, b0);
           if (p.terms == 3) {
-            reinterpret_cast<__nv_bfloat16 *>(xarrp(buf, part, 1, pp))[u] = t1;
-            reinterpret_cast<__nv_bfloat16 *>(xarrp(buf, part, 2, pp))[u] = t2;
+            *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<__nv_bfloat16 *>(xarrp(buf, part, 1, pp)) + u) =
+                __halves2bfloat162(a1, b1);
+            *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<__nv_bfloat16 *>(xarrp(buf, part, 2, pp)) + u) =
+                __halves2bfloat162(a2, b2);
           }
         }
       }
     }
-    }
   };
 
   int64_t it = blockIdx.x;
-  if (it < p.niters) convert(it, 0);
+  if (it < p.niters) fetch(it, 0);
+  cp_async_commit();
+  if (it + gridDim.x < p.niters) fetch(it + gridDim.x, 1);
+  cp_async_commit();
+  cp_async_wait<1>();
+  __syncthreads();
+  if (it < p.niters) convert(0, 0);
   tc::fence_async_smem();
   tc::tc_fence_before();
   __syncthreads();
@@ -192,9 +218,15 @@ __global__ void __launch_bounds__(kTcThreads) tc_resample_kernel(const TcParams 
       }
       tc::mma_commit(&bars[ts]);
     }
-    // convert the next iteration into the other buffer while the MMAs run
+    // stage iteration k+2 into the raw slot iteration k used, then convert iteration k+1
+    // (staged one iteration ago) into the other operand buffer while the MMAs run
     const int64_t nxt = it + gridDim.x;
-    if (dbuf && nxt < p.niters) convert(nxt, buf ^ 1);
+    const int64_t nxt2 = nxt + gridDim.x;
+    if (nxt2 < p.niters) fetch(nxt2, k & 1);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    if (dbuf && nxt < p.niters) convert((k + 1) & 1, buf ^ 1);
     tc::fence_async_smem();
     const bool got = tc::mbar_wait(&bars[ts], phase[ts]);
     phase[ts] ^= 1u;
@@ -240,13 +272,14 @@ __global__ void __launch_bounds__(kTcThreads) tc_resample_kernel(const TcParams 
     tc::tc_fence_after();
     if (!ok) break;
     if (!dbuf && nxt < p.niters) {
-      convert(nxt, 0);
+      convert((k + 1) & 1, 0);
       tc::fence_async_smem();
       tc::tc_fence_before();
       __syncthreads();
       tc::tc_fence_after();
     }
   }
+  cp_async_wait<0>();
   // drain: a timed-out wait above leaves MMAs possibly in flight; wait once more (bounded)
   if (!ok && tid == 0) {
     (void)tc::mbar_wait(&bars[0], phase[0]);
@@ -315,10 +348,12 @@ static TcPlan plan_tc(int64_t up, int64_t down, int64_t L, int64_t N_in, int64_t
     const size_t w = (size_t)p.P * p.terms * p.Nmma * p.Kp * 2;
     const size_t la = (size_t)8 * 128 * MT + p.Kp;
     const size_t xa = (la * 2 + 127) / 128 * 128;
-    return (w + 127) / 128 * 128 + (size_t)nbuf * nparts * p.terms * p.P * xa;
+    const size_t raw = 2 * (size_t)p.P * la * (xc ? 8 : 4);
+    return (w + 127) / 128 * 128 + (size_t)nbuf * nparts * p.terms * p.P * xa + raw;
   };
+  // prefer two CTAs per SM (<= 110 KB each), then one CTA with double buffering, then single
   int MT = 4, nbuf = 2;
-  while (MT > 1 && (smem_for(MT, nbuf) > 200 * 1024 || 2 * MT * nparts * p.Nmma > 512)) MT /= 2;
+  while (MT > 1 && (smem_for(MT, nbuf) > 110 * 1024 || 2 * MT * nparts * p.Nmma > 256)) MT /= 2;
   if (smem_for(MT, nbuf) > 200 * 1024) nbuf = 1;
   if (2 * MT * nparts * p.Nmma > 512 || smem_for(MT, nbuf) > 200 * 1024) {
     snprintf(pl.why, sizeof(pl.why), "tile needs %zu B of shared memory", smem_for(MT, nbuf));
