@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(kTcThreads) tc_resample_kernel(const TcParams 
   int64_t it = blockIdx.x;
   if (it < p.niters) fetch(it, 0);
   cp_async_commit();
-  if (it + gridDim.x < p.niters) fetch(it + gridDim.x, 1);
+  if (p.nbuf == 2 && it + gridDim.x < p.niters) fetch(it + gridDim.x, 1);
   cp_async_commit();
   cp_async_wait<1>();
   __syncthreads();
@@ -195,8 +195,10 @@ __global__ void __launch_bounds__(kTcThreads) tc_resample_kernel(const TcParams 
     const int ts = k & 1;                // TMEM accumulator set and mbarrier
     const uint32_t dset = tmem + (uint32_t)ts * set_cols;
     if (tid == 0) {
-      // A: xs_p + (8*128*m + 16*ks) elements, LBO 16 B, SBO 128 B;  W: K-major, LBO 128 B, SBO Kp/8*128 B
+      // A: xs_p + (8*128*m + 16*ks) elements, LBO 16 B, SBO 128 B;  W: K-major, LBO 128 B, SBO Kp/8*128 B.
+      // Advancing one K-step adds 32 B to A's start address and 256 B to W's (start field is in 16 B units).
       const uint32_t wsbo = (uint32_t)(p.Kp / 8) * 128u;
+      const int nks = p.Kp / 16;
       for (int m = 0; m < p.MT; m++) {
         for (int part = 0; part < NPARTS; part++) {
           const uint32_t d = dset + (uint32_t)((m * NPARTS + part) * p.Nmma);
@@ -204,13 +206,14 @@ __global__ void __launch_bounds__(kTcThreads) tc_resample_kernel(const TcParams 
           for (int pi = 0; pi < npairs; pi++) {
             const int ta = p.terms == 3 ? pa3[pi] : 0, tb = p.terms == 3 ? pb3[pi] : 0;
             for (int pp = 0; pp < p.P; pp++) {
-              const uint32_t xa = tc::smem_u32(xarrp(buf, part, ta, pp)) + (uint32_t)(8 * 128 * m) * 2u;
-              const uint32_t wa = tc::smem_u32(warr(pp, tb));
-              for (int ks = 0; ks < p.Kp / 16; ks++) {
-                const uint64_t ad = tc::smem_desc(xa + ks * 32u, 16u, 128u);
-                const uint64_t bd = tc::smem_desc(wa + ks * 256u, 128u, wsbo);
+              uint64_t ad = tc::smem_desc(tc::smem_u32(xarrp(buf, part, ta, pp)) + (uint32_t)(8 * 128 * m) * 2u, 16u,
+                                          128u);
+              uint64_t bd = tc::smem_desc(tc::smem_u32(warr(pp, tb)), 128u, wsbo);
+              for (int ks = 0; ks < nks; ks++) {
                 tc::mma_f16(d, ad, bd, idesc, acc);
                 acc = 1;
+                ad += 2;   // +32 B
+                bd += 16;  // +256 B
               }
             }
           }
@@ -222,11 +225,13 @@ __global__ void __launch_bounds__(kTcThreads) tc_resample_kernel(const TcParams 
     // (staged one iteration ago) into the other operand buffer while the MMAs run
     const int64_t nxt = it + gridDim.x;
     const int64_t nxt2 = nxt + gridDim.x;
-    if (nxt2 < p.niters) fetch(nxt2, k & 1);
-    cp_async_commit();
-    cp_async_wait<1>();
-    __syncthreads();
-    if (dbuf && nxt < p.niters) convert((k + 1) & 1, buf ^ 1);
+    if (dbuf) {
+      if (nxt2 < p.niters) fetch(nxt2, k & 1);
+      cp_async_commit();
+      cp_async_wait<1>();
+      __syncthreads();
+      if (nxt < p.niters) convert((k + 1) & 1, buf ^ 1);
+    }
     tc::fence_async_smem();
     const bool got = tc::mbar_wait(&bars[ts], phase[ts]);
     phase[ts] ^= 1u;
@@ -272,7 +277,11 @@ __global__ void __launch_bounds__(kTcThreads) tc_resample_kernel(const TcParams 
     tc::tc_fence_after();
     if (!ok) break;
     if (!dbuf && nxt < p.niters) {
-      convert((k + 1) & 1, 0);
+      fetch(nxt, 0);
+      cp_async_commit();
+      cp_async_wait<0>();
+      __syncthreads();
+      convert(0, 0);
       tc::fence_async_smem();
       tc::tc_fence_before();
       __syncthreads();
@@ -348,7 +357,7 @@ static TcPlan plan_tc(int64_t up, int64_t down, int64_t L, int64_t N_in, int64_t
     const size_t w = (size_t)p.P * p.terms * p.Nmma * p.Kp * 2;
     const size_t la = (size_t)8 * 128 * MT + p.Kp;
     const size_t xa = (la * 2 + 127) / 128 * 128;
-    const size_t raw = 2 * (size_t)p.P * la * (xc ? 8 : 4);
+    const size_t raw = (size_t)nbuf * p.P * la * (xc ? 8 : 4);
     return (w + 127) / 128 * 128 + (size_t)nbuf * nparts * p.terms * p.P * xa + raw;
   };
   // prefer two CTAs per SM (<= 110 KB each), then one CTA with double buffering, then single
@@ -394,6 +403,7 @@ int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf 
   if (rc) return rc;
   int occ = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kTcThreads, pl.smem);
+  if (pl.smem <= 110 * 1024) occ = std::max(occ, 2);
   if (occ < 1) occ = 1;
   // each CTA holds tmem_cols of the SM's 512 TMEM columns
   occ = std::min(occ, 512 / p.tmem_cols);
