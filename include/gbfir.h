@@ -155,6 +155,28 @@ GBFIR_API int gbfir_conv1d_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_b
                      gbfir_buf h, int32_t mode, void *workspace,
                      size_t workspace_bytes, gbfir_stream_t stream);
 
+/* Allocation-free variant of gbfir_resample_poly_bwd.  It has no counterpart in
+ * the reference library.  It is for callers that cannot hand this library a device
+ * workspace: callers whose calling convention has no slot for one (an operator
+ * signature fixed by another framework), and callers that must not touch the device
+ * allocator while they run (processing loops with a fixed memory budget, plugins
+ * inside a host application that owns every device allocation).
+ * Arguments and results are those of gbfir_resample_poly_bwd; the FP64 partial tap
+ * gradients live in a scratch array compiled into the library instead of in a
+ * caller workspace.  That array holds GBFIR_NOALLOC_SCRATCH_BYTES per device and stays
+ * resident on every GPU that loads the library until the process exits.  A call whose
+ * partials do not fit (about 2 * SMs * (h_len + 1) * 8 bytes) is rejected with
+ * GBFIR_ERR_INVALID_SIZE before any device work.  Nothing here calls cudaMalloc or
+ * cudaFree.  The first call on each device looks the array's device address up
+ * (cudaGetSymbolAddress) with that device current; make that first call before any
+ * stream capture.  All calls share the one array: calls whose work overlaps on the
+ * GPU (different streams without ordering, or different host threads) race on it and
+ * must be serialised by the caller. */
+#define GBFIR_NOALLOC_SCRATCH_BYTES (4u << 20)
+GBFIR_API int gbfir_resample_poly_bwd_noalloc(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy,
+                                              gbfir_buf x, gbfir_buf h, int64_t up,
+                                              int64_t down, gbfir_stream_t stream);
+
 /* ---- ragged batches (no MatX counterpart) --------------------------------
  * One persistent launch resamples `count` independent complex64 signals of
  * uneven length, tap count and up/down ratio.  Descriptors live in device

@@ -15,6 +15,8 @@
 // persistent CTA walks its row tiles (x window and gy tile double-buffered with
 // cp.async); the per-thread FP32 sums are reduced across row slices and CTAs in
 // FP64, in a fixed order, so the result is deterministic.
+#include <mutex>
+
 #include "rowtile.cuh"
 
 namespace gbfir {
@@ -331,6 +333,38 @@ static int run_dh(DhPlan &pl, int64_t batch, int64_t L, int64_t even_off, double
   return check_launch("backward dh reduce");
 }
 
+
+// ---- allocation-free backward -----------------------------------------------------
+// Scratch for gbfir_resample_poly_bwd_noalloc: the FP64 partial tap gradients of the
+// dh reduction, GBFIR_NOALLOC_SCRATCH_BYTES per device.  Host code must not use the
+// array's name as an address (it is a host-side stand-in); the device address is
+// looked up per device with cudaGetSymbolAddress and passed to the kernels.  Each call
+// writes every partial it later reads, so nothing has to be cleared between calls.
+static __device__ __align__(256) double g_noalloc_scratch[GBFIR_NOALLOC_SCRATCH_BYTES / sizeof(double)];
+
+static void *noalloc_scratch_address(int *rc_out) {
+  static std::mutex mu;
+  static void *addr[128] = {nullptr};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 128) {
+    *rc_out = GBFIR_ERR_CUDA;
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  if (!addr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      *rc_out = GBFIR_ERR_CUDA;
+      return nullptr;
+    }
+    addr[dev] = p;
+  }
+  *rc_out = GBFIR_SUCCESS;
+  return addr[dev];
+}
+
 static int check_real(const gbfir_buf &b, const char *name, bool allow_broadcast) {
   int rc = check_buf(b, name, allow_broadcast);
   if (rc) return rc;
@@ -408,6 +442,83 @@ int gbfir_resample_poly_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf 
     return GBFIR_SUCCESS;
   } catch (...) {
     GBFIR_FAIL(GBFIR_ERR_CUDA, "resample_poly_bwd: internal exception");
+  }
+}
+
+
+int gbfir_resample_poly_bwd_noalloc(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x, gbfir_buf h, int64_t up,
+                                    int64_t down, gbfir_stream_t stream) {
+  try {
+    int rc;
+    if ((rc = check_real(gy, "resample_poly_bwd_noalloc gy", false))) return rc;
+    if ((rc = check_real(x, "resample_poly_bwd_noalloc x", false))) return rc;
+    if ((rc = check_real(h, "resample_poly_bwd_noalloc h", false))) return rc;
+    if (up <= 0 || down <= 0)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "resample_poly_bwd_noalloc: up/down must be positive");
+    if (h.batch != 1) GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "resample_poly_bwd_noalloc: the filter must be one row");
+    if (gy.batch != x.batch) GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "resample_poly_bwd_noalloc: gy/x batch mismatch");
+    const int64_t up_size = x.len * up;
+    const int64_t olen = up_size / down + ((up_size % down) ? 1 : 0);
+    if (gy.len != olen)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "resample_poly_bwd_noalloc: gy length %lld, expected %lld",
+                 (long long)gy.len, (long long)olen);
+    if (dx.ptr) {
+      if ((rc = check_real(dx, "resample_poly_bwd_noalloc dx", false))) return rc;
+      if (dx.batch != x.batch || dx.len != x.len)
+        GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "resample_poly_bwd_noalloc: dx shape");
+    }
+    if (dh.ptr) {
+      if ((rc = check_real(dh, "resample_poly_bwd_noalloc dh", false))) return rc;
+      if (dh.batch != 1 || dh.len != h.len) GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "resample_poly_bwd_noalloc: dh shape");
+    }
+    const int64_t g = gcd64(up, down);
+    up /= g;
+    down /= g;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    DhPlan pl{};
+    const bool need_dh = dh.ptr && !(up == 1 && down == 1);
+    if (need_dh) {
+      pl = plan_dh((const float *)x.ptr, x.batch_stride, x.len, (const float *)gy.ptr, gy.batch_stride, gy.len,
+                   x.batch, h.len, up, down, -1, true);
+      const size_t need = (size_t)pl.grid * pl.p.Lo * sizeof(double);
+      if (need > GBFIR_NOALLOC_SCRATCH_BYTES)
+        GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE,
+                   "resample_poly_bwd_noalloc: %lld taps need %zu B of scratch, the built-in maximum is %u B; use "
+                   "gbfir_resample_poly_bwd with a workspace",
+                   (long long)h.len, need, (unsigned)GBFIR_NOALLOC_SCRATCH_BYTES);
+    }
+    int src = GBFIR_SUCCESS;
+    void *scratch = need_dh ? noalloc_scratch_address(&src) : nullptr;
+    if (need_dh && !scratch)
+      GBFIR_FAIL(src, "resample_poly_bwd_noalloc: cannot look up the scratch address on the current device");
+    if (up == 1 && down == 1) {  // forward was an identity copy
+      if (dx.ptr) {
+        cudaError_t e = cudaMemcpy2DAsync(dx.ptr, (size_t)std::max<int64_t>(dx.batch_stride, dx.len) * 4, gy.ptr,
+                                          (size_t)std::max<int64_t>(gy.batch_stride, gy.len) * 4, (size_t)x.len * 4,
+                                          (size_t)x.batch, cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess)
+          GBFIR_FAIL(GBFIR_ERR_CUDA, "resample_poly_bwd_noalloc: copy failed: %s", cudaGetErrorString(e));
+      }
+      if (dh.ptr) {
+        cudaError_t e = cudaMemsetAsync(dh.ptr, 0, (size_t)h.len * 4, s);
+        if (e != cudaSuccess)
+          GBFIR_FAIL(GBFIR_ERR_CUDA, "resample_poly_bwd_noalloc: memset failed: %s", cudaGetErrorString(e));
+      }
+      return GBFIR_SUCCESS;
+    }
+    if (dx.ptr) {
+      TileChoice tc;
+      rc = resample_pass<float, false, false>(gy.ptr, gy.batch_stride, gy.len, h.ptr, h.len, dx.ptr, dx.batch_stride,
+                                              x.len, x.batch, down, up, -1, true, 1, (double)up, tc, s);
+      if (rc) return rc;
+    }
+    if (need_dh) {
+      const int64_t even = (h.len % 2) == 0;
+      return run_dh(pl, x.batch, h.len, even, (double)up, (float *)dh.ptr, scratch, GBFIR_NOALLOC_SCRATCH_BYTES, s);
+    }
+    return GBFIR_SUCCESS;
+  } catch (...) {
+    GBFIR_FAIL(GBFIR_ERR_CUDA, "resample_poly_bwd_noalloc: internal exception");
   }
 }
 
