@@ -21,6 +21,8 @@ int channelize_poly_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_bu
                        cudaStream_t s);
 int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t up, int64_t down,
                      int precision, cudaStream_t s);
+int channelize_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t M, int64_t D,
+                       int precision, cudaStream_t s);
 int set_resample_tile(int rq, int wc, int group, int nbuf);
 int register_resample_tile(int64_t up, int64_t down, int64_t L, int rq, int wc, int group, int nbuf);
 int clear_resample_tiles();
@@ -195,7 +197,7 @@ int gbfir_channelize_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t M, i
       GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "channelize_poly: output row must hold T*M = %lld elements (got %lld)",
                  (long long)(T * M), (long long)out.len);
     if (precision != GBFIR_PREC_FP32)
-      GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "channelize_poly: only the FP32 form is available");
+      return channelize_poly_tc(out, in, h, M, D, precision, reinterpret_cast<cudaStream_t>(stream));
     return channelize_poly_fp(out, in, h, M, D, reinterpret_cast<cudaStream_t>(stream));
   } catch (...) {
     GBFIR_FAIL(GBFIR_ERR_CUDA, "channelize_poly: internal exception");

@@ -18,11 +18,15 @@
 // same W.  bf16x3 splits both operands into three bf16 terms and accumulates the six
 // products of order <= 2 (smallest first) — 24 significant bits, FP32-class accuracy.
 //
-// Pipeline (persistent CTA, 256 threads).  An iteration covers MT M-tiles of 128 rows.
-// Threads convert the next iteration's input samples into the bf16 term arrays of the
-// other shared buffer while one thread's MMAs for the current iteration run into one
-// of two TMEM accumulator sets; after a bounded mbarrier wait every warp reads its TMEM
-// lanes back and stores the outputs.
+// bf16x3 concatenates the three tap terms along N (W_cat = [b0 | b1 | b2]) so one K-step
+// is three MMAs — a0*[b0|b1|b2] into D[0:3N), a1*[b0|b1] into D[N:3N), a2*b0 into
+// D[2N:3N) — and the epilogue sums the three column blocks: exactly the six products of
+// order <= 2, with the small terms accumulated apart from a0*b0.
+//
+// Pipeline (persistent, warp-specialised CTA; roles below).  A stage covers MT M-tiles
+// of 128 rows; raw input is staged two stages ahead with cp.async, converted into a
+// two-slot operand ring, multiplied into one of two TMEM accumulator sets and drained
+// by the epilogue warps while the next stage's MMAs run.
 #include "rowtile.cuh"
 #include "tc.cuh"
 
@@ -66,40 +70,63 @@ __device__ __forceinline__ float tap_value(const TcParams &p, int64_t tp) {
   return p.h[te - p.even];
 }
 
+// Warp roles (12 warps): warp 0 lane 0 issues the MMAs; warps 1-7 stage raw input with
+// cp.async and convert it into the operand ring; warps 8-11 (one per TMEM lane quarter)
+// drain finished accumulators.  Handoffs use mbarriers: op_full / op_empty per operand
+// slot, tm_full / tm_empty per TMEM accumulator set.  Every wait is bounded.
+constexpr int kWsThreads = 384;
+constexpr int kProdWarp0 = 1, kProdWarps = 7, kEpiWarp0 = 8;
+constexpr int kNProd = kProdWarps * 32;
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(tc::smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void named_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 template <bool XC>
-__global__ void __launch_bounds__(kTcThreads) tc_resample_kernel(const TcParams p) {
+__global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcParams p) {
   using XT = typename val_of<float, XC>::type;
   constexpr int NPARTS = XC ? 2 : 1;  // real / imaginary operand rows
   extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ uint64_t bars[2];
+  __shared__ uint64_t op_full[2], op_empty[2], tm_full[2], tm_empty[2];
   __shared__ uint32_t tmem_slot;
+  __shared__ int s_fail, s_pok, s_eok;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-  // shared layout: W [P][terms][Nmma x Kp] ; xs [2 bufs][NPARTS][terms][P][LA]
-  const uint32_t wbytes = (uint32_t)p.Nmma * p.Kp * 2u;
+  // shared layout: W_cat [P][terms*Nmma rows][Kp] ; operand ring [2][NPARTS][terms][P][LA] ; raw ring [2][P*LA]
+  const int wrows = p.terms * p.Nmma;
+  const uint32_t wbytes = (uint32_t)wrows * p.Kp * 2u;
   unsigned char *wbase = smem;
-  unsigned char *xbase = smem + ((size_t)p.P * p.terms * wbytes + 127) / 128 * 128;
-  const size_t xarr = ((size_t)p.LA * 2 + 127) / 128 * 128;  // bytes per xs array
-  auto warr = [&](int pp, int t) { return wbase + ((size_t)pp * p.terms + t) * wbytes; };
-  auto xarrp = [&](int buf, int part, int t, int pp) {
-    return xbase + ((((size_t)buf * NPARTS + part) * p.terms + t) * p.P + pp) * xarr;
+  unsigned char *xbase = smem + ((size_t)p.P * wbytes + 127) / 128 * 128;
+  const size_t xarr = ((size_t)p.LA * 2 + 127) / 128 * 128;
+  auto warr = [&](int pp) { return wbase + (size_t)pp * wbytes; };
+  auto xarrp = [&](int slot, int part, int t, int pp) {
+    return xbase + ((((size_t)slot * NPARTS + part) * p.terms + t) * p.P + pp) * xarr;
   };
-  // raw input ring: two slots of P*LA samples (x as stored in HBM), filled by cp.async
   const size_t raw_elems = (size_t)p.P * p.LA;
-  XT *raw0 = reinterpret_cast<XT *>(xbase + (size_t)p.nbuf * NPARTS * p.terms * p.P * xarr);
+  XT *raw0 = reinterpret_cast<XT *>(xbase + (size_t)2 * NPARTS * p.terms * p.P * xarr);
   auto rawp = [&](int slot) { return raw0 + (size_t)slot * raw_elems; };
 
   if (warp == 0) tc::tmem_alloc(&tmem_slot, (uint32_t)p.tmem_cols);
   if (tid == 0) {
-    tc::mbar_init(&bars[0], 1);
-    tc::mbar_init(&bars[1], 1);
+    for (int i = 0; i < 2; i++) {
+      tc::mbar_init(&op_full[i], 1);
+      tc::mbar_init(&op_empty[i], 1);
+      tc::mbar_init(&tm_full[i], 1);
+      tc::mbar_init(&tm_empty[i], 1);
+    }
+    s_fail = 0;
     tc::mbar_fence_init();
   }
-  // ---- tap matrices W_p[j][k] (K-major core layout), split into terms ----
-  const int wel = p.Nmma * p.Kp;
-  for (int e = tid; e < p.P * wel; e += kTcThreads) {
+  // ---- W_cat[pp][t*Nmma + j][k] = term t of up*he[tap(j, k)] (K-major core layout) ----
+  const int wel = wrows * p.Kp;
+  for (int e = tid; e < p.P * wel; e += kWsThreads) {
     const int pp = e / wel, r = e - pp * wel;
-    const int j = r / p.Kp, k = r - j * p.Kp;
+    const int row = r / p.Kp, k = r - row * p.Kp;
+    const int t = row / p.Nmma, j = row - t * p.Nmma;
     float v = 0.f;
     if (j < p.Nt) {
       const int64_t kk = k + p.k0;
@@ -107,192 +134,214 @@ __global__ void __launch_bounds__(kTcThreads) tc_resample_kernel(const TcParams 
                                      : p.c + p.down * (int64_t)j - p.up * (pp + p.down * kk);
       v = tap_value(p, tp) * (float)p.scale;
     }
-    const uint32_t off = tc::kmajor_offset(j, k, p.Kp);
+    const uint32_t off = tc::kmajor_offset(row, k, p.Kp);
     if (p.fp16) {
-      *reinterpret_cast<__half *>(warr(pp, 0) + off) = __float2half_rn(v);
+      *reinterpret_cast<__half *>(warr(pp) + off) = __float2half_rn(v);
     } else {
       __nv_bfloat16 t0, t1, t2;
       tc::split3_bf16(v, t0, t1, t2);
-      *reinterpret_cast<__nv_bfloat16 *>(warr(pp, 0) + off) = t0;
-      if (p.terms == 3) {
-        *reinterpret_cast<__nv_bfloat16 *>(warr(pp, 1) + off) = t1;
-        *reinterpret_cast<__nv_bfloat16 *>(warr(pp, 2) + off) = t2;
-      }
+      *reinterpret_cast<__nv_bfloat16 *>(warr(pp) + off) = t == 0 ? t0 : (t == 1 ? t1 : t2);
     }
   }
-
-  // ---- input staging: raw samples of one iteration into a ring slot (cp.async, zero-filled) ----
-  const XT *xp = reinterpret_cast<const XT *>(p.x);
-  auto fetch = [&](int64_t itx, int slot) {
-    const int64_t b = itx / p.iters_per_row;
-    const int64_t q0 = (itx - b * p.iters_per_row) * (int64_t)(128 * p.MT);
-    const XT *row = xp + b * p.x_bstride;
-    // path A: raw[v] = x[8*q0 + k0 + v]; path B: raw[v] = x[down*(8*q0 + k0) + v], v = P*u + b
-    const int64_t base = p.path == 0 ? 8 * q0 + p.k0 : p.down * (8 * q0 + p.k0);
-    XT *dst = rawp(slot);
-    for (int v = tid; v < (int)raw_elems; v += kTcThreads) {
-      const int64_t gi = base + v;
-      const bool okk = gi >= 0 && gi < p.N;
-      cp_async_zfill<sizeof(XT)>(dst + v, okk ? (const void *)(row + gi) : (const void *)row, okk);
-    }
-  };
-  // ---- conversion of a staged slot into the bf16/fp16 term arrays of buffer `buf` ----
-  // Each thread converts two consecutive samples of one component (4-byte stores).
-  auto convert = [&](int slot, int buf) {
-    const XT *src = rawp(slot);
-    const int half = (p.LA + 1) / 2;
-    for (int e = tid; e < p.P * half; e += kTcThreads) {
-      const int pp = e / half, u = 2 * (e - pp * half);
-      const XT v0 = src[(size_t)u * p.P + pp];
-      const XT v1 = (u + 1 < p.LA) ? src[(size_t)(u + 1) * p.P + pp] : zero_val<XT>();
-#pragma unroll
-      for (int part = 0; part < NPARTS; part++) {
-        const float f0 = part == 0 ? re_of(v0) : im_of(v0);
-        const float f1 = part == 0 ? re_of(v1) : im_of(v1);
-        if (p.fp16) {
-          *reinterpret_cast<__half2 *>(reinterpret_cast<__half *>(xarrp(buf, part, 0, pp)) + u) =
-              __floats2half2_rn(f0, f1);
-        } else {
-          __nv_bfloat16 a0, a1, a2, b0, b1, b2;
-          tc::split3_bf16(f0, a0, a1, a2);
-          tc::split3_bf16(f1, b0, b1, b2);
-          *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<__nv_bfloat16 *>(xarrp(buf, part, 0, pp)) + u) =
-              __halves2bfloat162(a0, b0);
-          if (p.terms == 3) {
-            *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<__nv_bfloat16 *>(xarrp(buf, part, 1, pp)) + u) =
-                __halves2bfloat162(a1, b1);
-            *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<__nv_bfloat16 *>(xarrp(buf, part, 2, pp)) + u) =
-                __halves2bfloat162(a2, b2);
-          }
-        }
-      }
-    }
-  };
-
-  int64_t it = blockIdx.x;
-  if (it < p.niters) fetch(it, 0);
-  cp_async_commit();
-  if (p.nbuf == 2 && it + gridDim.x < p.niters) fetch(it + gridDim.x, 1);
-  cp_async_commit();
-  cp_async_wait<1>();
-  __syncthreads();
-  if (it < p.niters) convert(0, 0);
   tc::fence_async_smem();
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = tmem_slot;
-  const uint32_t set_cols = (uint32_t)(p.MT * NPARTS * p.Nmma);
-  const uint32_t idesc = tc::idesc_f16(128, (uint32_t)p.Nmma, p.fp16 ? 0u : 1u);
-  const int pa3[6] = {2, 1, 0, 1, 0, 0}, pb3[6] = {0, 1, 2, 0, 1, 0};
-  const int npairs = p.terms == 3 ? 6 : 1;
-  bool ok = true;
-  uint32_t phase[2] = {0, 0};
+  const uint32_t set_cols = (uint32_t)(p.MT * NPARTS * wrows);
+  const XT *xp = reinterpret_cast<const XT *>(p.x);
 
-  const bool dbuf = p.nbuf == 2;
-  for (int k = 0; it < p.niters; it += gridDim.x, ++k) {
-    const int buf = dbuf ? (k & 1) : 0;  // shared operand buffer
-    const int ts = k & 1;                // TMEM accumulator set and mbarrier
-    const uint32_t dset = tmem + (uint32_t)ts * set_cols;
-    if (tid == 0) {
-      // A: xs_p + (8*128*m + 16*ks) elements, LBO 16 B, SBO 128 B;  W: K-major, LBO 128 B, SBO Kp/8*128 B.
-      // Advancing one K-step adds 32 B to A's start address and 256 B to W's (start field is in 16 B units).
-      const uint32_t wsbo = (uint32_t)(p.Kp / 8) * 128u;
-      const int nks = p.Kp / 16;
-      for (int m = 0; m < p.MT; m++) {
+  if (warp >= kProdWarp0 && warp < kProdWarp0 + kProdWarps) {
+    // ================= producers =================
+    const int ptid = tid - kProdWarp0 * 32;
+    auto fetch = [&](int64_t itx, int slot) {
+      const int64_t b = itx / p.iters_per_row;
+      const int64_t q0 = (itx - b * p.iters_per_row) * (int64_t)(128 * p.MT);
+      const XT *row = xp + b * p.x_bstride;
+      const int64_t base = p.path == 0 ? 8 * q0 + p.k0 : p.down * (8 * q0 + p.k0);
+      XT *dst = rawp(slot);
+      for (int v = ptid; v < (int)raw_elems; v += kNProd) {
+        const int64_t gi = base + v;
+        const bool okk = gi >= 0 && gi < p.N;
+        cp_async_zfill<sizeof(XT)>(dst + v, okk ? (const void *)(row + gi) : (const void *)row, okk);
+      }
+    };
+    int64_t it = blockIdx.x;
+    if (it < p.niters) fetch(it, 0);
+    cp_async_commit();
+    if (it + gridDim.x < p.niters) fetch(it + gridDim.x, 1);
+    cp_async_commit();
+    for (int k = 0; it < p.niters; it += gridDim.x, ++k) {
+      const int slot = k & 1;
+      cp_async_wait<1>();
+      // one thread waits for the slot; the named barrier publishes its verdict (and every
+      // producer's landed copies) to all producers, so the role leaves the loop together
+      if (ptid == 0) s_pok = (k < 2) ? 1 : (tc::mbar_wait(&op_empty[slot], ((k - 2) >> 1) & 1) ? 1 : 0);
+      named_sync(1, kNProd);
+      if (!s_pok) {
+        s_fail = 1;
+        break;
+      }
+      // convert raw slot -> operand slot: two consecutive samples of one component per item
+      const XT *src = rawp(slot);
+      const int half = p.LA / 2;
+      for (int e = ptid; e < p.P * half; e += kNProd) {
+        const int pp = e / half, u = 2 * (e - pp * half);
+        XT v0, v1;
+        if (p.P == 1) {
+          if constexpr (XC) {
+            const float4 v = *reinterpret_cast<const float4 *>(src + u);
+            v0 = make_float2(v.x, v.y);
+            v1 = make_float2(v.z, v.w);
+          } else {
+            const float2 v = *reinterpret_cast<const float2 *>(src + u);
+            v0 = v.x;
+            v1 = v.y;
+          }
+        } else {
+          v0 = src[(size_t)u * p.P + pp];
+          v1 = src[(size_t)(u + 1) * p.P + pp];
+        }
+#pragma unroll
         for (int part = 0; part < NPARTS; part++) {
-          const uint32_t d = dset + (uint32_t)((m * NPARTS + part) * p.Nmma);
-          uint32_t acc = 0;
-          for (int pi = 0; pi < npairs; pi++) {
-            const int ta = p.terms == 3 ? pa3[pi] : 0, tb = p.terms == 3 ? pb3[pi] : 0;
-            for (int pp = 0; pp < p.P; pp++) {
-              uint64_t ad = tc::smem_desc(tc::smem_u32(xarrp(buf, part, ta, pp)) + (uint32_t)(8 * 128 * m) * 2u, 16u,
-                                          128u);
-              uint64_t bd = tc::smem_desc(tc::smem_u32(warr(pp, tb)), 128u, wsbo);
-              for (int ks = 0; ks < nks; ks++) {
-                tc::mma_f16(d, ad, bd, idesc, acc);
-                acc = 1;
-                ad += 2;   // +32 B
-                bd += 16;  // +256 B
-              }
+          const float f0 = part == 0 ? re_of(v0) : im_of(v0);
+          const float f1 = part == 0 ? re_of(v1) : im_of(v1);
+          if (p.fp16) {
+            *reinterpret_cast<__half2 *>(reinterpret_cast<__half *>(xarrp(slot, part, 0, pp)) + u) =
+                __floats2half2_rn(f0, f1);
+          } else {
+            __nv_bfloat16 a0, a1, a2, b0, b1, b2;
+            tc::split3_bf16(f0, a0, a1, a2);
+            tc::split3_bf16(f1, b0, b1, b2);
+            *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<__nv_bfloat16 *>(xarrp(slot, part, 0, pp)) + u) =
+                __halves2bfloat162(a0, b0);
+            if (p.terms == 3) {
+              *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<__nv_bfloat16 *>(xarrp(slot, part, 1, pp)) + u) =
+                  __halves2bfloat162(a1, b1);
+              *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<__nv_bfloat16 *>(xarrp(slot, part, 2, pp)) + u) =
+                  __halves2bfloat162(a2, b2);
             }
           }
         }
       }
-      tc::mma_commit(&bars[ts]);
-    }
-    // stage iteration k+2 into the raw slot iteration k used, then convert iteration k+1
-    // (staged one iteration ago) into the other operand buffer while the MMAs run
-    const int64_t nxt = it + gridDim.x;
-    const int64_t nxt2 = nxt + gridDim.x;
-    if (dbuf) {
-      if (nxt2 < p.niters) fetch(nxt2, k & 1);
+      tc::fence_async_smem();
+      named_sync(1, kNProd);
+      if (ptid == 0) mbar_arrive(&op_full[slot]);
+      // the raw slot is consumed: stage iteration k + 2 into it
+      const int64_t it2 = it + 2 * (int64_t)gridDim.x;
+      if (it2 < p.niters) fetch(it2, slot);
       cp_async_commit();
-      cp_async_wait<1>();
-      __syncthreads();
-      if (nxt < p.niters) convert((k + 1) & 1, buf ^ 1);
     }
-    tc::fence_async_smem();
-    const bool got = tc::mbar_wait(&bars[ts], phase[ts]);
-    phase[ts] ^= 1u;
-    if (!got) {
-      ok = false;
-      if (tid == 0) atomicExch(&g_tc_status, 1);
+    cp_async_wait<0>();
+  } else if (warp == 0) {
+    // ================= MMA issuer =================
+    if (lane == 0) {
+      const uint32_t idesc3 = tc::idesc_f16(128, (uint32_t)(3 * p.Nmma), 1u);
+      const uint32_t idesc2 = tc::idesc_f16(128, (uint32_t)(2 * p.Nmma), 1u);
+      const uint32_t idesc1 = tc::idesc_f16(128, (uint32_t)p.Nmma, p.fp16 ? 0u : 1u);
+      const uint32_t wsbo = (uint32_t)(p.Kp / 8) * 128u;
+      const int nks = p.Kp / 16;
+      int64_t it = blockIdx.x;
+      for (int k = 0; it < p.niters; it += gridDim.x, ++k) {
+        const int slot = k & 1;
+        if (!tc::mbar_wait(&op_full[slot], (k >> 1) & 1)) { s_fail = 1; break; }
+        if (k >= 2 && !tc::mbar_wait(&tm_empty[slot], ((k - 2) >> 1) & 1)) { s_fail = 1; break; }
+        tc::tc_fence_after();
+        const uint32_t dset = tmem + (uint32_t)slot * set_cols;
+        for (int m = 0; m < p.MT; m++) {
+          for (int part = 0; part < NPARTS; part++) {
+            const uint32_t d = dset + (uint32_t)((m * NPARTS + part) * wrows);
+            for (int pp = 0; pp < p.P; pp++) {
+              const uint32_t a_off = (uint32_t)(8 * 128 * m) * 2u;
+              uint64_t bd = tc::smem_desc(tc::smem_u32(warr(pp)), 128u, wsbo);
+              if (p.terms == 3) {
+                uint64_t a0 = tc::smem_desc(tc::smem_u32(xarrp(slot, part, 0, pp)) + a_off, 16u, 128u);
+                uint64_t a1 = tc::smem_desc(tc::smem_u32(xarrp(slot, part, 1, pp)) + a_off, 16u, 128u);
+                uint64_t a2 = tc::smem_desc(tc::smem_u32(xarrp(slot, part, 2, pp)) + a_off, 16u, 128u);
+                for (int ks = 0; ks < nks; ks++) {
+                  // D[0:3N) (+)= a0 * [b0|b1|b2];  D[N:3N) += a1 * [b0|b1];  D[2N:3N) += a2 * b0
+                  tc::mma_f16(d, a0, bd, idesc3, (pp > 0 || ks > 0) ? 1u : 0u);
+                  tc::mma_f16(d + (uint32_t)p.Nmma, a1, bd, idesc2, 1u);
+                  tc::mma_f16(d + (uint32_t)(2 * p.Nmma), a2, bd, idesc1, 1u);
+                  a0 += 2;
+                  a1 += 2;
+                  a2 += 2;
+                  bd += 16;
+                }
+              } else {
+                uint64_t a0 = tc::smem_desc(tc::smem_u32(xarrp(slot, part, 0, pp)) + a_off, 16u, 128u);
+                for (int ks = 0; ks < nks; ks++) {
+                  tc::mma_f16(d, a0, bd, idesc1, (pp > 0 || ks > 0) ? 1u : 0u);
+                  a0 += 2;
+                  bd += 16;
+                }
+              }
+            }
+          }
+        }
+        tc::mma_commit(&op_empty[slot]);
+        tc::mma_commit(&tm_full[slot]);
+      }
     }
-    tc::tc_fence_after();
-    // ---- epilogue: warp quarter w%4 owns TMEM lanes 32*(w%4) .. +32 (rows); warps 0-3 take
-    // even M-tiles, 4-7 odd ones ----
-    if (got) {
+  } else {
+    // ================= epilogue (warps 8-11: TMEM lane quarters 0-3) =================
+    const int quarter = warp - kEpiWarp0;
+    const uint32_t lane_base = (uint32_t)(32 * quarter) << 16;
+    int64_t it = blockIdx.x;
+    for (int k = 0; it < p.niters; it += gridDim.x, ++k) {
+      const int slot = k & 1;
+      if (quarter == 0 && lane == 0) s_eok = tc::mbar_wait(&tm_full[slot], (k >> 1) & 1) ? 1 : 0;
+      named_sync(2, 128);
+      if (!s_eok) {
+        s_fail = 1;
+        break;
+      }
+      tc::tc_fence_after();
+      const uint32_t dset = tmem + (uint32_t)slot * set_cols;
       const int64_t b = it / p.iters_per_row;
       const int64_t q0 = (it - b * p.iters_per_row) * (int64_t)(128 * p.MT);
       XT *orow = reinterpret_cast<XT *>(p.out) + b * p.out_bstride;
-      for (int m = warp >> 2; m < p.MT; m += 2) {
-        const int64_t q = q0 + 128 * m + 32 * (warp & 3) + lane;
+      for (int m = 0; m < p.MT; m++) {
+        const int64_t q = q0 + 128 * m + 32 * quarter + lane;
         for (int col = 0; col < p.Nmma; col += 16) {
-          uint32_t rr[16], ri[16];
-          const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
-          tc::tmem_ld16(dset + lane_base + (uint32_t)((m * NPARTS) * p.Nmma + col), rr);
-          if constexpr (XC) tc::tmem_ld16(dset + lane_base + (uint32_t)((m * NPARTS + 1) * p.Nmma + col), ri);
-          tc::tmem_ld_wait();
+          float acc[NPARTS][16];
+#pragma unroll
+          for (int part = 0; part < NPARTS; part++) {
+            const uint32_t base = dset + lane_base + (uint32_t)((m * NPARTS + part) * wrows + col);
+            uint32_t r[16];
+            tc::tmem_ld16(base, r);
+            tc::tmem_ld_wait();
+#pragma unroll
+            for (int i = 0; i < 16; i++) acc[part][i] = __uint_as_float(r[i]);
+            for (int t = 1; t < p.terms; t++) {
+              tc::tmem_ld16(base + (uint32_t)(t * p.Nmma), r);
+              tc::tmem_ld_wait();
+#pragma unroll
+              for (int i = 0; i < 16; i++) acc[part][i] += __uint_as_float(r[i]);
+            }
+          }
 #pragma unroll
           for (int i = 0; i < 16; i++) {
             const int j = col + i;
             const int64_t n = q * p.Nt + j;
             if (j < p.Nt && n < p.out_len) {
-              if constexpr (XC) {
-                float2 v;
-                v.x = __uint_as_float(rr[i]);
-                v.y = __uint_as_float(ri[i]);
-                orow[n] = v;
-              } else {
-                orow[n] = __uint_as_float(rr[i]);
-              }
+              if constexpr (XC) orow[n] = make_float2(acc[0][i], acc[1][i]);
+              else orow[n] = acc[0][i];
             }
           }
         }
       }
-    }
-    tc::tc_fence_before();
-    __syncthreads();
-    tc::tc_fence_after();
-    if (!ok) break;
-    if (!dbuf && nxt < p.niters) {
-      fetch(nxt, 0);
-      cp_async_commit();
-      cp_async_wait<0>();
-      __syncthreads();
-      convert(0, 0);
-      tc::fence_async_smem();
       tc::tc_fence_before();
-      __syncthreads();
-      tc::tc_fence_after();
+      named_sync(2, 128);
+      if (quarter == 0 && lane == 0) mbar_arrive(&tm_empty[slot]);
     }
   }
-  cp_async_wait<0>();
-  // drain: a timed-out wait above leaves MMAs possibly in flight; wait once more (bounded)
-  if (!ok && tid == 0) {
-    (void)tc::mbar_wait(&bars[0], phase[0]);
-    (void)tc::mbar_wait(&bars[1], phase[1]);
+  __syncthreads();
+  if (s_fail && tid == 0) {
+    atomicExch(&g_tc_status, 1);
+    // give MMAs still in flight a bounded chance to finish before the TMEM is freed
+    (void)tc::mbar_wait(&tm_full[0], 0);
+    (void)tc::mbar_wait(&tm_full[1], 0);
   }
   tc::tc_fence_before();
   __syncthreads();
@@ -353,31 +402,35 @@ static TcPlan plan_tc(int64_t up, int64_t down, int64_t L, int64_t N_in, int64_t
     return pl;
   }
   const int nparts = xc ? 2 : 1;
-  auto smem_for = [&](int MT, int nbuf) -> size_t {
-    const size_t w = (size_t)p.P * p.terms * p.Nmma * p.Kp * 2;
+  if (p.terms == 3 && 3 * p.Nmma > 256) {
+    snprintf(pl.why, sizeof(pl.why), "bf16x3 needs 3*%d MMA columns (> 256)", p.Nmma);
+    return pl;
+  }
+  const int wrows = p.terms * p.Nmma;
+  auto smem_for = [&](int MT) -> size_t {
+    const size_t w = (size_t)p.P * wrows * p.Kp * 2;
     const size_t la = (size_t)8 * 128 * MT + p.Kp;
     const size_t xa = (la * 2 + 127) / 128 * 128;
-    const size_t raw = (size_t)nbuf * p.P * la * (xc ? 8 : 4);
-    return (w + 127) / 128 * 128 + (size_t)nbuf * nparts * p.terms * p.P * xa + raw;
+    const size_t raw = 2 * (size_t)p.P * la * (xc ? 8 : 4);
+    return (w + 127) / 128 * 128 + (size_t)2 * nparts * p.terms * p.P * xa + raw;
   };
-  // prefer two CTAs per SM (<= 110 KB each), then one CTA with double buffering, then single
-  int MT = 4, nbuf = 2;
-  while (MT > 1 && (smem_for(MT, nbuf) > 110 * 1024 || 2 * MT * nparts * p.Nmma > 256)) MT /= 2;
-  if (smem_for(MT, nbuf) > 200 * 1024) nbuf = 1;
-  if (2 * MT * nparts * p.Nmma > 512 || smem_for(MT, nbuf) > 200 * 1024) {
-    snprintf(pl.why, sizeof(pl.why), "tile needs %zu B of shared memory", smem_for(MT, nbuf));
+  // MT M-tiles of 128 rows per pipeline stage: two TMEM accumulator sets must fit in 512 columns
+  int MT = 4;
+  while (MT > 1 && (smem_for(MT) > 200 * 1024 || 2 * MT * nparts * wrows > 512)) MT /= 2;
+  if (2 * MT * nparts * wrows > 512 || smem_for(MT) > 200 * 1024) {
+    snprintf(pl.why, sizeof(pl.why), "tile needs %zu B of shared memory", smem_for(MT));
     return pl;
   }
   p.MT = MT;
-  p.nbuf = nbuf;
+  p.nbuf = 2;
   p.LA = 8 * 128 * MT + p.Kp;
   uint32_t cols = 32;
-  while (cols < (uint32_t)(2 * MT * nparts * p.Nmma)) cols <<= 1;
+  while (cols < (uint32_t)(2 * MT * nparts * wrows)) cols <<= 1;
   p.tmem_cols = (int32_t)cols;
   p.rows = (out_len + p.Nt - 1) / p.Nt;
   p.iters_per_row = (p.rows + 128 * MT - 1) / (128 * MT);
   p.niters = p.iters_per_row * batch;
-  pl.smem = smem_for(MT, nbuf);
+  pl.smem = smem_for(MT);
   pl.ok = true;
   return pl;
 }
@@ -402,15 +455,13 @@ int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf 
   int rc = ensure_smem(fn, pl.smem, "resample_poly (tensor cores)");
   if (rc) return rc;
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kTcThreads, pl.smem);
-  if (pl.smem <= 110 * 1024) occ = std::max(occ, 2);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kWsThreads, pl.smem);
   if (occ < 1) occ = 1;
-  // each CTA holds tmem_cols of the SM's 512 TMEM columns
-  occ = std::min(occ, 512 / p.tmem_cols);
+  occ = std::min(occ, 512 / p.tmem_cols);  // each CTA holds tmem_cols of the SM's 512 TMEM columns
   int64_t grid = (int64_t)num_sms() * occ;
   if (grid > p.niters) grid = p.niters;
   void *args[] = {&p};
-  cudaError_t e = cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kTcThreads), args, pl.smem, s);
+  cudaError_t e = cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kWsThreads), args, pl.smem, s);
   if (e != cudaSuccess) GBFIR_FAIL(GBFIR_ERR_CUDA, "resample_poly (tensor cores): %s", cudaGetErrorString(e));
   count_launch();
   return GBFIR_SUCCESS;
