@@ -56,7 +56,8 @@ struct TcParams {
   int64_t iters_per_row, niters;
   double scale;     // up
   int32_t tmem_cols;
-  int32_t nbuf;     // 2: convert the next iteration during the MMAs; 1: after them
+  int32_t nbuf;     // operand ring slots (2)
+  int32_t nraw;     // raw staging slots: 2 = stage two iterations ahead, 1 = one ahead
 };
 
 // Bounded-wait status of the tensor-core kernels (1 = a wait gave up); read and
@@ -166,14 +167,19 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
         cp_async_zfill<sizeof(XT)>(dst + v, okk ? (const void *)(row + gi) : (const void *)row, okk);
       }
     };
+    const int nraw = p.nraw;
     int64_t it = blockIdx.x;
     if (it < p.niters) fetch(it, 0);
     cp_async_commit();
-    if (it + gridDim.x < p.niters) fetch(it + gridDim.x, 1);
+    if (nraw == 2 && it + gridDim.x < p.niters) fetch(it + gridDim.x, 1);
     cp_async_commit();
     for (int k = 0; it < p.niters; it += gridDim.x, ++k) {
       const int slot = k & 1;
-      cp_async_wait<1>();
+      const int rslot = nraw == 2 ? slot : 0;
+      // with two raw slots this iteration's group is the older of two outstanding ones;
+      // with one slot it is the most recent group
+      if (nraw == 2) cp_async_wait<1>();
+      else cp_async_wait<0>();
       // one thread waits for the slot; the named barrier publishes its verdict (and every
       // producer's landed copies) to all producers, so the role leaves the loop together
       if (ptid == 0) s_pok = (k < 2) ? 1 : (tc::mbar_wait(&op_empty[slot], ((k - 2) >> 1) & 1) ? 1 : 0);
@@ -183,7 +189,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
         break;
       }
       // convert raw slot -> operand slot: two consecutive samples of one component per item
-      const XT *src = rawp(slot);
+      const XT *src = rawp(rslot);
       const int half = p.LA / 2;
       for (int e = ptid; e < p.P * half; e += kNProd) {
         const int pp = e / half, u = 2 * (e - pp * half);
@@ -227,9 +233,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
       tc::fence_async_smem();
       named_sync(1, kNProd);
       if (ptid == 0) mbar_arrive(&op_full[slot]);
-      // the raw slot is consumed: stage iteration k + 2 into it
-      const int64_t it2 = it + 2 * (int64_t)gridDim.x;
-      if (it2 < p.niters) fetch(it2, slot);
+      // the raw slot is consumed: stage iteration k + nraw into it
+      const int64_t it2 = it + (int64_t)nraw * gridDim.x;
+      if (it2 < p.niters) fetch(it2, rslot);
       cp_async_commit();
     }
     cp_async_wait<0>();
@@ -407,22 +413,25 @@ static TcPlan plan_tc(int64_t up, int64_t down, int64_t L, int64_t N_in, int64_t
     return pl;
   }
   const int wrows = p.terms * p.Nmma;
-  auto smem_for = [&](int MT) -> size_t {
+  auto smem_for = [&](int MT, int nraw) -> size_t {
     const size_t w = (size_t)p.P * wrows * p.Kp * 2;
     const size_t la = (size_t)8 * 128 * MT + p.Kp;
     const size_t xa = (la * 2 + 127) / 128 * 128;
-    const size_t raw = 2 * (size_t)p.P * la * (xc ? 8 : 4);
+    const size_t raw = (size_t)nraw * p.P * la * (xc ? 8 : 4);
     return (w + 127) / 128 * 128 + (size_t)2 * nparts * p.terms * p.P * xa + raw;
   };
   // MT M-tiles of 128 rows per pipeline stage: two TMEM accumulator sets must fit in 512 columns
-  int MT = 4;
-  while (MT > 1 && (smem_for(MT) > 200 * 1024 || 2 * MT * nparts * wrows > 512)) MT /= 2;
-  if (2 * MT * nparts * wrows > 512 || smem_for(MT) > 200 * 1024) {
-    snprintf(pl.why, sizeof(pl.why), "tile needs %zu B of shared memory", smem_for(MT));
+  const size_t kMaxSmem = 225 * 1024;
+  int MT = 4, nraw = 2;
+  while (MT > 1 && (smem_for(MT, nraw) > kMaxSmem || 2 * MT * nparts * wrows > 512)) MT /= 2;
+  if (smem_for(MT, nraw) > kMaxSmem) nraw = 1;
+  if (2 * MT * nparts * wrows > 512 || smem_for(MT, nraw) > kMaxSmem) {
+    snprintf(pl.why, sizeof(pl.why), "tile needs %zu B of shared memory", smem_for(MT, nraw));
     return pl;
   }
   p.MT = MT;
   p.nbuf = 2;
+  p.nraw = nraw;
   p.LA = 8 * 128 * MT + p.Kp;
   uint32_t cols = 32;
   while (cols < (uint32_t)(2 * MT * nparts * wrows)) cols <<= 1;
@@ -430,7 +439,7 @@ static TcPlan plan_tc(int64_t up, int64_t down, int64_t L, int64_t N_in, int64_t
   p.rows = (out_len + p.Nt - 1) / p.Nt;
   p.iters_per_row = (p.rows + 128 * MT - 1) / (128 * MT);
   p.niters = p.iters_per_row * batch;
-  pl.smem = smem_for(MT);
+  pl.smem = smem_for(MT, nraw);
   pl.ok = true;
   return pl;
 }
