@@ -139,13 +139,15 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_from_profile():
-    """Per-launch DRAM bytes of the (3,2) resample launch from the committed ncu summary."""
+def traffic_from_profile(up, down):
+    """Per-launch DRAM bytes (read + write) of the FP32 (up, down) launch, taken from the
+    committed one-pass ncu capture of the full-size workload."""
     p = os.path.join(ROOT, "profiles", "resample_rowtile_c64_64x2p20.md")
     if not os.path.exists(p):
         return None
+    key = f"traffic_bytes_per_launch_{up}_{down}:"
     for line in open(p):
-        if line.startswith("traffic_bytes_per_launch_3_2:"):
+        if line.startswith(key):
             try:
                 return float(line.split(":", 1)[1].strip())
             except ValueError:
@@ -398,7 +400,7 @@ def main():
     u, d = RATIOS[dom]
     bytes_dom = alg_bytes(NSAMP, len(taps_np[dom]), u, d, BATCH)
     achieved = bytes_dom / (per_ms[dom] * 1e-3) / 1e9
-    traffic = traffic_from_profile()
+    traffic = traffic_from_profile(u, d) if (prec == "fp32" and BATCH == 64) else None
     per_ratio = {}
     for i, (u2, d2) in enumerate(RATIOS):
         b2 = alg_bytes(NSAMP, len(taps_np[i]), u2, d2, BATCH)

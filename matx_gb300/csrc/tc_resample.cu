@@ -56,7 +56,8 @@ struct TcParams {
   int64_t iters_per_row, niters;
   double scale;     // up
   int32_t tmem_cols;
-  int32_t nbuf;     // operand ring slots (2)
+  int32_t nbuf;     // operand ring slots (1 or 2)
+  int32_t nsets;    // TMEM accumulator sets (1 or 2)
   int32_t nraw;     // raw staging slots: 2 = stage two iterations ahead, 1 = one ahead
 };
 
@@ -97,7 +98,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
   __shared__ int s_fail, s_pok, s_eok;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-  // shared layout: W_cat [P][terms*Nmma rows][Kp] ; operand ring [2][NPARTS][terms][P][LA] ; raw ring [2][P*LA]
+  // shared layout: W_cat [P][terms*Nmma rows][Kp] ; operand ring [nbuf][NPARTS][terms][P][LA] ;
+  // raw ring [nraw][P*LA]
   const int wrows = p.terms * p.Nmma;
   const uint32_t wbytes = (uint32_t)wrows * p.Kp * 2u;
   unsigned char *wbase = smem;
@@ -108,7 +110,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
     return xbase + ((((size_t)slot * NPARTS + part) * p.terms + t) * p.P + pp) * xarr;
   };
   const size_t raw_elems = (size_t)p.P * p.LA;
-  XT *raw0 = reinterpret_cast<XT *>(xbase + (size_t)2 * NPARTS * p.terms * p.P * xarr);
+  XT *raw0 = reinterpret_cast<XT *>(xbase + (size_t)p.nbuf * NPARTS * p.terms * p.P * xarr);
   auto rawp = [&](int slot) { return raw0 + (size_t)slot * raw_elems; };
 
   if (warp == 0) tc::tmem_alloc(&tmem_slot, (uint32_t)p.tmem_cols);
@@ -151,6 +153,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
   const uint32_t tmem = tmem_slot;
   const uint32_t set_cols = (uint32_t)(p.MT * NPARTS * wrows);
   const XT *xp = reinterpret_cast<const XT *>(p.x);
+  (void)xp;
 
   if (warp >= kProdWarp0 && warp < kProdWarp0 + kProdWarps) {
     // ================= producers =================
@@ -173,16 +176,18 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
     cp_async_commit();
     if (nraw == 2 && it + gridDim.x < p.niters) fetch(it + gridDim.x, 1);
     cp_async_commit();
+    const int nslots = p.nbuf;
     for (int k = 0; it < p.niters; it += gridDim.x, ++k) {
-      const int slot = k & 1;
-      const int rslot = nraw == 2 ? slot : 0;
+      const int slot = k % nslots;
+      const int rslot = nraw == 2 ? (k & 1) : 0;
       // with two raw slots this iteration's group is the older of two outstanding ones;
       // with one slot it is the most recent group
       if (nraw == 2) cp_async_wait<1>();
       else cp_async_wait<0>();
       // one thread waits for the slot; the named barrier publishes its verdict (and every
       // producer's landed copies) to all producers, so the role leaves the loop together
-      if (ptid == 0) s_pok = (k < 2) ? 1 : (tc::mbar_wait(&op_empty[slot], ((k - 2) >> 1) & 1) ? 1 : 0);
+      if (ptid == 0)
+        s_pok = (k < nslots) ? 1 : (tc::mbar_wait(&op_empty[slot], ((k - nslots) / nslots) & 1) ? 1 : 0);
       named_sync(1, kNProd);
       if (!s_pok) {
         s_fail = 1;
@@ -249,11 +254,11 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
       const int nks = p.Kp / 16;
       int64_t it = blockIdx.x;
       for (int k = 0; it < p.niters; it += gridDim.x, ++k) {
-        const int slot = k & 1;
-        if (!tc::mbar_wait(&op_full[slot], (k >> 1) & 1)) { s_fail = 1; break; }
-        if (k >= 2 && !tc::mbar_wait(&tm_empty[slot], ((k - 2) >> 1) & 1)) { s_fail = 1; break; }
+        const int slot = k % p.nbuf, tset = k % p.nsets;
+        if (!tc::mbar_wait(&op_full[slot], (k / p.nbuf) & 1)) { s_fail = 1; break; }
+        if (k >= p.nsets && !tc::mbar_wait(&tm_empty[tset], ((k - p.nsets) / p.nsets) & 1)) { s_fail = 1; break; }
         tc::tc_fence_after();
-        const uint32_t dset = tmem + (uint32_t)slot * set_cols;
+        const uint32_t dset = tmem + (uint32_t)tset * set_cols;
         for (int m = 0; m < p.MT; m++) {
           for (int part = 0; part < NPARTS; part++) {
             const uint32_t d = dset + (uint32_t)((m * NPARTS + part) * wrows);
@@ -286,7 +291,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
           }
         }
         tc::mma_commit(&op_empty[slot]);
-        tc::mma_commit(&tm_full[slot]);
+        tc::mma_commit(&tm_full[tset]);
       }
     }
   } else {
@@ -295,8 +300,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
     const uint32_t lane_base = (uint32_t)(32 * quarter) << 16;
     int64_t it = blockIdx.x;
     for (int k = 0; it < p.niters; it += gridDim.x, ++k) {
-      const int slot = k & 1;
-      if (quarter == 0 && lane == 0) s_eok = tc::mbar_wait(&tm_full[slot], (k >> 1) & 1) ? 1 : 0;
+      const int slot = k % p.nsets;
+      if (quarter == 0 && lane == 0) s_eok = tc::mbar_wait(&tm_full[slot], (k / p.nsets) & 1) ? 1 : 0;
       named_sync(2, 128);
       if (!s_eok) {
         s_fail = 1;
@@ -346,8 +351,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
   if (s_fail && tid == 0) {
     atomicExch(&g_tc_status, 1);
     // give MMAs still in flight a bounded chance to finish before the TMEM is freed
-    (void)tc::mbar_wait(&tm_full[0], 0);
-    (void)tc::mbar_wait(&tm_full[1], 0);
+    for (int i = 0; i < p.nsets; i++) (void)tc::mbar_wait(&tm_full[i], 0);
   }
   tc::tc_fence_before();
   __syncthreads();
@@ -413,33 +417,39 @@ static TcPlan plan_tc(int64_t up, int64_t down, int64_t L, int64_t N_in, int64_t
     return pl;
   }
   const int wrows = p.terms * p.Nmma;
-  auto smem_for = [&](int MT, int nraw) -> size_t {
+  auto smem_for = [&](int MT, int nraw, int nslots) -> size_t {
     const size_t w = (size_t)p.P * wrows * p.Kp * 2;
     const size_t la = (size_t)8 * 128 * MT + p.Kp;
     const size_t xa = (la * 2 + 127) / 128 * 128;
     const size_t raw = (size_t)nraw * p.P * la * (xc ? 8 : 4);
-    return (w + 127) / 128 * 128 + (size_t)2 * nparts * p.terms * p.P * xa + raw;
+    return (w + 127) / 128 * 128 + (size_t)nslots * nparts * p.terms * p.P * xa + raw;
   };
-  // MT M-tiles of 128 rows per pipeline stage: two TMEM accumulator sets must fit in 512 columns
+  // A stage holds MT M-tiles of 128 rows.  Shrink, in this order, until it fits: MT, the raw
+  // staging depth, the number of TMEM accumulator sets (512 columns), the operand ring depth.
   const size_t kMaxSmem = 225 * 1024;
-  int MT = 4, nraw = 2;
-  while (MT > 1 && (smem_for(MT, nraw) > kMaxSmem || 2 * MT * nparts * wrows > 512)) MT /= 2;
-  if (smem_for(MT, nraw) > kMaxSmem) nraw = 1;
-  if (2 * MT * nparts * wrows > 512 || smem_for(MT, nraw) > kMaxSmem) {
-    snprintf(pl.why, sizeof(pl.why), "tile needs %zu B of shared memory", smem_for(MT, nraw));
+  int MT = 4, nraw = 2, nsets = 2, nslots = 2;
+  auto smem_ok = [&]() { return smem_for(MT, nraw, nslots) <= kMaxSmem; };
+  auto tmem_ok = [&]() { return nsets * MT * nparts * wrows <= 512; };
+  while (MT > 1 && !(smem_ok() && tmem_ok())) MT /= 2;
+  if (!smem_ok()) nraw = 1;
+  if (!tmem_ok()) nsets = 1;
+  if (!smem_ok()) nslots = 1;
+  if (!smem_ok() || !tmem_ok()) {
+    snprintf(pl.why, sizeof(pl.why), "tile needs %zu B of shared memory", smem_for(MT, nraw, nslots));
     return pl;
   }
   p.MT = MT;
-  p.nbuf = 2;
+  p.nbuf = nslots;
   p.nraw = nraw;
+  p.nsets = nsets;
   p.LA = 8 * 128 * MT + p.Kp;
   uint32_t cols = 32;
-  while (cols < (uint32_t)(2 * MT * nparts * wrows)) cols <<= 1;
+  while (cols < (uint32_t)(nsets * MT * nparts * wrows)) cols <<= 1;
   p.tmem_cols = (int32_t)cols;
   p.rows = (out_len + p.Nt - 1) / p.Nt;
   p.iters_per_row = (p.rows + 128 * MT - 1) / (128 * MT);
   p.niters = p.iters_per_row * batch;
-  pl.smem = smem_for(MT, nraw);
+  pl.smem = smem_for(MT, nraw, nslots);
   pl.ok = true;
   return pl;
 }
