@@ -309,6 +309,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     ap.add_argument("--batch", type=int, default=BATCH, help="rows per GPU (profiling cases)")
     ap.add_argument("--no-tune", action="store_true", help="use the built-in tile heuristic")
+    ap.add_argument("--tiles", default="",
+                    help="fixed row tiles instead of tuning, e.g. '3/2=4,2,4,2;4/5=2,1,1,2' "
+                         "(rows_per_thread, col_warps, group, buffers; profiling cases)")
     ap.add_argument("--ratios", default="3/2,4/5,160/147", help="comma-separated up/down list (profiling cases)")
     ap.add_argument("--workload", default="resample", choices=["resample", "ragged"],
                     help="ragged: 4096 uneven signals in one persistent launch (separate JSON line)")
@@ -355,7 +358,16 @@ def main():
 
     # ---- tile autotuning (before the timed region) ----------------------------------------
     tiles = {}
-    if not args.no_tune and prec == "fp32":
+    if args.tiles:
+        from matx_gb300 import autotune
+        for item in args.tiles.split(";"):
+            r, t = item.split("=")
+            u, d = (int(v) for v in r.split("/"))
+            tile = tuple(int(v) for v in t.split(","))
+            autotune.register(u, d, len(taps_np[RATIOS.index((u, d))]), tile)
+            tiles[r] = {"rows_per_thread": tile[0], "col_warps": tile[1], "group": tile[2], "buffers": tile[3],
+                        "fixed": True}
+    elif not args.no_tune and prec == "fp32":
         from matx_gb300 import autotune
         for (u, d), h, o in zip(RATIOS, taps, outs):
             r = autotune.tune_resample(x, h, u, d, out=o, use_cache=False)

@@ -92,7 +92,7 @@ struct RgParams {
 __global__ void __launch_bounds__(kRgThreads) ragged_rowtile(const RgParams rp) {
   using XT = float2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  TapVec<float, false> *table = reinterpret_cast<TapVec<float, false> *>(smem_raw);
+  unsigned char *table = smem_raw;
   XT *xbuf = reinterpret_cast<XT *>(smem_raw + rp.table_bytes);
   __shared__ long long s_tile;
   __shared__ RsParams s_p;
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kRgThreads) ragged_rowtile(const RgParams rp) 
       continue;
     }
     if (sig != last_sig) {
-      build_tap_table<float, false>(p, reinterpret_cast<const float *>(p.h), table, tid, kRgThreads);
+      build_tap_table<float, true, false>(p, reinterpret_cast<const float *>(p.h), table, tid, kRgThreads);
       last_sig = sig;
     }
     const int64_t xs0 = q0 * p.S + p.kmin;
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(kRgThreads) ragged_rowtile(const RgParams rp) 
 }
 
 static int64_t table_bytes_of(const RgGeom &g) {
-  return g.identity ? 0 : (((int64_t)g.ncg * g.span * 16 + 15) & ~15LL);
+  return g.identity ? 0 : (int64_t)tap_table_bytes<float, true, false>(g.ncg, g.span);
 }
 
 }  // namespace gbfir

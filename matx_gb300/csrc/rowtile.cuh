@@ -56,6 +56,27 @@ template <typename T>
 struct TapVec<T, true> {
   typename cplx_of<T>::type v[4];
 };
+// Complex signal, real float taps: each tap stored twice, (t0,t0,t1,t1),(t2,t2,t3,t3), so a
+// 16-byte shared load yields the (t,t) operand pairs of two packed f32x2 FMAs.
+struct TapDup {
+  float4 v[2];
+};
+
+template <typename T, bool XC, bool HC>
+struct TapEntry {
+  using type = TapVec<T, HC>;
+};
+template <>
+struct TapEntry<float, true, false> {
+  using type = TapDup;
+};
+
+// Shared bytes of the tap table: ncg*span entries, then one int32 band offset per group.
+template <typename T, bool XC, bool HC>
+__host__ __device__ inline size_t tap_table_bytes(int64_t ncg, int64_t span) {
+  const size_t taps = ((size_t)ncg * span * sizeof(typename TapEntry<T, XC, HC>::type) + 15) & ~(size_t)15;
+  return taps + (((size_t)ncg * 4 + 15) & ~(size_t)15);
+}
 
 template <bool PAD>
 __device__ __forceinline__ int smem_idx(int p) {
@@ -63,11 +84,15 @@ __device__ __forceinline__ int smem_idx(int p) {
   else return p;
 }
 
-// table[g*span + kk].v[jj] = he[c + (4g+jj)*down - (kl0(g)+kk)*up] (reversed when rev), 0 outside.
-template <typename T, bool HC>
+// table[g*span + kk] holds the 4 taps he[c + (4g+jj)*down - (kl0(g)+kk)*up] (reversed when
+// rev, 0 outside); goff[g] = kl0(g) - kmin is where band g starts in the tile window.
+template <typename T, bool XC, bool HC>
 __device__ __forceinline__ void build_tap_table(const RsParams &p, const typename val_of<T, HC>::type *hp,
-                                                TapVec<T, HC> *table, int tid, int nthreads) {
+                                                unsigned char *table_raw, int tid, int nthreads) {
   using HT = typename val_of<T, HC>::type;
+  using TE = typename TapEntry<T, XC, HC>::type;
+  TE *table = reinterpret_cast<TE *>(table_raw);
+  int *goff = reinterpret_cast<int *>(table_raw + (((size_t)p.ncg * p.span * sizeof(TE) + 15) & ~(size_t)15));
   const int nent = p.ncg * p.span * 4;
   for (int e = tid; e < nent; e += nthreads) {
     const int g = e / (p.span * 4);
@@ -81,7 +106,121 @@ __device__ __forceinline__ void build_tap_table(const RsParams &p, const typenam
       const int64_t te = p.rev ? p.Lo - 1 - tp : tp;  // index into he
       if (!(p.even && te == 0)) v = hp[te - p.even];
     }
-    table[g * p.span + kk].v[jj] = v;
+    if constexpr (std::is_same<TE, TapDup>::value) {
+      float *f = reinterpret_cast<float *>(&table[g * p.span + kk]);
+      f[2 * jj] = v;
+      f[2 * jj + 1] = v;
+    } else {
+      table[g * p.span + kk].v[jj] = v;
+    }
+  }
+  for (int g = tid; g < p.ncg; g += nthreads)
+    goff[g] = (int)(ceil_div(p.c + 4 * (int64_t)g * p.down - p.Lo + 1, p.up) - p.kmin);
+}
+
+__device__ __forceinline__ const int *tap_goff(const RsParams &p, const unsigned char *table_raw, size_t entry) {
+  return reinterpret_cast<const int *>(table_raw + (((size_t)p.ncg * p.span * entry + 15) & ~(size_t)15));
+}
+
+// Packed FP32 pair arithmetic: one f32x2 instruction, each lane an IEEE round-to-nearest
+// fma / mul, so the values equal two scalar fmaf / __fmul_rn calls.
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+
+// Complex float signal x real float taps, the hot case: the same three-range walk as the
+// generic form below with (re, im) accumulated by one f32x2 FMA per sample and phase
+// (each lane is the fma of MatX's madd for a real tap, so results are unchanged), and
+// each row's 8 outputs written as four 16-byte stores when they are whole and aligned.
+template <int RQ, bool PAD>
+__device__ __forceinline__ void rowtile_compute_c2(const RsParams &p, const float2 *cur,
+                                                   const unsigned char *table_raw, float2 *orow, int64_t q0, int wr,
+                                                   int wc, int lane, float scale) {
+  const TapDup *table = reinterpret_cast<const TapDup *>(table_raw);
+  const int *goff = tap_goff(p, table_raw, sizeof(TapDup));
+  const int nsg = (p.ncg + 1) / 2;
+  const int rbase = wr * 32 * RQ + lane;
+  const float2 sc = make_float2(scale, scale);
+  const int Nt = (int)p.Nt;
+  for (int sg = wc; sg < nsg; sg += p.WC) {
+    const int gA = 2 * sg, gB = 2 * sg + 1;
+    const bool hasB = gB < p.ncg;
+    const int oA = goff[gA];
+    const int d = hasB ? goff[gB] - oA : 0;
+    int base[RQ];
+#pragma unroll
+    for (int i = 0; i < RQ; i++) base[i] = (rbase + 32 * i) * (int)p.S + oA;
+    float2 acc[RQ][8];
+#pragma unroll
+    for (int i = 0; i < RQ; i++)
+#pragma unroll
+      for (int jj = 0; jj < 8; jj++) acc[i][jj] = make_float2(0.f, 0.f);
+    const TapDup *tA = table + gA * p.span;
+    const TapDup *tB = table + (hasB ? gB : gA) * p.span;
+    const int e1 = hasB ? min(d, p.span) : p.span;
+#pragma unroll 2
+    for (int kk = 0; kk < e1; kk++) {
+      const float4 a0 = tA[kk].v[0], a1 = tA[kk].v[1];
+#pragma unroll
+      for (int i = 0; i < RQ; i++) {
+        const float2 xv = cur[smem_idx<PAD>(base[i] + kk)];
+        acc[i][0] = fma2(xv, make_float2(a0.x, a0.y), acc[i][0]);
+        acc[i][1] = fma2(xv, make_float2(a0.z, a0.w), acc[i][1]);
+        acc[i][2] = fma2(xv, make_float2(a1.x, a1.y), acc[i][2]);
+        acc[i][3] = fma2(xv, make_float2(a1.z, a1.w), acc[i][3]);
+      }
+    }
+    if (hasB) {
+#pragma unroll 2
+      for (int kk = d; kk < p.span; kk++) {
+        const float4 a0 = tA[kk].v[0], a1 = tA[kk].v[1];
+        const float4 b0 = tB[kk - d].v[0], b1 = tB[kk - d].v[1];
+#pragma unroll
+        for (int i = 0; i < RQ; i++) {
+          const float2 xv = cur[smem_idx<PAD>(base[i] + kk)];
+          acc[i][0] = fma2(xv, make_float2(a0.x, a0.y), acc[i][0]);
+          acc[i][1] = fma2(xv, make_float2(a0.z, a0.w), acc[i][1]);
+          acc[i][2] = fma2(xv, make_float2(a1.x, a1.y), acc[i][2]);
+          acc[i][3] = fma2(xv, make_float2(a1.z, a1.w), acc[i][3]);
+          acc[i][4] = fma2(xv, make_float2(b0.x, b0.y), acc[i][4]);
+          acc[i][5] = fma2(xv, make_float2(b0.z, b0.w), acc[i][5]);
+          acc[i][6] = fma2(xv, make_float2(b1.x, b1.y), acc[i][6]);
+          acc[i][7] = fma2(xv, make_float2(b1.z, b1.w), acc[i][7]);
+        }
+      }
+#pragma unroll 2
+      for (int kk = max(p.span, d); kk < d + p.span; kk++) {
+        const float4 b0 = tB[kk - d].v[0], b1 = tB[kk - d].v[1];
+#pragma unroll
+        for (int i = 0; i < RQ; i++) {
+          const float2 xv = cur[smem_idx<PAD>(base[i] + kk)];
+          acc[i][4] = fma2(xv, make_float2(b0.x, b0.y), acc[i][4]);
+          acc[i][5] = fma2(xv, make_float2(b0.z, b0.w), acc[i][5]);
+          acc[i][6] = fma2(xv, make_float2(b1.x, b1.y), acc[i][6]);
+          acc[i][7] = fma2(xv, make_float2(b1.z, b1.w), acc[i][7]);
+        }
+      }
+    }
+    const int j0 = 8 * sg;
+    const int ncol = min(8, Nt - j0);
+#pragma unroll
+    for (int i = 0; i < RQ; i++) {
+      const int64_t n0 = (q0 + rbase + 32 * i) * p.Nt + j0;
+      const int64_t left = p.out_len - n0;
+      const int nv = left < ncol ? (left > 0 ? (int)left : 0) : ncol;
+      float2 *dst = orow + n0;
+      if (nv == 8 && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0)) {
+        float4 *d4 = reinterpret_cast<float4 *>(dst);
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const float2 lo = mul2(acc[i][2 * u], sc), hi = mul2(acc[i][2 * u + 1], sc);
+          d4[u] = make_float4(lo.x, lo.y, hi.x, hi.y);
+        }
+      } else {
+#pragma unroll
+        for (int jj = 0; jj < 8; jj++)
+          if (jj < nv) dst[jj] = mul2(acc[i][jj], sc);
+      }
+    }
   }
 }
 
@@ -89,75 +228,82 @@ __device__ __forceinline__ void build_tap_table(const RsParams &p, const typenam
 // super-groups for RQ rows per lane and stores them (masked by Nt and out_len).
 template <typename T, bool XC, bool HC, int RQ, bool PAD>
 __device__ __forceinline__ void rowtile_compute(const RsParams &p, const typename val_of<T, XC>::type *cur,
-                                                const TapVec<T, HC> *table, typename val_of<T, XC || HC>::type *orow,
-                                                int64_t q0, int wr, int wc, int lane, T scale) {
-  using XT = typename val_of<T, XC>::type;
-  constexpr bool OC = XC || HC;
-  const int nsg = (p.ncg + 1) / 2;
-  const int rbase = wr * 32 * RQ + lane;  // local row of slice i is rbase + 32*i
-  for (int sg = wc; sg < nsg; sg += p.WC) {
-    const int gA = 2 * sg, gB = 2 * sg + 1;
-    const bool hasB = gB < p.ncg;
-    const int oA = (int)(ceil_div(p.c + 4 * (int64_t)gA * p.down - p.Lo + 1, p.up) - p.kmin);
-    const int oB = hasB ? (int)(ceil_div(p.c + 4 * (int64_t)gB * p.down - p.Lo + 1, p.up) - p.kmin) : oA;
-    const int d = oB - oA;  // band B starts d samples after band A
-    int base[RQ];
+                                                const unsigned char *table_raw,
+                                                typename val_of<T, XC || HC>::type *orow, int64_t q0, int wr, int wc,
+                                                int lane, T scale) {
+  if constexpr (std::is_same<typename TapEntry<T, XC, HC>::type, TapDup>::value) {
+    rowtile_compute_c2<RQ, PAD>(p, cur, table_raw, orow, q0, wr, wc, lane, scale);
+  } else {
+    using XT = typename val_of<T, XC>::type;
+    constexpr bool OC = XC || HC;
+    const TapVec<T, HC> *table = reinterpret_cast<const TapVec<T, HC> *>(table_raw);
+    const int *goff = tap_goff(p, table_raw, sizeof(TapVec<T, HC>));
+    const int nsg = (p.ncg + 1) / 2;
+    const int rbase = wr * 32 * RQ + lane;  // local row of slice i is rbase + 32*i
+    for (int sg = wc; sg < nsg; sg += p.WC) {
+      const int gA = 2 * sg, gB = 2 * sg + 1;
+      const bool hasB = gB < p.ncg;
+      const int oA = goff[gA];
+      const int d = hasB ? goff[gB] - oA : 0;  // band B starts d samples after band A
+      int base[RQ];
 #pragma unroll
-    for (int i = 0; i < RQ; i++) base[i] = (rbase + 32 * i) * (int)p.S + oA;
-    Acc<T, OC> acc[RQ][8];
+      for (int i = 0; i < RQ; i++) base[i] = (rbase + 32 * i) * (int)p.S + oA;
+      Acc<T, OC> acc[RQ][8];
 #pragma unroll
-    for (int i = 0; i < RQ; i++)
+      for (int i = 0; i < RQ; i++)
 #pragma unroll
-      for (int jj = 0; jj < 8; jj++) acc[i][jj].zero();
-    const TapVec<T, HC> *tA = table + gA * p.span;
-    const TapVec<T, HC> *tB = table + (hasB ? gB : gA) * p.span;
-    // range 1: band A only
-    const int e1 = hasB ? min(d, p.span) : p.span;
+        for (int jj = 0; jj < 8; jj++) acc[i][jj].zero();
+      const TapVec<T, HC> *tA = table + gA * p.span;
+      const TapVec<T, HC> *tB = table + (hasB ? gB : gA) * p.span;
+      // range 1: band A only
+      const int e1 = hasB ? min(d, p.span) : p.span;
 #pragma unroll 2
-    for (int kk = 0; kk < e1; kk++) {
-      const TapVec<T, HC> t = tA[kk];
+      for (int kk = 0; kk < e1; kk++) {
+        const TapVec<T, HC> t = tA[kk];
+#pragma unroll
+        for (int i = 0; i < RQ; i++) {
+          const XT xv = cur[smem_idx<PAD>(base[i] + kk)];
+#pragma unroll
+          for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][jj], xv, t.v[jj]);
+        }
+      }
+      if (hasB) {
+        // range 2: both bands
+#pragma unroll 2
+        for (int kk = d; kk < p.span; kk++) {
+          const TapVec<T, HC> ta = tA[kk];
+          const TapVec<T, HC> tb = tB[kk - d];
+#pragma unroll
+          for (int i = 0; i < RQ; i++) {
+            const XT xv = cur[smem_idx<PAD>(base[i] + kk)];
+#pragma unroll
+            for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][jj], xv, ta.v[jj]);
+#pragma unroll
+            for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][4 + jj], xv, tb.v[jj]);
+          }
+        }
+        // range 3: band B only
+#pragma unroll 2
+        for (int kk = max(p.span, d); kk < d + p.span; kk++) {
+          const TapVec<T, HC> tb = tB[kk - d];
+#pragma unroll
+          for (int i = 0; i < RQ; i++) {
+            const XT xv = cur[smem_idx<PAD>(base[i] + kk)];
+#pragma unroll
+            for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][4 + jj], xv, tb.v[jj]);
+          }
+        }
+      }
+      const int j0 = 8 * sg;
+      const int ncol = min(8, (int)p.Nt - j0);
 #pragma unroll
       for (int i = 0; i < RQ; i++) {
-        const XT xv = cur[smem_idx<PAD>(base[i] + kk)];
+        const int64_t n0 = (q0 + rbase + 32 * i) * p.Nt + j0;
+        const int64_t left = p.out_len - n0;
+        const int nv = left < ncol ? (left > 0 ? (int)left : 0) : ncol;
 #pragma unroll
-        for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][jj], xv, t.v[jj]);
-      }
-    }
-    if (hasB) {
-      // range 2: both bands
-#pragma unroll 2
-      for (int kk = d; kk < p.span; kk++) {
-        const TapVec<T, HC> ta = tA[kk];
-        const TapVec<T, HC> tb = tB[kk - d];
-#pragma unroll
-        for (int i = 0; i < RQ; i++) {
-          const XT xv = cur[smem_idx<PAD>(base[i] + kk)];
-#pragma unroll
-          for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][jj], xv, ta.v[jj]);
-#pragma unroll
-          for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][4 + jj], xv, tb.v[jj]);
-        }
-      }
-      // range 3: band B only
-#pragma unroll 2
-      for (int kk = max(p.span, d); kk < d + p.span; kk++) {
-        const TapVec<T, HC> tb = tB[kk - d];
-#pragma unroll
-        for (int i = 0; i < RQ; i++) {
-          const XT xv = cur[smem_idx<PAD>(base[i] + kk)];
-#pragma unroll
-          for (int jj = 0; jj < 4; jj++) mac<T, XC, HC>(acc[i][4 + jj], xv, tb.v[jj]);
-        }
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < RQ; i++) {
-      const int64_t q = q0 + rbase + 32 * i;
-#pragma unroll
-      for (int jj = 0; jj < 8; jj++) {
-        const int64_t j = 8 * (int64_t)sg + jj;
-        const int64_t n = q * p.Nt + j;
-        if (j < p.Nt && n < p.out_len) orow[n] = pack<T, OC>(acc[i][jj], scale);
+        for (int jj = 0; jj < 8; jj++)
+          if (jj < nv) orow[n0 + jj] = pack<T, OC>(acc[i][jj], scale);
       }
     }
   }
@@ -170,8 +316,8 @@ __global__ void __launch_bounds__(256) resample_rowtile(const RsParams p) {
   using OT = typename val_of<T, XC || HC>::type;
   constexpr bool OC = XC || HC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  TapVec<T, HC> *table = reinterpret_cast<TapVec<T, HC> *>(smem_raw);
-  const size_t table_bytes = ((size_t)p.ncg * p.span * sizeof(TapVec<T, HC>) + 15) & ~(size_t)15;
+  unsigned char *table = smem_raw;
+  const size_t table_bytes = tap_table_bytes<T, XC, HC>(p.ncg, p.span);
   XT *xbuf0 = reinterpret_cast<XT *>(smem_raw + table_bytes);
   XT *xbuf1 = xbuf0 + p.win_alloc;
 
@@ -180,7 +326,7 @@ __global__ void __launch_bounds__(256) resample_rowtile(const RsParams p) {
   const XT *xp = reinterpret_cast<const XT *>(p.x);
   OT *op = reinterpret_cast<OT *>(p.out);
 
-  build_tap_table<T, HC>(p, hp, table, tid, blockDim.x);
+  build_tap_table<T, XC, HC>(p, hp, table, tid, blockDim.x);
 
   auto issue_loads = [&](int64_t tile, XT *buf) {
     const int64_t b = tile / p.tiles_per_row;
@@ -369,8 +515,7 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
     const int64_t QC = 32LL * rq * (8 / wc);
     const int64_t win = (QC - 1) * geo.S + (geo.kmax - geo.kmin) + 1;
     const int64_t alloc = pad ? win + (win >> 4) + 1 : win;
-    const size_t table = ((size_t)geo.ncg * geo.span * 4 * sizeof(HT) + 15) & ~(size_t)15;
-    return table + (size_t)nbuf * (size_t)alloc * sizeof(XT);
+    return tap_table_bytes<T, XC, HC>(geo.ncg, geo.span) + (size_t)nbuf * (size_t)alloc * sizeof(XT);
   };
   int rq = tc.rq > 0 ? tc.rq : 2;
   if (sizeof(T) == 8) rq = 1;

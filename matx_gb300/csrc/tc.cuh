@@ -141,5 +141,18 @@ __device__ __forceinline__ void split3_bf16(float a, __nv_bfloat16 &a0, __nv_bfl
   a2 = __float2bfloat16_rn(r2);
 }
 
+// The same split for two values at once: each bf16x2 conversion rounds both lanes to
+// nearest, and the residuals are exact, so t_i.x / t_i.y equal split3_bf16 of a.x / a.y.
+__device__ __forceinline__ void split3_bf16x2(float2 a, __nv_bfloat162 &t0, __nv_bfloat162 &t1,
+                                              __nv_bfloat162 &t2) {
+  t0 = __float22bfloat162_rn(a);
+  const float2 b0 = __bfloat1622float2(t0);
+  const float2 r1 = __fadd2_rn(a, make_float2(-b0.x, -b0.y));
+  t1 = __float22bfloat162_rn(r1);
+  const float2 b1 = __bfloat1622float2(t1);
+  const float2 r2 = __fadd2_rn(r1, make_float2(-b1.x, -b1.y));
+  t2 = __float22bfloat162_rn(r2);
+}
+
 }  // namespace tc
 }  // namespace gbfir

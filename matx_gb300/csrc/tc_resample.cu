@@ -32,7 +32,6 @@
 
 namespace gbfir {
 
-constexpr int kTcThreads = 256;
 
 struct TcParams {
   const void *x;
@@ -196,41 +195,42 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
       // convert raw slot -> operand slot: two consecutive samples of one component per item
       const XT *src = rawp(rslot);
       const int half = p.LA / 2;
-      for (int e = ptid; e < p.P * half; e += kNProd) {
-        const int pp = e / half, u = 2 * (e - pp * half);
-        XT v0, v1;
-        if (p.P == 1) {
-          if constexpr (XC) {
-            const float4 v = *reinterpret_cast<const float4 *>(src + u);
-            v0 = make_float2(v.x, v.y);
-            v1 = make_float2(v.z, v.w);
-          } else {
-            const float2 v = *reinterpret_cast<const float2 *>(src + u);
-            v0 = v.x;
-            v1 = v.y;
-          }
-        } else {
-          v0 = src[(size_t)u * p.P + pp];
-          v1 = src[(size_t)(u + 1) * p.P + pp];
-        }
+      for (int pp = 0; pp < p.P; pp++) {
+        unsigned char *dst[NPARTS][3];
 #pragma unroll
-        for (int part = 0; part < NPARTS; part++) {
-          const float f0 = part == 0 ? re_of(v0) : im_of(v0);
-          const float f1 = part == 0 ? re_of(v1) : im_of(v1);
-          if (p.fp16) {
-            *reinterpret_cast<__half2 *>(reinterpret_cast<__half *>(xarrp(slot, part, 0, pp)) + u) =
-                __floats2half2_rn(f0, f1);
+        for (int part = 0; part < NPARTS; part++)
+#pragma unroll
+          for (int t = 0; t < 3; t++) dst[part][t] = xarrp(slot, part, t < p.terms ? t : 0, pp);
+        for (int v = ptid; v < half; v += kNProd) {
+          const int u = 2 * v;
+          XT v0, v1;
+          if (p.P == 1) {
+            if constexpr (XC) {
+              const float4 w = *reinterpret_cast<const float4 *>(src + u);
+              v0 = make_float2(w.x, w.y);
+              v1 = make_float2(w.z, w.w);
+            } else {
+              const float2 w = *reinterpret_cast<const float2 *>(src + u);
+              v0 = w.x;
+              v1 = w.y;
+            }
           } else {
-            __nv_bfloat16 a0, a1, a2, b0, b1, b2;
-            tc::split3_bf16(f0, a0, a1, a2);
-            tc::split3_bf16(f1, b0, b1, b2);
-            *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<__nv_bfloat16 *>(xarrp(slot, part, 0, pp)) + u) =
-                __halves2bfloat162(a0, b0);
-            if (p.terms == 3) {
-              *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<__nv_bfloat16 *>(xarrp(slot, part, 1, pp)) + u) =
-                  __halves2bfloat162(a1, b1);
-              *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<__nv_bfloat16 *>(xarrp(slot, part, 2, pp)) + u) =
-                  __halves2bfloat162(a2, b2);
+            v0 = src[(size_t)u * p.P + pp];
+            v1 = src[(size_t)(u + 1) * p.P + pp];
+          }
+#pragma unroll
+          for (int part = 0; part < NPARTS; part++) {
+            const float2 f = part == 0 ? make_float2(re_of(v0), re_of(v1)) : make_float2(im_of(v0), im_of(v1));
+            if (p.fp16) {
+              reinterpret_cast<__half2 *>(dst[part][0])[v] = __float22half2_rn(f);
+            } else {
+              __nv_bfloat162 t0, t1, t2;
+              tc::split3_bf16x2(f, t0, t1, t2);
+              reinterpret_cast<__nv_bfloat162 *>(dst[part][0])[v] = t0;
+              if (p.terms == 3) {
+                reinterpret_cast<__nv_bfloat162 *>(dst[part][1])[v] = t1;
+                reinterpret_cast<__nv_bfloat162 *>(dst[part][2])[v] = t2;
+              }
             }
           }
         }
@@ -252,6 +252,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
       const uint32_t idesc1 = tc::idesc_f16(128, (uint32_t)p.Nmma, p.fp16 ? 0u : 1u);
       const uint32_t wsbo = (uint32_t)(p.Kp / 8) * 128u;
       const int nks = p.Kp / 16;
+      // descriptor fields that never change; only the 14-bit start address (bytes >> 4) moves
+      const uint64_t afix = tc::smem_desc(0u, 16u, 128u), bfix = tc::smem_desc(0u, 128u, wsbo);
+      const uint32_t xs0 = tc::smem_u32(xbase), w0 = tc::smem_u32(wbase);
       int64_t it = blockIdx.x;
       for (int k = 0; it < p.niters; it += gridDim.x, ++k) {
         const int slot = k % p.nbuf, tset = k % p.nsets;
@@ -259,34 +262,38 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
         if (k >= p.nsets && !tc::mbar_wait(&tm_empty[tset], ((k - p.nsets) / p.nsets) & 1)) { s_fail = 1; break; }
         tc::tc_fence_after();
         const uint32_t dset = tmem + (uint32_t)tset * set_cols;
-        for (int m = 0; m < p.MT; m++) {
-          for (int part = 0; part < NPARTS; part++) {
-            const uint32_t d = dset + (uint32_t)((m * NPARTS + part) * wrows);
+        // Issue order (measured): with three terms, accumulator-major — per (M-tile, part)
+        // the K-steps, each step's a0*[b0|b1|b2], a1*[b0|b1], a2*b0 back to back; with one
+        // term, step-major — consecutive MMAs write different accumulators.
+        const int nacc = p.MT * NPARTS;
+        auto a_desc = [&](int a, int t, int pp, int ks) -> uint64_t {
+          const int m = a / NPARTS, part = a - m * NPARTS;
+          const uint32_t aaddr = xs0 + (uint32_t)((((slot * NPARTS + part) * p.terms + t) * p.P + pp) * xarr) +
+                                 (uint32_t)(8 * 128 * m) * 2u;
+          return (afix | (uint64_t)(aaddr >> 4)) + (uint64_t)(2 * ks);
+        };
+        if (p.terms == 3) {
+          for (int a = 0; a < nacc; a++) {
+            const uint32_t d = dset + (uint32_t)(a * wrows);
             for (int pp = 0; pp < p.P; pp++) {
-              const uint32_t a_off = (uint32_t)(8 * 128 * m) * 2u;
-              uint64_t bd = tc::smem_desc(tc::smem_u32(warr(pp)), 128u, wsbo);
-              if (p.terms == 3) {
-                uint64_t a0 = tc::smem_desc(tc::smem_u32(xarrp(slot, part, 0, pp)) + a_off, 16u, 128u);
-                uint64_t a1 = tc::smem_desc(tc::smem_u32(xarrp(slot, part, 1, pp)) + a_off, 16u, 128u);
-                uint64_t a2 = tc::smem_desc(tc::smem_u32(xarrp(slot, part, 2, pp)) + a_off, 16u, 128u);
-                for (int ks = 0; ks < nks; ks++) {
-                  // D[0:3N) (+)= a0 * [b0|b1|b2];  D[N:3N) += a1 * [b0|b1];  D[2N:3N) += a2 * b0
-                  tc::mma_f16(d, a0, bd, idesc3, (pp > 0 || ks > 0) ? 1u : 0u);
-                  tc::mma_f16(d + (uint32_t)p.Nmma, a1, bd, idesc2, 1u);
-                  tc::mma_f16(d + (uint32_t)(2 * p.Nmma), a2, bd, idesc1, 1u);
-                  a0 += 2;
-                  a1 += 2;
-                  a2 += 2;
-                  bd += 16;
-                }
-              } else {
-                uint64_t a0 = tc::smem_desc(tc::smem_u32(xarrp(slot, part, 0, pp)) + a_off, 16u, 128u);
-                for (int ks = 0; ks < nks; ks++) {
-                  tc::mma_f16(d, a0, bd, idesc1, (pp > 0 || ks > 0) ? 1u : 0u);
-                  a0 += 2;
-                  bd += 16;
-                }
+              const uint64_t bd0 = bfix | (uint64_t)((w0 + (uint32_t)pp * wbytes) >> 4);
+              for (int ks = 0; ks < nks; ks++) {
+                const uint64_t bd = bd0 + (uint64_t)(16 * ks);
+                // D[0:3N) (+)= a0 * [b0|b1|b2];  D[N:3N) += a1 * [b0|b1];  D[2N:3N) += a2 * b0
+                tc::mma_f16(d, a_desc(a, 0, pp, ks), bd, idesc3, (pp > 0 || ks > 0) ? 1u : 0u);
+                tc::mma_f16(d + (uint32_t)p.Nmma, a_desc(a, 1, pp, ks), bd, idesc2, 1u);
+                tc::mma_f16(d + (uint32_t)(2 * p.Nmma), a_desc(a, 2, pp, ks), bd, idesc1, 1u);
               }
+            }
+          }
+        } else {
+          for (int pp = 0; pp < p.P; pp++) {
+            const uint64_t bd0 = bfix | (uint64_t)((w0 + (uint32_t)pp * wbytes) >> 4);
+            for (int ks = 0; ks < nks; ks++) {
+              const uint64_t bd = bd0 + (uint64_t)(16 * ks);
+              for (int a = 0; a < nacc; a++)
+                tc::mma_f16(dset + (uint32_t)(a * wrows), a_desc(a, 0, pp, ks), bd, idesc1,
+                            (pp > 0 || ks > 0) ? 1u : 0u);
             }
           }
         }
@@ -314,31 +321,48 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
       XT *orow = reinterpret_cast<XT *>(p.out) + b * p.out_bstride;
       for (int m = 0; m < p.MT; m++) {
         const int64_t q = q0 + 128 * m + 32 * quarter + lane;
+        const int64_t n0 = q * p.Nt;
+        const int64_t left64 = p.out_len - n0;
+        const int nv = left64 < p.Nt ? (left64 > 0 ? (int)left64 : 0) : p.Nt;  // valid outputs of this row
+        XT *dst = orow + n0;
+        const bool vec = XC && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0);
         for (int col = 0; col < p.Nmma; col += 16) {
           float acc[NPARTS][16];
 #pragma unroll
           for (int part = 0; part < NPARTS; part++) {
             const uint32_t base = dset + lane_base + (uint32_t)((m * NPARTS + part) * wrows + col);
-            uint32_t r[16];
-            tc::tmem_ld16(base, r);
+            uint32_t r0[16], r1[16], r2[16];
+            tc::tmem_ld16(base, r0);
+            if (p.terms == 3) {
+              tc::tmem_ld16(base + (uint32_t)p.Nmma, r1);
+              tc::tmem_ld16(base + (uint32_t)(2 * p.Nmma), r2);
+            }
             tc::tmem_ld_wait();
+            if (p.terms == 3) {
 #pragma unroll
-            for (int i = 0; i < 16; i++) acc[part][i] = __uint_as_float(r[i]);
-            for (int t = 1; t < p.terms; t++) {
-              tc::tmem_ld16(base + (uint32_t)(t * p.Nmma), r);
-              tc::tmem_ld_wait();
+              for (int i = 0; i < 16; i++)
+                acc[part][i] = (__uint_as_float(r0[i]) + __uint_as_float(r1[i])) + __uint_as_float(r2[i]);
+            } else {
 #pragma unroll
-              for (int i = 0; i < 16; i++) acc[part][i] += __uint_as_float(r[i]);
+              for (int i = 0; i < 16; i++) acc[part][i] = __uint_as_float(r0[i]);
             }
           }
+          if constexpr (XC) {
+            // pairs of outputs as one 16-byte store where the row start is 16-byte aligned
 #pragma unroll
-          for (int i = 0; i < 16; i++) {
-            const int j = col + i;
-            const int64_t n = q * p.Nt + j;
-            if (j < p.Nt && n < p.out_len) {
-              if constexpr (XC) orow[n] = make_float2(acc[0][i], acc[1][i]);
-              else orow[n] = acc[0][i];
+            for (int i = 0; i < 16; i += 2) {
+              if (vec && col + i + 1 < nv) {
+                *reinterpret_cast<float4 *>(dst + col + i) =
+                    make_float4(acc[0][i], acc[1][i], acc[0][i + 1], acc[1][i + 1]);
+              } else {
+                if (col + i < nv) dst[col + i] = make_float2(acc[0][i], acc[1][i]);
+                if (col + i + 1 < nv) dst[col + i + 1] = make_float2(acc[0][i + 1], acc[1][i + 1]);
+              }
             }
+          } else {
+#pragma unroll
+            for (int i = 0; i < 16; i++)
+              if (col + i < nv) dst[col + i] = acc[0][i];
           }
         }
       }
