@@ -207,6 +207,202 @@ def run_reference(args, rank, world):
     return 0
 
 
+def _flush_l2(buf):
+    """Overwrite a buffer larger than L2 (129 MB) so the next launch starts cold."""
+    buf.zero_()
+
+
+def _timed(fn, steps, flush, stream):
+    """Sum of per-launch CUDA-event times of fn over `steps` calls, L2 flushed before each."""
+    import torch
+    total = 0.0
+    for _ in range(steps):
+        flush()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        total += e0.elapsed_time(e1)
+    return total / steps
+
+
+def _peak():
+    return peaks()[0]
+
+
+def run_conv1d(args, rank, world, dev):
+    """conv1d direct FULL, real fp32: 8 rows x 2^20 samples uniform[-1,1], one 63-tap
+    Hamming-windowed sinc low-pass (cut-off 0.25 of Nyquist, unit DC gain)."""
+    import torch
+    from scipy import signal
+    import matx_gb300 as mx
+    B, N, L = 8, 1 << 20, 63
+    rng = np.random.default_rng(21 + rank)
+    xh = rng.uniform(-1, 1, (B, N)).astype(np.float32)
+    h = signal.firwin(L, 0.25, window="hamming").astype(np.float32)
+    x, hd = torch.from_numpy(xh).to(dev), torch.from_numpy(h).to(dev)
+    y = torch.empty(B, N + L - 1, dtype=torch.float32, device=dev)
+    flushbuf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    run = lambda: mx.conv1d(x, hd, "full", out=y)
+    for _ in range(args.warmup):
+        run()
+    l0 = mx.launch_count()
+    steps = max(3, min(args.steps, 100))
+    ms = _timed(run, steps, lambda: _flush_l2(flushbuf), stream)
+    launches = mx.launch_count() - l0
+    macs = B * N * L
+    nbytes = B * 4 * (N + (N + L - 1)) + 4 * L
+    err = None
+    try:
+        import oracle
+        oracle.build()
+        r = oracle.conv1d(xh[:1].astype(np.float64), h.astype(np.float64), 0)
+        err = float(np.linalg.norm(y[:1].cpu().numpy() - r) / np.linalg.norm(r))
+    except Exception as e:  # noqa: BLE001
+        err = {"unavailable": str(e)[:160]}
+    forms = {}
+    for form in ("bf16x3", "bf16", "fp16"):
+        runf = lambda: mx.conv1d(x, hd, "full", out=y, precision=form)
+        try:
+            runf()
+        except mx.GbfirError as ge:
+            forms[form] = {"unavailable": str(ge)[:140]}
+            continue
+        for _ in range(args.warmup):
+            runf()
+        msf = _timed(runf, steps, lambda: _flush_l2(flushbuf), stream)
+        ent = {"ms": msf, "gmacs": macs / (msf * 1e-3) / 1e9, "vs_fp32": ms / msf,
+               "hbm_frac": nbytes / (msf * 1e-3) / 1e9 / _peak()}
+        if isinstance(err, float):
+            ent["rel_l2_vs_fp64_row0"] = float(np.linalg.norm(y[:1].cpu().numpy() - r) / np.linalg.norm(r))
+        forms[form] = ent
+    line = {"metric": "FIR GMAC/s (conv1d direct FULL, real fp32)", "value": macs / (ms * 1e-3) / 1e9,
+            "unit": "GMAC/s", "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded uniform[-1,1]; Hamming sinc taps)",
+            "config": {"workload": "conv1d FULL 8x2^20 f32, 63-tap Hamming sinc (cut-off 0.25)",
+                       "l2": "flushed (256 MB write) before every timed launch"},
+            "hbm_gbs": nbytes / (ms * 1e-3) / 1e9, "hbm_frac": nbytes / (ms * 1e-3) / 1e9 / _peak(),
+            "fp32_tflops": 2 * macs / (ms * 1e-3) / 1e12, "rel_l2_vs_fp64_row0": err, "gpu_launches": launches,
+            "forms": forms}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_channelize(args, rank, world, dev):
+    """channelize_poly c64, maximally decimated: 4 rows x 2^24 samples, M = 64 with a
+    64x32 Kaiser sinc prototype and M = 256 with 16 taps per channel; FP32 and the
+    tensor-core DFT-GEMM forms."""
+    import torch
+    from scipy import signal
+    import matx_gb300 as mx
+    B, N = 4, 1 << 24
+    g = torch.Generator(device=dev).manual_seed(31 + rank)
+    x = torch.randn(B, N, dtype=torch.complex64, device=dev, generator=g)
+    flushbuf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    res = {}
+    steps = max(3, min(args.steps, 30))
+    for M, P in ((64, 32), (256, 16)):
+        h = torch.from_numpy(signal.firwin(M * P, 1.0 / M, window=("kaiser", 5.0)).astype(np.float32)).to(dev)
+        T = (N + M - 1) // M
+        y = torch.empty(B, T, M, dtype=torch.complex64, device=dev)
+        macs = B * N * P                      # FIR branch MACs (complex x real)
+        nbytes = B * (8 * N + 8 * T * M) + 4 * M * P
+        xr = x[1:2].cpu().numpy().astype(np.complex128)
+        r64 = None
+        try:
+            import oracle
+            oracle.build()
+            r64 = oracle.channelize_poly(xr[:, : M * 4096], h.cpu().numpy().astype(np.float64), M, M)
+        except Exception:  # noqa: BLE001
+            pass
+        for form in ("fp32", "bf16x3", "bf16", "fp16"):
+            run = lambda: mx.channelize_poly(x, h, M, M, precision=form, out=y)
+            try:
+                run()
+            except mx.GbfirError as ge:
+                res[f"M{M}/{form}"] = {"unavailable": str(ge)[:140]}
+                continue
+            for _ in range(args.warmup):
+                run()
+            ms = _timed(run, steps, lambda: _flush_l2(flushbuf), stream)
+            ent = {"ms": ms, "gmacs_fir": macs / (ms * 1e-3) / 1e9, "hbm_gbs": nbytes / (ms * 1e-3) / 1e9,
+                   "hbm_frac": nbytes / (ms * 1e-3) / 1e9 / _peak(),
+                   "output_samples_per_s": B * T * M / (ms * 1e-3)}
+            if r64 is not None:
+                yy = y[1, :4096].cpu().numpy()
+                ent["rel_l2_vs_fp64"] = float(np.linalg.norm(yy - r64[0]) / np.linalg.norm(r64[0]))
+            res[f"M{M}/{form}"] = ent
+    best = res["M64/fp32"]
+    line = {"metric": "FIR GMAC/s (channelize_poly c64, FIR branch MACs; DFT fused)",
+            "value": best["gmacs_fir"], "unit": "GMAC/s", "n_gpus": world, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": best["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded complex Gaussian; Kaiser sinc prototype)",
+            "config": {"workload": "channelize_poly c64 4x2^24, D = M, M=64 (P=32) and M=256 (P=16)",
+                       "l2": "inputs larger than L2, also flushed before every timed launch"},
+            "forms": res}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_fwdbwd(args, rank, world, dev):
+    """Differentiable resample_poly fp32: 256 rows x 16384 samples uniform[-1,1], a
+    learnable 127-tap filter N(0, 1/127), (up, down) = (3, 2) and (1, 1), loss = MSE
+    against the output of a fixed seeded Kaiser filter; one step = forward + backward."""
+    import torch
+    from scipy import signal
+    import matx_gb300 as mx
+    from matx_gb300 import autograd as ag
+    B, N, L = 256, 16384, 127
+    g = torch.Generator(device=dev).manual_seed(41 + rank)
+    x = (torch.rand(B, N, device=dev, generator=g) * 2 - 1).requires_grad_(True)
+    flushbuf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    res = {}
+    steps = max(3, min(args.steps, 100))
+    total_macs, total_ms = 0, 0.0
+    for up, down in ((3, 2), (1, 1)):
+        h = (torch.randn(L, device=dev, generator=g) / L ** 0.5).requires_grad_(True)
+        href = torch.from_numpy(signal.firwin(L, 1.0 / max(up, down, 2), window=("kaiser", 5.0))
+                                .astype(np.float32)).to(dev)
+        with torch.no_grad():
+            target = mx.resample_poly(x.detach(), href, up, down)
+
+        def step():
+            x.grad = None
+            h.grad = None
+            y = ag.resample_poly(x, h, up, down)
+            loss = torch.mean((y - target) ** 2)
+            loss.backward()
+        for _ in range(args.warmup):
+            step()
+        l0 = mx.launch_count()
+        ms = _timed(step, steps, lambda: _flush_l2(flushbuf), stream)
+        launches = mx.launch_count() - l0
+        fmacs = mac_count(N, L, up, down) * B if (up, down) != (1, 1) else 0
+        macs = 3 * fmacs                       # forward, dL/dx (transposed resampler), dL/dh
+        res[f"{up}/{down}"] = {"ms": ms, "gmacs": (macs / (ms * 1e-3) / 1e9) if macs else None,
+                               "fwd_macs": fmacs, "library_launches_per_step": launches / steps}
+        total_macs += macs
+        total_ms += ms
+    line = {"metric": "FIR GMAC/s (resample_poly fp32 forward + backward, dL/dx and dL/dh)",
+            "value": total_macs / (total_ms * 1e-3) / 1e9, "unit": "GMAC/s", "n_gpus": world, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": total_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform[-1,1]; N(0,1/127) taps)",
+            "config": {"workload": "differentiable resample_poly 256x16384 f32, 127 taps, (3,2) and (1,1); "
+                                   "MSE loss, torch.autograd through the hand-written adjoint",
+                       "l2": "flushed (256 MB write) before every timed step"},
+            "per_ratio": res}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 RAGGED_RATIOS = [(1, 2), (2, 3), (3, 4), (5, 4), (160, 147)]
 
 
@@ -314,8 +510,11 @@ def main():
                     help="fixed row tiles instead of tuning, e.g. '3/2=4,2,4,2;4/5=2,1,1,2' "
                          "(rows_per_thread, col_warps, group, buffers; profiling cases)")
     ap.add_argument("--ratios", default="3/2,4/5,160/147", help="comma-separated up/down list (profiling cases)")
-    ap.add_argument("--workload", default="resample", choices=["resample", "ragged"],
-                    help="ragged: 4096 uneven signals in one persistent launch (separate JSON line)")
+    ap.add_argument("--workload", default="resample",
+                    choices=["resample", "ragged", "conv1d", "channelize", "fwdbwd"],
+                    help="secondary workloads, each printing its own JSON line: ragged (4096 uneven signals "
+                         "in one persistent launch), conv1d (8x2^20 FULL), channelize (4x2^24, M=64/256), "
+                         "fwdbwd (256x16384 forward + backward)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     BATCH = args.batch
@@ -338,6 +537,12 @@ def main():
     stream = torch.cuda.current_stream()
     if args.workload == "ragged":
         return run_ragged(args, rank, world, dev)
+    if args.workload == "conv1d":
+        return run_conv1d(args, rank, world, dev)
+    if args.workload == "channelize":
+        return run_channelize(args, rank, world, dev)
+    if args.workload == "fwdbwd":
+        return run_fwdbwd(args, rank, world, dev)
 
     xh = make_inputs(1234 + rank)
     taps_np = [kaiser_taps(u, d) for u, d in RATIOS]

@@ -112,12 +112,14 @@ def set_resample_tile(rows_per_thread: int = 0, col_warps: int = 0, group: int =
 
 
 def conv1d(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torch.Tensor | None = None,
-           _corr: bool = False) -> torch.Tensor:
+           precision="fp32", _corr: bool = False) -> torch.Tensor:
     """Direct 1-D convolution (MatX conv1d with MATX_C_METHOD_DIRECT).
 
     Output length: N+L-1 (FULL), max(N,L) (SAME), max(N,L)-min(N,L)+1 (VALID).
     The operand with more dimensions sets the batch shape; a 1-D operand is
-    broadcast across the other's batch (conv.h:467-532).
+    broadcast across the other's batch (conv.h:467-532).  ``precision`` "bf16",
+    "fp16" or "bf16x3" runs the Toeplitz MMA form on the tensor cores (a real
+    float32 filter shared by all rows, signal at least as long as the filter).
     """
     lib = _lib.load()
     m = _mode(mode)
@@ -138,13 +140,14 @@ def conv1d(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torc
     if out is None:
         out = torch.empty(*batch_shape, olen, dtype=odt, device=x.device)
     _lib.check(lib.gbfir_conv1d(_buf(out, "conv1d out"), _buf(x, "conv1d x"), _buf(h, "conv1d h"),
-                                m, int(_corr), 0, _stream()))
+                                m, int(_corr), _prec(precision), _stream()))
     return out
 
 
-def corr(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torch.Tensor | None = None):
+def corr(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torch.Tensor | None = None,
+         precision="fp32"):
     """Direct correlation: corr(x, h) = conv1d(x, reverse(conj(h))) (corr.h:67)."""
-    return conv1d(x, h, mode, out=out, _corr=True)
+    return conv1d(x, h, mode, out=out, precision=precision, _corr=True)
 
 
 def resample_out_len(n: int, up: int, down: int) -> int:

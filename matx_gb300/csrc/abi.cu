@@ -23,6 +23,8 @@ int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf 
                      int precision, cudaStream_t s);
 int channelize_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t M, int64_t D,
                        int precision, cudaStream_t s);
+int conv1d_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int mode, int is_corr, int precision,
+              cudaStream_t s);
 int set_resample_tile(int rq, int wc, int group, int nbuf);
 int register_resample_tile(int64_t up, int64_t down, int64_t L, int rq, int wc, int group, int nbuf);
 int clear_resample_tiles();
@@ -142,7 +144,7 @@ int gbfir_conv1d(gbfir_buf out, gbfir_buf in, gbfir_buf h, int32_t mode, int32_t
       GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "conv1d: output length %lld, expected %lld", (long long)out.len,
                  (long long)want);
     if (precision != GBFIR_PREC_FP32)
-      GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "conv1d: only the FP32 form is available for conv1d");
+      return conv1d_tc(out, in, h, mode, is_corr != 0, precision, reinterpret_cast<cudaStream_t>(stream));
     return conv1d_fp(out, in, h, mode, is_corr != 0, reinterpret_cast<cudaStream_t>(stream));
   } catch (...) {
     GBFIR_FAIL(GBFIR_ERR_CUDA, "conv1d: internal exception");

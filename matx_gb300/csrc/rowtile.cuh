@@ -56,19 +56,9 @@ template <typename T>
 struct TapVec<T, true> {
   typename cplx_of<T>::type v[4];
 };
-// Complex signal, real float taps: each tap stored twice, (t0,t0,t1,t1),(t2,t2,t3,t3), so a
-// 16-byte shared load yields the (t,t) operand pairs of two packed f32x2 FMAs.
-struct TapDup {
-  float4 v[2];
-};
-
 template <typename T, bool XC, bool HC>
 struct TapEntry {
   using type = TapVec<T, HC>;
-};
-template <>
-struct TapEntry<float, true, false> {
-  using type = TapDup;
 };
 
 // Shared bytes of the tap table: ncg*span entries, then one int32 band offset per group.
@@ -106,13 +96,7 @@ __device__ __forceinline__ void build_tap_table(const RsParams &p, const typenam
       const int64_t te = p.rev ? p.Lo - 1 - tp : tp;  // index into he
       if (!(p.even && te == 0)) v = hp[te - p.even];
     }
-    if constexpr (std::is_same<TE, TapDup>::value) {
-      float *f = reinterpret_cast<float *>(&table[g * p.span + kk]);
-      f[2 * jj] = v;
-      f[2 * jj + 1] = v;
-    } else {
-      table[g * p.span + kk].v[jj] = v;
-    }
+    table[g * p.span + kk].v[jj] = v;
   }
   for (int g = tid; g < p.ncg; g += nthreads)
     goff[g] = (int)(ceil_div(p.c + 4 * (int64_t)g * p.down - p.Lo + 1, p.up) - p.kmin);
@@ -129,14 +113,16 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a
 
 // Complex float signal x real float taps, the hot case: the same three-range walk as the
 // generic form below with (re, im) accumulated by one f32x2 FMA per sample and phase
-// (each lane is the fma of MatX's madd for a real tap, so results are unchanged), and
+// (each lane is the fma of MatX's madd for a real tap, so results are unchanged; the
+// (t, t) operand pairs are formed in registers from one 16-byte load of 4 taps), and
 // each row's 8 outputs written as four 16-byte stores when they are whole and aligned.
 template <int RQ, bool PAD>
 __device__ __forceinline__ void rowtile_compute_c2(const RsParams &p, const float2 *cur,
                                                    const unsigned char *table_raw, float2 *orow, int64_t q0, int wr,
                                                    int wc, int lane, float scale) {
-  const TapDup *table = reinterpret_cast<const TapDup *>(table_raw);
-  const int *goff = tap_goff(p, table_raw, sizeof(TapDup));
+  using TV = TapVec<float, false>;
+  const TV *table = reinterpret_cast<const TV *>(table_raw);
+  const int *goff = tap_goff(p, table_raw, sizeof(TV));
   const int nsg = (p.ncg + 1) / 2;
   const int rbase = wr * 32 * RQ + lane;
   const float2 sc = make_float2(scale, scale);
@@ -154,12 +140,13 @@ __device__ __forceinline__ void rowtile_compute_c2(const RsParams &p, const floa
     for (int i = 0; i < RQ; i++)
 #pragma unroll
       for (int jj = 0; jj < 8; jj++) acc[i][jj] = make_float2(0.f, 0.f);
-    const TapDup *tA = table + gA * p.span;
-    const TapDup *tB = table + (hasB ? gB : gA) * p.span;
+    const TV *tA = table + gA * p.span;
+    const TV *tB = table + (hasB ? gB : gA) * p.span;
     const int e1 = hasB ? min(d, p.span) : p.span;
 #pragma unroll 2
     for (int kk = 0; kk < e1; kk++) {
-      const float4 a0 = tA[kk].v[0], a1 = tA[kk].v[1];
+      const float4 a = *reinterpret_cast<const float4 *>(tA[kk].v);
+      const float4 a0 = make_float4(a.x, a.x, a.y, a.y), a1 = make_float4(a.z, a.z, a.w, a.w);
 #pragma unroll
       for (int i = 0; i < RQ; i++) {
         const float2 xv = cur[smem_idx<PAD>(base[i] + kk)];
@@ -172,8 +159,10 @@ __device__ __forceinline__ void rowtile_compute_c2(const RsParams &p, const floa
     if (hasB) {
 #pragma unroll 2
       for (int kk = d; kk < p.span; kk++) {
-        const float4 a0 = tA[kk].v[0], a1 = tA[kk].v[1];
-        const float4 b0 = tB[kk - d].v[0], b1 = tB[kk - d].v[1];
+        const float4 a = *reinterpret_cast<const float4 *>(tA[kk].v);
+        const float4 b = *reinterpret_cast<const float4 *>(tB[kk - d].v);
+        const float4 a0 = make_float4(a.x, a.x, a.y, a.y), a1 = make_float4(a.z, a.z, a.w, a.w);
+        const float4 b0 = make_float4(b.x, b.x, b.y, b.y), b1 = make_float4(b.z, b.z, b.w, b.w);
 #pragma unroll
         for (int i = 0; i < RQ; i++) {
           const float2 xv = cur[smem_idx<PAD>(base[i] + kk)];
@@ -189,7 +178,8 @@ __device__ __forceinline__ void rowtile_compute_c2(const RsParams &p, const floa
       }
 #pragma unroll 2
       for (int kk = max(p.span, d); kk < d + p.span; kk++) {
-        const float4 b0 = tB[kk - d].v[0], b1 = tB[kk - d].v[1];
+        const float4 b = *reinterpret_cast<const float4 *>(tB[kk - d].v);
+        const float4 b0 = make_float4(b.x, b.x, b.y, b.y), b1 = make_float4(b.z, b.z, b.w, b.w);
 #pragma unroll
         for (int i = 0; i < RQ; i++) {
           const float2 xv = cur[smem_idx<PAD>(base[i] + kk)];
@@ -231,7 +221,7 @@ __device__ __forceinline__ void rowtile_compute(const RsParams &p, const typenam
                                                 const unsigned char *table_raw,
                                                 typename val_of<T, XC || HC>::type *orow, int64_t q0, int wr, int wc,
                                                 int lane, T scale) {
-  if constexpr (std::is_same<typename TapEntry<T, XC, HC>::type, TapDup>::value) {
+  if constexpr (std::is_same<T, float>::value && XC && !HC) {
     rowtile_compute_c2<RQ, PAD>(p, cur, table_raw, orow, q0, wr, wc, lane, scale);
   } else {
     using XT = typename val_of<T, XC>::type;

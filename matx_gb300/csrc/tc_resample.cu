@@ -393,19 +393,38 @@ struct TcPlan {
   char why[160];
 };
 
-static TcPlan plan_tc(int64_t up, int64_t down, int64_t L, int64_t N_in, int64_t out_len, int64_t batch, int xc,
-                      int precision, int rev) {
+// Tap geometry of one pass: y[n] = scale * sum_i x[i] * he(c + n*down - i*up), with he the
+// filter of logical length Lo (a virtual leading zero when `even`), read reversed when rev.
+struct TcTaps {
+  int64_t Lo, c;
+  int32_t even, rev;
+  double scale;
+};
+
+// resample_poly: scipy centring, even filters extended by a leading zero, gain up.
+static TcTaps resample_taps(int64_t L, int64_t up) {
+  TcTaps t{};
+  t.even = (L % 2) == 0;
+  t.Lo = L + t.even;
+  t.c = (t.Lo - 1) / 2;
+  t.rev = 0;
+  t.scale = (double)up;
+  return t;
+}
+
+static TcPlan plan_tc(int64_t up, int64_t down, const TcTaps &taps, int64_t N_in, int64_t out_len, int64_t batch,
+                      int xc, int precision) {
   TcPlan pl{};
   TcParams &p = pl.p;
-  p.even = (L % 2) == 0;
-  p.Lo = L + p.even;
-  p.c = (p.Lo - 1) / 2;
-  p.rev = rev;
+  p.even = taps.even;
+  p.Lo = taps.Lo;
+  p.c = taps.c;
+  p.rev = taps.rev;
   p.up = up;
   p.down = down;
   p.N = N_in;
   p.out_len = out_len;
-  p.scale = (double)up;
+  p.scale = taps.scale;
   p.fp16 = precision == GBFIR_PREC_FP16;
   p.terms = precision == GBFIR_PREC_BF16X3 ? 3 : 1;
   p.path = (8 % down == 0) ? 0 : 1;
@@ -478,24 +497,16 @@ static TcPlan plan_tc(int64_t up, int64_t down, int64_t L, int64_t N_in, int64_t
   return pl;
 }
 
-int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t up, int64_t down,
-                     int precision, cudaStream_t s) {
-  if (dtype_double(in.dtype) || dtype_complex(h.dtype))
-    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly: tensor-core forms take float32/complex64 signals and real "
-                                        "float32 taps");
-  const bool xc = dtype_complex(in.dtype);
-  TcPlan pl = plan_tc(up, down, h.len, in.len, out.len, out.batch, xc, precision, 0);
-  if (!pl.ok)
-    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly: tensor-core form unavailable for up=%lld down=%lld: %s",
-               (long long)up, (long long)down, pl.why);
+static int launch_tc(TcPlan &pl, const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, bool xc,
+                     const char *what, cudaStream_t s) {
   TcParams &p = pl.p;
   p.x = in.ptr;
-  p.x_bstride = out.batch > 1 ? in.batch_stride : 0;
+  p.x_bstride = (out.batch > 1 && in.batch > 1) ? in.batch_stride : 0;
   p.h = reinterpret_cast<const float *>(h.ptr);
   p.out = out.ptr;
   p.out_bstride = out.batch_stride;
   const void *fn = xc ? (const void *)tc_resample_kernel<true> : (const void *)tc_resample_kernel<false>;
-  int rc = ensure_smem(fn, pl.smem, "resample_poly (tensor cores)");
+  int rc = ensure_smem(fn, pl.smem, what);
   if (rc) return rc;
   int occ = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kWsThreads, pl.smem);
@@ -505,9 +516,50 @@ int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf 
   if (grid > p.niters) grid = p.niters;
   void *args[] = {&p};
   cudaError_t e = cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kWsThreads), args, pl.smem, s);
-  if (e != cudaSuccess) GBFIR_FAIL(GBFIR_ERR_CUDA, "resample_poly (tensor cores): %s", cudaGetErrorString(e));
+  if (e != cudaSuccess) GBFIR_FAIL(GBFIR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
   count_launch();
   return GBFIR_SUCCESS;
+}
+
+int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t up, int64_t down,
+                     int precision, cudaStream_t s) {
+  if (dtype_double(in.dtype) || dtype_complex(h.dtype))
+    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly: tensor-core forms take float32/complex64 signals and real "
+                                        "float32 taps");
+  const bool xc = dtype_complex(in.dtype);
+  TcPlan pl = plan_tc(up, down, resample_taps(h.len, up), in.len, out.len, out.batch, xc, precision);
+  if (!pl.ok)
+    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly: tensor-core form unavailable for up=%lld down=%lld: %s",
+               (long long)up, (long long)down, pl.why);
+  return launch_tc(pl, out, in, h, xc, "resample_poly (tensor cores)", s);
+}
+
+// conv1d / corr on the tensor cores: the Toeplitz pass with up = down = 1, no even-length
+// extension, gain 1 and the mode's start offset as the centre (conv.h:155-168 semantics:
+// out[o] = full[o + start], start = 0 FULL, (L-1)/2 or L/2-1 SAME, L-1 VALID); corr reads
+// the (real) taps reversed.  Covers a real float32 filter row shared by every signal row,
+// with the signal at least as long as the filter (no operand swap).
+int conv1d_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int mode, int is_corr, int precision,
+              cudaStream_t s) {
+  if (dtype_double(in.dtype) || dtype_complex(h.dtype))
+    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "conv1d: tensor-core forms take float32/complex64 signals and real "
+                                        "float32 taps");
+  if (h.batch > 1)
+    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "conv1d: tensor-core forms take one filter row for all signal rows");
+  if (in.len < h.len)
+    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "conv1d: tensor-core forms need the signal at least as long as the filter "
+                                        "(%lld < %lld)", (long long)in.len, (long long)h.len);
+  const int64_t L = h.len;
+  TcTaps t{};
+  t.Lo = L;
+  t.even = 0;
+  t.rev = is_corr ? 1 : 0;
+  t.scale = 1.0;
+  t.c = mode == GBFIR_MODE_SAME ? ((L & 1) ? (L - 1) / 2 : L / 2 - 1) : mode == GBFIR_MODE_VALID ? L - 1 : 0;
+  const bool xc = dtype_complex(in.dtype);
+  TcPlan pl = plan_tc(1, 1, t, in.len, out.len, out.batch, xc, precision);
+  if (!pl.ok) GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "conv1d: tensor-core form unavailable: %s", pl.why);
+  return launch_tc(pl, out, in, h, xc, "conv1d (tensor cores)", s);
 }
 
 int tc_status_read_and_clear() {
