@@ -109,7 +109,10 @@ typedef struct gbfir_buf {
  *  at (Lmin-1)/2 for odd Lmin and Lmin/2-1 for even Lmin (kernels/conv.cuh:155-168).
  *  is_corr != 0 computes corr(in, h) = conv1d(in, reverse(conj(h))) (corr.h:67).
  *  `in` and `h` may each be batched (same row count as out) or broadcast.
- *  out is complex if either operand is complex. */
+ *  out is complex if either operand is complex.
+ *  precision != FP32 runs the Toeplitz MMA form on the tensor cores; it takes float32 /
+ *  complex64 signals with one real float32 filter row no longer than the signal, and
+ *  returns GBFIR_ERR_NOT_SUPPORTED for other operands. */
 GBFIR_API int gbfir_conv1d(gbfir_buf out, gbfir_buf in, gbfir_buf h, int32_t mode,
                  int32_t is_corr, int32_t precision, gbfir_stream_t stream);
 
@@ -119,7 +122,10 @@ GBFIR_API int gbfir_conv1d(gbfir_buf out, gbfir_buf in, gbfir_buf h, int32_t mod
  *  out.len must equal ceil(in.len*up/down) with the UNREDUCED up/down
  *  (resample_poly.h:318-320); up/down are then divided by their gcd; up==down
  *  copies the input and ignores h (resample_poly.h:333-336).
- *  h is one row (broadcast); real or complex. */
+ *  h is one row (broadcast); real or complex.
+ *  precision != FP32 runs the Toeplitz MMA form on the tensor cores for float32 /
+ *  complex64 signals and real float32 taps; rates whose 8-sample rows need more than
+ *  256 MMA columns (for example 160/147) return GBFIR_ERR_NOT_SUPPORTED. */
 GBFIR_API int gbfir_resample_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t up,
                         int64_t down, int32_t precision, gbfir_stream_t stream);
 
@@ -127,7 +133,10 @@ GBFIR_API int gbfir_resample_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int6
  * fused FIR branch filtering + unnormalised positive-sign M-point DFT
  * (include/matx/transforms/channelize_poly.h:724-849, host semantics :858-1029).
  *  out is [batch][T][M] complex with T = ceil(in.len/D): out.len == T*M.
- *  h is one row of any length L; it is zero-padded to P*M with P = ceil(L/M). */
+ *  h is one row of any length L; it is zero-padded to P*M with P = ceil(L/M).
+ *  precision != FP32 runs the cross-channel DFT as a dense complex GEMM on the tensor
+ *  cores (complex64 signal, real float32 taps, D == M with M in {16, 32, 64}); other
+ *  shapes return GBFIR_ERR_NOT_SUPPORTED. */
 GBFIR_API int gbfir_channelize_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t M,
                           int64_t D, int32_t precision, gbfir_stream_t stream);
 
