@@ -262,9 +262,10 @@ GBFIR_API int gbfir_tc_gemm_selftest(const float *A, const float *B, float *C, i
                            int32_t N, int32_t K, int32_t terms, int32_t swap_offsets,
                            int32_t *status, gbfir_stream_t stream);
 
-/* Status of the bounded waits inside the tensor-core kernels of the current device
- * since the last call: 0 = none gave up, 1 = at least one gave up (its results
- * are incomplete), -1 = could not be read.  Synchronous; clears the flag. */
+/* Status of the bounded waits inside the pipelined kernels of the current device (the
+ * tensor-core kernels and the TMA-fed row tile) since the last call: 0 = none gave up,
+ * 1 = at least one gave up (its results are incomplete), -1 = could not be read.
+ * Synchronous; clears the flags. */
 GBFIR_API int gbfir_tc_status(void);
 
 /* Number of device kernels this library has launched in this process. */

@@ -372,6 +372,10 @@ static int check_real(const gbfir_buf &b, const char *name, bool allow_broadcast
   return GBFIR_SUCCESS;
 }
 
+// Bounded-wait status of the row-tile launches made from this file (1 = a window copy
+// did not complete); read and cleared by gbfir_tc_status().
+int adjoint_rowtile_status() { return rowtile_status_take(); }
+
 }  // namespace gbfir
 
 using namespace gbfir;

@@ -165,9 +165,9 @@ __global__ void __launch_bounds__(kRgThreads) ragged_rowtile(const RgParams rp) 
     const int wr = wid / p.WC, wc = wid - wr * p.WC;
     float2 *orow = reinterpret_cast<float2 *>(p.out);
     if (pad) {
-      rowtile_compute<float, true, false, 1, true>(p, xbuf, table, orow, q0, wr, wc, lane, (float)p.scale);
+      rowtile_compute<float, true, false, 1, true>(p, xbuf, table, orow, q0, wr, wc, lane, (float)p.scale, 0);
     } else {
-      rowtile_compute<float, true, false, 1, false>(p, xbuf, table, orow, q0, wr, wc, lane, (float)p.scale);
+      rowtile_compute<float, true, false, 1, false>(p, xbuf, table, orow, q0, wr, wc, lane, (float)p.scale, 0);
     }
     __syncthreads();
   }

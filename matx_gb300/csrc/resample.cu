@@ -142,4 +142,8 @@ int set_resample_tile(int rq, int wc, int group, int nbuf) {
   return GBFIR_SUCCESS;
 }
 
+// Bounded-wait status of the row-tile launches made from this file (1 = a window copy
+// did not complete); read and cleared by gbfir_tc_status().
+int resample_rowtile_status() { return rowtile_status_take(); }
+
 }  // namespace gbfir

@@ -21,8 +21,20 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "tc.cuh"
 
 namespace gbfir {
+
+// Bounded-wait status of the row-tile kernels of this translation unit (1 = a window copy
+// did not complete within the spin limit); read and cleared through rowtile_status_take().
+static __device__ int32_t g_rowtile_status;
+
+static inline int rowtile_status_take() {
+  int32_t v = 0, zero = 0;
+  if (cudaMemcpyFromSymbol(&v, g_rowtile_status, sizeof(v)) != cudaSuccess) return -1;
+  cudaMemcpyToSymbol(g_rowtile_status, &zero, sizeof(zero));
+  return v;
+}
 
 struct RsParams {
   const void *x;
@@ -119,7 +131,7 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a
 template <int RQ, bool PAD>
 __device__ __forceinline__ void rowtile_compute_c2(const RsParams &p, const float2 *cur,
                                                    const unsigned char *table_raw, float2 *orow, int64_t q0, int wr,
-                                                   int wc, int lane, float scale) {
+                                                   int wc, int lane, float scale, int woff) {
   using TV = TapVec<float, false>;
   const TV *table = reinterpret_cast<const TV *>(table_raw);
   const int *goff = tap_goff(p, table_raw, sizeof(TV));
@@ -134,7 +146,7 @@ __device__ __forceinline__ void rowtile_compute_c2(const RsParams &p, const floa
     const int d = hasB ? goff[gB] - oA : 0;
     int base[RQ];
 #pragma unroll
-    for (int i = 0; i < RQ; i++) base[i] = (rbase + 32 * i) * (int)p.S + oA;
+    for (int i = 0; i < RQ; i++) base[i] = (rbase + 32 * i) * (int)p.S + oA + woff;
     float2 acc[RQ][8];
 #pragma unroll
     for (int i = 0; i < RQ; i++)
@@ -216,13 +228,15 @@ __device__ __forceinline__ void rowtile_compute_c2(const RsParams &p, const floa
 
 // One tile of QC rows starting at row q0: every warp (wr, wc) accumulates its 8-phase
 // super-groups for RQ rows per lane and stores them (masked by Nt and out_len).
+// woff: where element 0 of the tile's logical window sits in `cur` (the window copy may
+// start up to 15 bytes early so that it is 16-byte aligned).
 template <typename T, bool XC, bool HC, int RQ, bool PAD>
 __device__ __forceinline__ void rowtile_compute(const RsParams &p, const typename val_of<T, XC>::type *cur,
                                                 const unsigned char *table_raw,
                                                 typename val_of<T, XC || HC>::type *orow, int64_t q0, int wr, int wc,
-                                                int lane, T scale) {
+                                                int lane, T scale, int woff) {
   if constexpr (std::is_same<T, float>::value && XC && !HC) {
-    rowtile_compute_c2<RQ, PAD>(p, cur, table_raw, orow, q0, wr, wc, lane, scale);
+    rowtile_compute_c2<RQ, PAD>(p, cur, table_raw, orow, q0, wr, wc, lane, scale, woff);
   } else {
     using XT = typename val_of<T, XC>::type;
     constexpr bool OC = XC || HC;
@@ -237,7 +251,7 @@ __device__ __forceinline__ void rowtile_compute(const RsParams &p, const typenam
       const int d = hasB ? goff[gB] - oA : 0;  // band B starts d samples after band A
       int base[RQ];
 #pragma unroll
-      for (int i = 0; i < RQ; i++) base[i] = (rbase + 32 * i) * (int)p.S + oA;
+      for (int i = 0; i < RQ; i++) base[i] = (rbase + 32 * i) * (int)p.S + oA + woff;
       Acc<T, OC> acc[RQ][8];
 #pragma unroll
       for (int i = 0; i < RQ; i++)
@@ -318,50 +332,137 @@ __global__ void __launch_bounds__(256) resample_rowtile(const RsParams p) {
 
   build_tap_table<T, XC, HC>(p, hp, table, tid, blockDim.x);
 
-  auto issue_loads = [&](int64_t tile, XT *buf) {
-    const int64_t b = tile / p.tiles_per_row;
-    const int64_t q0 = (tile - b * p.tiles_per_row) * p.QC;
-    const int64_t xs0 = q0 * p.S + p.kmin;
-    const XT *row = xp + b * p.x_bstride;
-    for (int e = tid; e < p.win; e += blockDim.x) {
-      const int64_t gi = xs0 + e;
-      const bool ok = gi >= 0 && gi < p.N;
-      cp_async_zfill<sizeof(XT)>(&buf[smem_idx<PAD>(e)], ok ? (const void *)(row + gi) : (const void *)row, ok);
-    }
-  };
-
-  const bool dbuf = p.nbuf == 2;
-  int64_t tile = blockIdx.x;
-  if (tile < p.ntiles) issue_loads(tile, xbuf0);
-  cp_async_commit();
-
   const int wid = tid >> 5, lane = tid & 31;
   const int wr = wid / p.WC, wc = wid - wr * p.WC;
   const T scale = T(p.scale);
+  const bool dbuf = p.nbuf == 2;
 
-  for (int it = 0; tile < p.ntiles; tile += gridDim.x, ++it) {
-    XT *cur = (dbuf && (it & 1)) ? xbuf1 : xbuf0;
-    const int64_t next = tile + gridDim.x;
-    if (dbuf) {
-      if (next < p.ntiles) issue_loads(next, (it & 1) ? xbuf0 : xbuf1);
-      cp_async_commit();
-      cp_async_wait<1>();
-    } else {
-      cp_async_wait<0>();
+  if constexpr (PAD) {
+    // Even row stride: the window is stored with one pad element per 16 (bank-conflict
+    // free row-strided reads), which a bulk copy cannot produce; stage it with cp.async
+    // (zero-filled outside the signal).
+    auto issue_loads = [&](int64_t tile, XT *buf) {
+      const int64_t b = tile / p.tiles_per_row;
+      const int64_t q0 = (tile - b * p.tiles_per_row) * p.QC;
+      const int64_t xs0 = q0 * p.S + p.kmin;
+      const XT *row = xp + b * p.x_bstride;
+      if (xs0 >= 0 && xs0 + p.win <= p.N) {
+        const XT *src = row + xs0;
+        for (int e = tid; e < p.win; e += blockDim.x) cp_async_zfill<sizeof(XT)>(&buf[smem_idx<PAD>(e)], src + e, true);
+      } else {
+        for (int e = tid; e < p.win; e += blockDim.x) {
+          const int64_t gi = xs0 + e;
+          const bool ok = gi >= 0 && gi < p.N;
+          cp_async_zfill<sizeof(XT)>(&buf[smem_idx<PAD>(e)], ok ? (const void *)(row + gi) : (const void *)row, ok);
+        }
+      }
+    };
+
+    int64_t tile = blockIdx.x;
+    if (tile < p.ntiles) issue_loads(tile, xbuf0);
+    cp_async_commit();
+    for (int it = 0; tile < p.ntiles; tile += gridDim.x, ++it) {
+      XT *cur = (dbuf && (it & 1)) ? xbuf1 : xbuf0;
+      const int64_t next = tile + gridDim.x;
+      if (dbuf) {
+        if (next < p.ntiles) issue_loads(next, (it & 1) ? xbuf0 : xbuf1);
+        cp_async_commit();
+        cp_async_wait<1>();
+      } else {
+        cp_async_wait<0>();
+      }
+      __syncthreads();
+
+      const int64_t b = tile / p.tiles_per_row;
+      const int64_t q0 = (tile - b * p.tiles_per_row) * p.QC;
+      OT *orow = op + b * p.out_bstride;
+      rowtile_compute<T, XC, HC, RQ, PAD>(p, cur, table, orow, q0, wr, wc, lane, scale, 0);
+      __syncthreads();
+      if (!dbuf && next < p.ntiles) {
+        issue_loads(next, xbuf0);
+        cp_async_commit();
+      }
+    }
+    cp_async_wait<0>();
+  } else {
+    // Odd row stride: the window is one contiguous run of the signal, brought in by one
+    // TMA bulk copy (thread 0) that completes on an mbarrier.  The copy starts at the
+    // 16-byte boundary at or below the window start (`a` elements early) and covers a
+    // multiple of 16 bytes; windows that reach past either end of the signal are staged
+    // element by element with zeros outside instead.
+    constexpr int ES = (int)sizeof(XT), G = 16 / ES;
+    __shared__ uint64_t s_bar[2];
+    __shared__ int s_ok;
+    if (tid == 0) {
+      tc::mbar_init(&s_bar[0], 1);
+      tc::mbar_init(&s_bar[1], 1);
+      tc::mbar_fence_init();
     }
     __syncthreads();
+    // every thread computes the same origin offset of tile t
+    auto origin = [&](int64_t t, int64_t &b, int64_t &w0) -> int {
+      b = t / p.tiles_per_row;
+      const int64_t q0 = (t - b * p.tiles_per_row) * p.QC;
+      const int64_t xs0 = q0 * p.S + p.kmin;
+      const int a = (int)((reinterpret_cast<uintptr_t>(xp + b * p.x_bstride + xs0) & 15) / ES);
+      w0 = xs0 - a;
+      return a;
+    };
+    auto issue_window = [&](int64_t t, XT *buf, uint64_t *bar) {
+      int64_t b, w0;
+      const int a = origin(t, b, w0);
+      const int64_t wl = (p.win + a + G - 1) / G * G;
+      const XT *row = xp + b * p.x_bstride;
+      // the bulk copy's alignment rules hold by construction; check them anyway and take
+      // the element path if they do not
+      const bool aligned = ((reinterpret_cast<uintptr_t>(row + w0) | (uintptr_t)tc::smem_u32(buf)) & 15) == 0;
+      if (aligned && w0 >= 0 && w0 + wl <= p.N) {
+        if (tid == 0) {
+          const uint32_t bytes = (uint32_t)(wl * ES);
+          tc::fence_async_smem();
+          tc::mbar_arrive_expect_tx(bar, bytes);
+          tc::bulk_copy_g2s(buf, row + w0, bytes, bar);
+        }
+      } else {
+        for (int64_t e = tid; e < wl; e += blockDim.x) {
+          const int64_t gi = w0 + e;
+          buf[e] = (gi >= 0 && gi < p.N) ? row[gi] : zero_val<XT>();
+        }
+        if (tid == 0) tc::mbar_arrive_plain(bar);
+      }
+    };
 
-    const int64_t b = tile / p.tiles_per_row;
-    const int64_t q0 = (tile - b * p.tiles_per_row) * p.QC;
-    OT *orow = op + b * p.out_bstride;
-    rowtile_compute<T, XC, HC, RQ, PAD>(p, cur, table, orow, q0, wr, wc, lane, scale);
-    __syncthreads();
-    if (!dbuf && next < p.ntiles) {
-      issue_loads(next, xbuf0);
-      cp_async_commit();
+    int64_t tile = blockIdx.x;
+    if (tile < p.ntiles) issue_window(tile, xbuf0, &s_bar[0]);
+    for (int it = 0; tile < p.ntiles; tile += gridDim.x, ++it) {
+      const int k = dbuf ? (it & 1) : 0;
+      XT *cur = k ? xbuf1 : xbuf0;
+      const uint32_t parity = dbuf ? ((it >> 1) & 1) : (it & 1);
+      const int64_t next = tile + gridDim.x;
+      // the other buffer was released by the barrier that ended the previous tile
+      if (dbuf && next < p.ntiles) issue_window(next, k ? xbuf0 : xbuf1, &s_bar[k ^ 1]);
+      if (tid == 0) s_ok = tc::mbar_wait(&s_bar[k], parity) ? 1 : 0;
+      __syncthreads();
+      if (!s_ok) {
+        // a copy that never completed: record it and stop; give the copies in flight a
+        // bounded chance to land before the CTA (and its shared memory) goes away
+        if (tid == 0) {
+          atomicExch(&g_rowtile_status, 1);
+          (void)tc::mbar_wait(&s_bar[k], parity);
+          if (dbuf) (void)tc::mbar_wait(&s_bar[k ^ 1], parity);
+        }
+        __syncthreads();
+        break;
+      }
+      int64_t b, w0;
+      const int a = origin(tile, b, w0);
+      const int64_t q0 = (tile - b * p.tiles_per_row) * p.QC;
+      OT *orow = op + b * p.out_bstride;
+      rowtile_compute<T, XC, HC, RQ, PAD>(p, cur, table, orow, q0, wr, wc, lane, scale, a);
+      __syncthreads();
+      if (!dbuf && next < p.ntiles) issue_window(next, xbuf0, &s_bar[0]);
     }
   }
-  cp_async_wait<0>();
 }
 
 // Host planning shared by the forward launch and the ragged planner.
@@ -501,10 +602,15 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
   }
   if (wc > nsg) wc = 1;
   const bool pad = (geo.S % 2) == 0;
+  // window buffer: padded layout for even S; for odd S room for the 16-byte-aligned bulk copy
+  constexpr int64_t G16 = 16 / (int64_t)sizeof(XT);
+  auto window_alloc = [&](int64_t win) -> int64_t {
+    return pad ? win + (win >> 4) + 1 : (win + 3 * G16 - 1) / G16 * G16;
+  };
   auto smem_for = [&](int rq, int nbuf) -> size_t {
     const int64_t QC = 32LL * rq * (8 / wc);
     const int64_t win = (QC - 1) * geo.S + (geo.kmax - geo.kmin) + 1;
-    const int64_t alloc = pad ? win + (win >> 4) + 1 : win;
+    const int64_t alloc = window_alloc(win);
     return tap_table_bytes<T, XC, HC>(geo.ncg, geo.span) + (size_t)nbuf * (size_t)alloc * sizeof(XT);
   };
   int rq = tc.rq > 0 ? tc.rq : 2;
@@ -547,7 +653,7 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
     p.ntiles = p.tiles_per_row * batch;
     const int64_t win = (int64_t)(p.QC - 1) * geo.S + (geo.kmax - geo.kmin) + 1;
     p.win = (int32_t)win;
-    p.win_alloc = (int32_t)(pad ? win + (win >> 4) + 1 : win);
+    p.win_alloc = (int32_t)window_alloc(win);
     return dispatch_rq<T, XC, HC>(p, rq, pad, smem, s);
   }
   // row tile too large for shared memory: direct form

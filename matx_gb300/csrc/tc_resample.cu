@@ -571,4 +571,18 @@ int tc_status_read_and_clear() {
 
 }  // namespace gbfir
 
-extern "C" int gbfir_tc_status(void) { return gbfir::tc_status_read_and_clear(); }
+namespace gbfir {
+int resample_rowtile_status();
+int adjoint_rowtile_status();
+}  // namespace gbfir
+
+// 0 if every bounded wait of the pipelined kernels (tensor-core kernels and the TMA-fed
+// row tile) completed since the last call; 1 if one gave up; -1 if the status could not
+// be read.
+extern "C" int gbfir_tc_status(void) {
+  const int a = gbfir::tc_status_read_and_clear();
+  const int b = gbfir::resample_rowtile_status();
+  const int c = gbfir::adjoint_rowtile_status();
+  if (a < 0 || b < 0 || c < 0) return -1;
+  return (a | b | c) ? 1 : 0;
+}
