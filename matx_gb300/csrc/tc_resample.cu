@@ -497,6 +497,10 @@ static TcPlan plan_tc(int64_t up, int64_t down, const TcTaps &taps, int64_t N_in
   return pl;
 }
 
+}  // namespace gbfir
+#include "tc_wide.h"
+namespace gbfir {
+
 static int launch_tc(TcPlan &pl, const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, bool xc,
                      const char *what, cudaStream_t s) {
   TcParams &p = pl.p;
@@ -527,7 +531,15 @@ int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf 
     GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly: tensor-core forms take float32/complex64 signals and real "
                                         "float32 taps");
   const bool xc = dtype_complex(in.dtype);
-  TcPlan pl = plan_tc(up, down, resample_taps(h.len, up), in.len, out.len, out.batch, xc, precision);
+  const TcTaps taps = resample_taps(h.len, up);
+  // 64-sample rows where they fill at least half of the 128 MMA lanes with output phases
+  // (measured faster there); the 8-sample-row kernel otherwise
+  if (64 % down == 0 && 64 * up / down >= 64) {
+    TwPlan wp = plan_tc_wide(up, down, taps.Lo, taps.c, taps.even, taps.rev, taps.scale, in.len, out.len, out.batch,
+                             xc, precision);
+    if (wp.ok) return launch_tc_wide(wp, out, in, h, xc, "resample_poly (tensor cores)", s);
+  }
+  TcPlan pl = plan_tc(up, down, taps, in.len, out.len, out.batch, xc, precision);
   if (!pl.ok)
     GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly: tensor-core form unavailable for up=%lld down=%lld: %s",
                (long long)up, (long long)down, pl.why);
@@ -574,6 +586,7 @@ int tc_status_read_and_clear() {
 namespace gbfir {
 int resample_rowtile_status();
 int adjoint_rowtile_status();
+int tc_wide_status_take();
 }  // namespace gbfir
 
 // 0 if every bounded wait of the pipelined kernels (tensor-core kernels and the TMA-fed
@@ -583,6 +596,7 @@ extern "C" int gbfir_tc_status(void) {
   const int a = gbfir::tc_status_read_and_clear();
   const int b = gbfir::resample_rowtile_status();
   const int c = gbfir::adjoint_rowtile_status();
-  if (a < 0 || b < 0 || c < 0) return -1;
-  return (a | b | c) ? 1 : 0;
+  const int d = gbfir::tc_wide_status_take();
+  if (a < 0 || b < 0 || c < 0 || d < 0) return -1;
+  return (a | b | c | d) ? 1 : 0;
 }

@@ -15,6 +15,12 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
+def seed_of(*key) -> int:
+    """A seed fixed by the test parameters (Python's own hash() of strings changes per process)."""
+    import zlib
+    return zlib.crc32(repr(key).encode())
+
+
 def rel_l2(a, b):
     a = np.asarray(a, dtype=np.complex128).ravel()
     b = np.asarray(b, dtype=np.complex128).ravel()

@@ -11,7 +11,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, load_cases, rel_l2
+from conftest import GOLDEN, load_cases, rel_l2, seed_of
 
 pytestmark = pytest.mark.gpu
 
@@ -83,7 +83,7 @@ CONV_SHAPES = [(3, 5000, 63), (2, 4097, 64), (1, 100, 1), (2, 1, 1), (2, 7, 300)
 @pytest.mark.parametrize("is_corr", [False, True])
 def test_conv_random(mx, orc, shape, mode, kind, is_corr):
     B, N, L = shape
-    rng = np.random.default_rng(abs(hash((shape, mode, kind, is_corr))) % 2**32)
+    rng = np.random.default_rng(seed_of(shape, mode, kind, is_corr))
     dbl = kind in ("f64", "c128")
     x = rng.uniform(-1, 1, (B, N))
     h = rng.standard_normal(L)
@@ -100,7 +100,11 @@ def test_conv_random(mx, orc, shape, mode, kind, is_corr):
     y = host((mx.corr if is_corr else mx.conv1d)(dev(x), dev(h), mode))
     r = orc.conv1d(x, h, mode, is_corr)
     assert y.shape == r.shape
-    assert rel_l2(y, r) < (FP64_TOL if dbl else FP32_TOL)
+    # rel-L2 against the result, or against the magnitude of the products (the forward
+    # error bound of a sum) where the result itself cancels to much less than that
+    scale = np.linalg.norm(orc.conv1d(np.abs(x), np.abs(h), mode, is_corr))
+    err = np.linalg.norm(y - r) / max(np.linalg.norm(r), 0.1 * scale)
+    assert err < (FP64_TOL if dbl else FP32_TOL)
 
 
 def test_conv_batched_filters(mx, orc):
@@ -161,7 +165,7 @@ RATIOS = [(3, 2), (4, 5), (160, 147), (1, 2), (2, 3), (3, 4), (5, 4), (2, 1), (7
 @pytest.mark.parametrize("kind", ["c64_rh", "f32", "c64_ch", "f32_ch", "c128_rh", "f64"])
 def test_resample_random(mx, orc, updown, kind):
     up, down = updown
-    rng = np.random.default_rng(abs(hash((updown, kind))) % 2**32)
+    rng = np.random.default_rng(seed_of(updown, kind))
     B, N = 3, 5003
     dbl = kind.startswith("c128") or kind == "f64"
     x = rng.standard_normal((B, N))
@@ -280,7 +284,7 @@ def test_channelize_harris2003_oversampled(mx, double):
 @pytest.mark.parametrize("kind", ["c64_rh", "c64_ch", "f32"])
 def test_channelize_random(mx, orc, MD, taps_per, kind):
     M, D = MD
-    rng = np.random.default_rng(abs(hash((MD, taps_per, kind))) % 2**32)
+    rng = np.random.default_rng(seed_of(MD, taps_per, kind))
     N = 40 * M + 17
     x = rng.standard_normal((2, N))
     if kind.startswith("c"):
