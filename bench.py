@@ -390,6 +390,25 @@ def run_fwdbwd(args, rank, world, dev):
                                "fwd_macs": fmacs, "library_launches_per_step": launches / steps}
         total_macs += macs
         total_ms += ms
+        if (up, down) == (3, 2):
+            # tensor-core forms of the forward and dL/dx (dL/dh stays FP32 with FP64 sums)
+            forms = {}
+            for form in ("bf16x3", "bf16", "fp16"):
+                def step_f():
+                    x.grad = None
+                    h.grad = None
+                    y = ag.resample_poly(x, h, up, down, precision=form)
+                    torch.mean((y - target) ** 2).backward()
+                try:
+                    step_f()
+                except mx.GbfirError as ge:
+                    forms[form] = {"unavailable": str(ge)[:140]}
+                    continue
+                for _ in range(args.warmup):
+                    step_f()
+                msf = _timed(step_f, steps, lambda: _flush_l2(flushbuf), stream)
+                forms[form] = {"ms": msf, "gmacs": macs / (msf * 1e-3) / 1e9, "vs_fp32": ms / msf}
+            res["3/2"]["forms"] = forms
     line = {"metric": "FIR GMAC/s (resample_poly fp32 forward + backward, dL/dx and dL/dh)",
             "value": total_macs / (total_ms * 1e-3) / 1e9, "unit": "GMAC/s", "n_gpus": world, "steps": steps,
             "warmup": args.warmup, "ms_per_step": total_ms, "higher_is_better": True, "scaling": "weak",

@@ -54,6 +54,7 @@ SIGNATURES = [
     ("gbfir_channelize_poly", ctypes.c_int, [_B, _B, _B, _i64, _i64, _i32, _p]),
     ("gbfir_resample_poly_bwd_workspace_size", _sz, [_i64, _i64, _i64, _i64, _i64]),
     ("gbfir_resample_poly_bwd", ctypes.c_int, [_B, _B, _B, _B, _B, _i64, _i64, _p, _sz, _p]),
+    ("gbfir_resample_poly_bwd_prec", ctypes.c_int, [_B, _B, _B, _B, _B, _i64, _i64, _i32, _p, _sz, _p]),
     ("gbfir_resample_poly_bwd_noalloc", ctypes.c_int, [_B, _B, _B, _B, _B, _i64, _i64, _p]),
     ("gbfir_conv1d_bwd_workspace_size", _sz, [_i64, _i64, _i64, _i32]),
     ("gbfir_conv1d_bwd", ctypes.c_int, [_B, _B, _B, _B, _B, _i32, _p, _sz, _p]),

@@ -21,7 +21,7 @@ import torch
 from . import _lib
 from . import conv1d as _conv1d_fwd
 from . import resample_poly as _resample_fwd
-from . import _buf, _mode, _stream
+from . import _buf, _mode, _prec, _stream
 
 _WS = {}
 
@@ -40,8 +40,12 @@ def _null_buf():
 
 
 def resample_poly_bwd(gy: torch.Tensor, x: torch.Tensor, h: torch.Tensor, up: int, down: int,
-                      need_dx: bool = True, need_dh: bool = True):
-    """(dx, dh) of y = resample_poly(x, h, up, down) for upstream gradient gy."""
+                      need_dx: bool = True, need_dh: bool = True, precision="fp32"):
+    """(dx, dh) of y = resample_poly(x, h, up, down) for upstream gradient gy.
+
+    ``precision`` other than "fp32" computes dx on the tensor cores (bf16, fp16 or
+    bf16x3 Toeplitz MMAs); dh always comes from the FP32 reduction with FP64 sums.
+    """
     lib = _lib.load()
     gy = gy.contiguous()
     x = x.contiguous()
@@ -51,9 +55,9 @@ def resample_poly_bwd(gy: torch.Tensor, x: torch.Tensor, h: torch.Tensor, up: in
     B = x.numel() // x.shape[-1]
     nb = lib.gbfir_resample_poly_bwd_workspace_size(B, x.shape[-1], h.shape[-1], up, down)
     ws = _workspace(nb, x.device)
-    _lib.check(lib.gbfir_resample_poly_bwd(
+    _lib.check(lib.gbfir_resample_poly_bwd_prec(
         _buf(dx, "dx") if need_dx else _null_buf(), _buf(dh, "dh") if need_dh else _null_buf(),
-        _buf(gy, "gy"), _buf(x, "x"), _buf(h, "h"), int(up), int(down),
+        _buf(gy, "gy"), _buf(x, "x"), _buf(h, "h"), int(up), int(down), _prec(precision),
         ctypes.c_void_p(ws.data_ptr()), ws.numel(), _stream()))
     return dx, dh
 
@@ -80,16 +84,17 @@ def conv1d_bwd(gy: torch.Tensor, x: torch.Tensor, h: torch.Tensor, mode, need_dx
 
 class ResamplePolyFn(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, x, h, up, down):
+    def forward(ctx, x, h, up, down, precision="fp32"):
         ctx.save_for_backward(x, h)
-        ctx.up, ctx.down = int(up), int(down)
-        return _resample_fwd(x, h, up, down)
+        ctx.up, ctx.down, ctx.precision = int(up), int(down), precision
+        return _resample_fwd(x, h, up, down, precision=precision)
 
     @staticmethod
     def backward(ctx, gy):
         x, h = ctx.saved_tensors
-        dx, dh = resample_poly_bwd(gy, x, h, ctx.up, ctx.down, ctx.needs_input_grad[0], ctx.needs_input_grad[1])
-        return dx, dh, None, None
+        dx, dh = resample_poly_bwd(gy, x, h, ctx.up, ctx.down, ctx.needs_input_grad[0], ctx.needs_input_grad[1],
+                                   precision=ctx.precision)
+        return dx, dh, None, None, None
 
 
 class Conv1dFn(torch.autograd.Function):
@@ -106,10 +111,11 @@ class Conv1dFn(torch.autograd.Function):
         return dx, dh, None
 
 
-def resample_poly(x: torch.Tensor, h: torch.Tensor, up: int, down: int) -> torch.Tensor:
+def resample_poly(x: torch.Tensor, h: torch.Tensor, up: int, down: int, precision="fp32") -> torch.Tensor:
+    """Differentiable resample_poly; ``precision`` selects the forward and dL/dx arithmetic."""
     if x.dtype != torch.float32 or h.dtype != torch.float32 or h.dim() != 1:
         raise TypeError("matx_gb300.autograd.resample_poly: real float32 x and a 1-D float32 filter")
-    return ResamplePolyFn.apply(x, h, up, down)
+    return ResamplePolyFn.apply(x, h, up, down, precision)
 
 
 def conv1d(x: torch.Tensor, h: torch.Tensor, mode=0) -> torch.Tensor:

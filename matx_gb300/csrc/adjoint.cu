@@ -380,6 +380,11 @@ int adjoint_rowtile_status() { return rowtile_status_take(); }
 
 using namespace gbfir;
 
+namespace gbfir {
+int resample_poly_bwd_dx_tc(const gbfir_buf &dx, const gbfir_buf &gy, const gbfir_buf &h, int64_t up, int64_t down,
+                            int precision, cudaStream_t s);
+}  // namespace gbfir
+
 extern "C" {
 
 size_t gbfir_resample_poly_bwd_workspace_size(int64_t batch, int64_t in_len, int64_t h_len, int64_t up,
@@ -392,8 +397,9 @@ size_t gbfir_resample_poly_bwd_workspace_size(int64_t batch, int64_t in_len, int
   return (size_t)max_parts() * (size_t)(h_len + 1) * sizeof(double);
 }
 
-int gbfir_resample_poly_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x, gbfir_buf h, int64_t up,
-                            int64_t down, void *workspace, size_t workspace_bytes, gbfir_stream_t stream) {
+static int resample_bwd_impl(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x, gbfir_buf h, int64_t up,
+                             int64_t down, int32_t precision, void *workspace, size_t workspace_bytes,
+                             gbfir_stream_t stream) {
   try {
     int rc;
     if ((rc = check_real(gy, "resample_poly_bwd gy", false))) return rc;
@@ -431,7 +437,11 @@ int gbfir_resample_poly_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf 
       }
       return GBFIR_SUCCESS;
     }
-    if (dx.ptr) {
+    if (dx.ptr && precision != GBFIR_PREC_FP32) {
+      // dL/dx on the tensor cores: the transposed resampler as a Toeplitz MMA pass
+      rc = resample_poly_bwd_dx_tc(dx, gy, h, up, down, precision, s);
+      if (rc) return rc;
+    } else if (dx.ptr) {
       TileChoice tc;
       rc = resample_pass<float, false, false>(gy.ptr, gy.batch_stride, gy.len, h.ptr, h.len, dx.ptr, dx.batch_stride,
                                               x.len, x.batch, down, up, -1, true, 1, (double)up, tc, s);
@@ -449,6 +459,19 @@ int gbfir_resample_poly_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf 
   }
 }
 
+
+int gbfir_resample_poly_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x, gbfir_buf h, int64_t up,
+                            int64_t down, void *workspace, size_t workspace_bytes, gbfir_stream_t stream) {
+  return resample_bwd_impl(dx, dh, gy, x, h, up, down, GBFIR_PREC_FP32, workspace, workspace_bytes, stream);
+}
+
+int gbfir_resample_poly_bwd_prec(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x, gbfir_buf h, int64_t up,
+                                 int64_t down, int32_t precision, void *workspace, size_t workspace_bytes,
+                                 gbfir_stream_t stream) {
+  if (precision < GBFIR_PREC_FP32 || precision > GBFIR_PREC_BF16X3)
+    GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "resample_poly_bwd: unknown precision %d", (int)precision);
+  return resample_bwd_impl(dx, dh, gy, x, h, up, down, precision, workspace, workspace_bytes, stream);
+}
 
 int gbfir_resample_poly_bwd_noalloc(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x, gbfir_buf h, int64_t up,
                                     int64_t down, gbfir_stream_t stream) {

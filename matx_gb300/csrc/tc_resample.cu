@@ -574,6 +574,24 @@ int conv1d_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int
   return launch_tc(pl, out, in, h, xc, "conv1d (tensor cores)", s);
 }
 
+// dL/dx of resample_poly on the tensor cores: the transposed resampler
+//   dx[m] = up * sum_k gy[k] * he(Lo - 1 - (c + m*up - k*down))
+// is the forward pass with the rates swapped and the taps read reversed (the FP32 adjoint
+// runs the same pass on the CUDA cores).  Real float32 operands, gcd-reduced rates.
+int resample_poly_bwd_dx_tc(const gbfir_buf &dx, const gbfir_buf &gy, const gbfir_buf &h, int64_t up, int64_t down,
+                            int precision, cudaStream_t s) {
+  TcTaps taps = resample_taps(h.len, up);
+  taps.rev = 1;
+  TwPlan wp = plan_tc_wide(down, up, taps.Lo, taps.c, taps.even, taps.rev, taps.scale, gy.len, dx.len, dx.batch, 0,
+                           precision);
+  if (wp.ok) return launch_tc_wide(wp, dx, gy, h, false, "resample_poly_bwd dx (tensor cores)", s);
+  TcPlan pl = plan_tc(down, up, taps, gy.len, dx.len, dx.batch, 0, precision);
+  if (!pl.ok)
+    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly_bwd: tensor-core dx unavailable for up=%lld down=%lld: %s",
+               (long long)up, (long long)down, pl.why);
+  return launch_tc(pl, dx, gy, h, false, "resample_poly_bwd dx (tensor cores)", s);
+}
+
 int tc_status_read_and_clear() {
   int32_t v = 0, zero = 0;
   if (cudaMemcpyFromSymbol(&v, g_tc_status, sizeof(v)) != cudaSuccess) return -1;
