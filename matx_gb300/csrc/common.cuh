@@ -102,8 +102,15 @@ __device__ __forceinline__ void mac(Acc<T, XC || HC> &a,
     a.im = fma(im_of(x), re_of(h), a.im);
     a.im = fma(re_of(x), im_of(h), a.im);
   } else if constexpr (XC) {
-    a.re = fma(re_of(x), h, a.re);
-    a.im = fma(im_of(x), h, a.im);
+    if constexpr (std::is_same<T, float>::value) {
+      // one packed f32x2 FMA: each lane is exactly the scalar fma of the line below
+      const float2 r = __ffma2_rn(x, make_float2(h, h), make_float2(a.re, a.im));
+      a.re = r.x;
+      a.im = r.y;
+    } else {
+      a.re = fma(re_of(x), h, a.re);
+      a.im = fma(im_of(x), h, a.im);
+    }
   } else if constexpr (HC) {
     a.re = fma(x, re_of(h), a.re);
     a.im = fma(x, im_of(h), a.im);
