@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(kDhThreads) rowtile_dh(const DhParams p) {
     for (int e = tid; e < p.win; e += kDhThreads) {
       const int64_t gi = xs0 + e;
       const bool ok = gi >= 0 && gi < p.N;
-      cp_async_zfill<4>(&xb[smem_idx<PAD>(e)], ok ? (const void *)(xr + gi) : (const void *)xr, ok);
+      cp_async_zfill<4>(&xb[smem_idx<PAD ? 4 : 0>(e)], ok ? (const void *)(xr + gi) : (const void *)xr, ok);
     }
     const float *gr = p.gy + b * p.gy_bstride;
     const int64_t g0 = q0 * p.Nt;
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(kDhThreads) rowtile_dh(const DhParams p) {
           const float4 gv = *reinterpret_cast<const float4 *>(gq + gcol[m]);
           float xv[4];
 #pragma unroll
-          for (int kk = 0; kk < 4; kk++) xv[kk] = xc[smem_idx<PAD>(xq + kb[m] + kk)];
+          for (int kk = 0; kk < 4; kk++) xv[kk] = xc[smem_idx<PAD ? 4 : 0>(xq + kb[m] + kk)];
 #pragma unroll
           for (int kk = 0; kk < 4; kk++) {
             acc[m][kk * 4 + 0] = fmaf(xv[kk], gv.x, acc[m][kk * 4 + 0]);

@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(kRgThreads) ragged_rowtile(const RgParams rp) 
     for (int e = tid; e < p.win; e += kRgThreads) {
       const int64_t gi = xs0 + e;
       const bool ok = gi >= 0 && gi < p.N;
-      const int si = pad ? smem_idx<true>(e) : e;
+      const int si = pad ? smem_idx<4>(e) : e;
       cp_async_zfill<8>(&xbuf[si], ok ? (const void *)(row + gi) : (const void *)row, ok);
     }
     cp_async_commit();
@@ -165,9 +165,9 @@ __global__ void __launch_bounds__(kRgThreads) ragged_rowtile(const RgParams rp) 
     const int wr = wid / p.WC, wc = wid - wr * p.WC;
     float2 *orow = reinterpret_cast<float2 *>(p.out);
     if (pad) {
-      rowtile_compute<float, true, false, 1, true>(p, xbuf, table, orow, q0, wr, wc, lane, (float)p.scale, 0);
+      rowtile_compute<float, true, false, 1, 4>(p, xbuf, table, orow, q0, wr, wc, lane, (float)p.scale, 0);
     } else {
-      rowtile_compute<float, true, false, 1, false>(p, xbuf, table, orow, q0, wr, wc, lane, (float)p.scale, 0);
+      rowtile_compute<float, true, false, 1, 0>(p, xbuf, table, orow, q0, wr, wc, lane, (float)p.scale, 0);
     }
     __syncthreads();
   }

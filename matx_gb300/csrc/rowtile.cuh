@@ -80,9 +80,12 @@ __host__ __device__ inline size_t tap_table_bytes(int64_t ncg, int64_t span) {
   return taps + (((size_t)ncg * 4 + 15) & ~(size_t)15);
 }
 
-template <bool PAD>
+// Padded window layout: one pad element after every 2^PAD elements (PAD = 0: none).  A
+// row stride S that is a multiple of 16, 32 or 64 samples reads conflict-free with PAD =
+// 4, 5 or 6 respectively (lanes read rows q*S + k).
+template <int PAD>
 __device__ __forceinline__ int smem_idx(int p) {
-  if constexpr (PAD) return p + (p >> 4);
+  if constexpr (PAD > 0) return p + (p >> PAD);
   else return p;
 }
 
@@ -128,7 +131,7 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a
 // (each lane is the fma of MatX's madd for a real tap, so results are unchanged; the
 // (t, t) operand pairs are formed in registers from one 16-byte load of 4 taps), and
 // each row's 8 outputs written as four 16-byte stores when they are whole and aligned.
-template <int RQ, bool PAD>
+template <int RQ, int PAD>
 __device__ __forceinline__ void rowtile_compute_c2(const RsParams &p, const float2 *cur,
                                                    const unsigned char *table_raw, float2 *orow, int64_t q0, int wr,
                                                    int wc, int lane, float scale, int woff) {
@@ -230,7 +233,7 @@ __device__ __forceinline__ void rowtile_compute_c2(const RsParams &p, const floa
 // super-groups for RQ rows per lane and stores them (masked by Nt and out_len).
 // woff: where element 0 of the tile's logical window sits in `cur` (the window copy may
 // start up to 15 bytes early so that it is 16-byte aligned).
-template <typename T, bool XC, bool HC, int RQ, bool PAD>
+template <typename T, bool XC, bool HC, int RQ, int PAD>
 __device__ __forceinline__ void rowtile_compute(const RsParams &p, const typename val_of<T, XC>::type *cur,
                                                 const unsigned char *table_raw,
                                                 typename val_of<T, XC || HC>::type *orow, int64_t q0, int wr, int wc,
@@ -313,7 +316,7 @@ __device__ __forceinline__ void rowtile_compute(const RsParams &p, const typenam
   }
 }
 
-template <typename T, bool XC, bool HC, int RQ, bool PAD>
+template <typename T, bool XC, bool HC, int RQ, int PAD>
 __global__ void __launch_bounds__(256) resample_rowtile(const RsParams p) {
   using XT = typename val_of<T, XC>::type;
   using HT = typename val_of<T, HC>::type;
@@ -337,7 +340,7 @@ __global__ void __launch_bounds__(256) resample_rowtile(const RsParams p) {
   const T scale = T(p.scale);
   const bool dbuf = p.nbuf == 2;
 
-  if constexpr (PAD) {
+  if constexpr (PAD > 0) {
     // Even row stride: the window is stored with one pad element per 16 (bank-conflict
     // free row-strided reads), which a bulk copy cannot produce; stage it with cp.async
     // (zero-filled outside the signal).
@@ -541,7 +544,7 @@ __global__ void __launch_bounds__(256) resample_direct(const RsParams p, int h_i
   }
 }
 
-template <typename T, bool XC, bool HC, int RQ, bool PAD>
+template <typename T, bool XC, bool HC, int RQ, int PAD>
 inline int launch_rowtile(RsParams &p, size_t smem, cudaStream_t s) {
   auto fn = resample_rowtile<T, XC, HC, RQ, PAD>;
   int rc = ensure_smem((const void *)fn, smem, "resample_poly");
@@ -555,22 +558,25 @@ inline int launch_rowtile(RsParams &p, size_t smem, cudaStream_t s) {
   return check_launch("resample_poly");
 }
 
-template <typename T, bool XC, bool HC>
-inline int dispatch_rq(RsParams &p, int rq, bool pad, size_t smem, cudaStream_t s) {
-  if (pad) {
-    if (rq == 1) return launch_rowtile<T, XC, HC, 1, true>(p, smem, s);
-    if constexpr (sizeof(T) == 4) {
-      if (rq == 2) return launch_rowtile<T, XC, HC, 2, true>(p, smem, s);
-      return launch_rowtile<T, XC, HC, 4, true>(p, smem, s);
-    }
-  } else {
-    if (rq == 1) return launch_rowtile<T, XC, HC, 1, false>(p, smem, s);
-    if constexpr (sizeof(T) == 4) {
-      if (rq == 2) return launch_rowtile<T, XC, HC, 2, false>(p, smem, s);
-      return launch_rowtile<T, XC, HC, 4, false>(p, smem, s);
-    }
+template <typename T, bool XC, bool HC, int PAD>
+inline int dispatch_rq_pad(RsParams &p, int rq, size_t smem, cudaStream_t s) {
+  if (rq == 1) return launch_rowtile<T, XC, HC, 1, PAD>(p, smem, s);
+  if constexpr (sizeof(T) == 4) {
+    if (rq == 2) return launch_rowtile<T, XC, HC, 2, PAD>(p, smem, s);
+    return launch_rowtile<T, XC, HC, 4, PAD>(p, smem, s);
   }
-  return launch_rowtile<T, XC, HC, 1, false>(p, smem, s);
+  return launch_rowtile<T, XC, HC, 1, PAD>(p, smem, s);
+}
+
+// pad: 0 (odd row stride) or the pad shift 4, 5, 6 of the window layout
+template <typename T, bool XC, bool HC>
+inline int dispatch_rq(RsParams &p, int rq, int pad, size_t smem, cudaStream_t s) {
+  if (pad == 0) return dispatch_rq_pad<T, XC, HC, 0>(p, rq, smem, s);
+  if constexpr (std::is_same<T, float>::value && XC && !HC) {
+    if (pad == 5) return dispatch_rq_pad<T, XC, HC, 5>(p, rq, smem, s);
+    if (pad == 6) return dispatch_rq_pad<T, XC, HC, 6>(p, rq, smem, s);
+  }
+  return dispatch_rq_pad<T, XC, HC, 4>(p, rq, smem, s);
 }
 
 // Tile shape knobs: rq rows per thread (1, 2, 4), wc column warps (1..8), G row
@@ -601,11 +607,14 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
     while (wc < 8 && nsg % (wc * 2) == 0) wc *= 2;
   }
   if (wc > nsg) wc = 1;
-  const bool pad = (geo.S % 2) == 0;
+  // even row strides need a padded window (coarser pads for strides of 32 or 64 samples,
+  // complex float signals with real taps)
+  int pad = (geo.S % 2) ? 0 : 4;
+  if (pad && std::is_same<T, float>::value && XC && !HC) pad = geo.S % 64 == 0 ? 6 : geo.S % 32 == 0 ? 5 : 4;
   // window buffer: padded layout for even S; for odd S room for the 16-byte-aligned bulk copy
   constexpr int64_t G16 = 16 / (int64_t)sizeof(XT);
   auto window_alloc = [&](int64_t win) -> int64_t {
-    return pad ? win + (win >> 4) + 1 : (win + 3 * G16 - 1) / G16 * G16;
+    return pad ? win + (win >> pad) + 1 : (win + 3 * G16 - 1) / G16 * G16;
   };
   auto smem_for = [&](int rq, int nbuf) -> size_t {
     const int64_t QC = 32LL * rq * (8 / wc);
