@@ -31,7 +31,8 @@ static std::mutex g_tile_mu;
 static std::unordered_map<TileKey, TileChoice, TileKeyHash> g_tiles;
 
 static bool valid_tile(int rq, int wc, int group, int nbuf) {
-  return (rq == 0 || rq == 1 || rq == 2 || rq == 4) && (wc == 0 || wc == 1 || wc == 2 || wc == 4 || wc == 8) &&
+  // column warps: 1, 2, 4, 8 (8/wc row slices per CTA) or 9..16 (one row slice, rows per thread 1)
+  return (rq == 0 || rq == 1 || rq == 2 || rq == 4) && (wc >= 0 && wc <= 16 && (wc <= 8 ? 8 % (wc ? wc : 1) == 0 : rq == 1)) &&
          group >= 0 && group <= 64 && (nbuf == 0 || nbuf == 1 || nbuf == 2);
 }
 

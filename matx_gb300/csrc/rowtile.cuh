@@ -316,8 +316,10 @@ __device__ __forceinline__ void rowtile_compute(const RsParams &p, const typenam
   }
 }
 
+// 256 threads (8 warps) per CTA, or up to 512 (one row slice of 9..16 column warps) with one
+// row per thread.
 template <typename T, bool XC, bool HC, int RQ, int PAD>
-__global__ void __launch_bounds__(256) resample_rowtile(const RsParams p) {
+__global__ void __launch_bounds__(RQ == 1 ? 512 : 256) resample_rowtile(const RsParams p) {
   using XT = typename val_of<T, XC>::type;
   using HT = typename val_of<T, HC>::type;
   using OT = typename val_of<T, XC || HC>::type;
@@ -545,38 +547,38 @@ __global__ void __launch_bounds__(256) resample_direct(const RsParams p, int h_i
 }
 
 template <typename T, bool XC, bool HC, int RQ, int PAD>
-inline int launch_rowtile(RsParams &p, size_t smem, cudaStream_t s) {
+inline int launch_rowtile(RsParams &p, size_t smem, cudaStream_t s, int threads) {
   auto fn = resample_rowtile<T, XC, HC, RQ, PAD>;
   int rc = ensure_smem((const void *)fn, smem, "resample_poly");
   if (rc) return rc;
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, 256, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, smem);
   if (occ < 1) GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly: tile needs %zu B of shared memory", smem);
   int64_t grid = (int64_t)num_sms() * occ;
   if (grid > p.ntiles) grid = p.ntiles;
-  fn<<<(unsigned)grid, 256, smem, s>>>(p);
+  fn<<<(unsigned)grid, (unsigned)threads, smem, s>>>(p);
   return check_launch("resample_poly");
 }
 
 template <typename T, bool XC, bool HC, int PAD>
-inline int dispatch_rq_pad(RsParams &p, int rq, size_t smem, cudaStream_t s) {
-  if (rq == 1) return launch_rowtile<T, XC, HC, 1, PAD>(p, smem, s);
+inline int dispatch_rq_pad(RsParams &p, int rq, size_t smem, cudaStream_t s, int threads) {
+  if (rq == 1) return launch_rowtile<T, XC, HC, 1, PAD>(p, smem, s, threads);
   if constexpr (sizeof(T) == 4) {
-    if (rq == 2) return launch_rowtile<T, XC, HC, 2, PAD>(p, smem, s);
-    return launch_rowtile<T, XC, HC, 4, PAD>(p, smem, s);
+    if (rq == 2) return launch_rowtile<T, XC, HC, 2, PAD>(p, smem, s, threads);
+    return launch_rowtile<T, XC, HC, 4, PAD>(p, smem, s, threads);
   }
-  return launch_rowtile<T, XC, HC, 1, PAD>(p, smem, s);
+  return launch_rowtile<T, XC, HC, 1, PAD>(p, smem, s, threads);
 }
 
 // pad: 0 (odd row stride) or the pad shift 4, 5, 6 of the window layout
 template <typename T, bool XC, bool HC>
-inline int dispatch_rq(RsParams &p, int rq, int pad, size_t smem, cudaStream_t s) {
-  if (pad == 0) return dispatch_rq_pad<T, XC, HC, 0>(p, rq, smem, s);
+inline int dispatch_rq(RsParams &p, int rq, int pad, size_t smem, cudaStream_t s, int threads) {
+  if (pad == 0) return dispatch_rq_pad<T, XC, HC, 0>(p, rq, smem, s, threads);
   if constexpr (std::is_same<T, float>::value && XC && !HC) {
-    if (pad == 5) return dispatch_rq_pad<T, XC, HC, 5>(p, rq, smem, s);
-    if (pad == 6) return dispatch_rq_pad<T, XC, HC, 6>(p, rq, smem, s);
+    if (pad == 5) return dispatch_rq_pad<T, XC, HC, 5>(p, rq, smem, s, threads);
+    if (pad == 6) return dispatch_rq_pad<T, XC, HC, 6>(p, rq, smem, s, threads);
   }
-  return dispatch_rq_pad<T, XC, HC, 4>(p, rq, smem, s);
+  return dispatch_rq_pad<T, XC, HC, 4>(p, rq, smem, s, threads);
 }
 
 // Tile shape knobs: rq rows per thread (1, 2, 4), wc column warps (1..8), G row
@@ -606,7 +608,11 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
     // the largest power of two <= 8 that divides the super-group count (balanced warps)
     while (wc < 8 && nsg % (wc * 2) == 0) wc *= 2;
   }
-  if (wc > nsg) wc = 1;
+  if (wc > nsg || wc < 1 || wc > 16 || (wc <= 8 && 8 % wc != 0)) wc = 1;
+  // row slices per CTA: 8/wc for 1, 2, 4, 8 column warps, one slice (one row per thread)
+  // for 9..16, so the CTA has 8 warps or wc of them
+  const int wr = wc <= 8 ? 8 / wc : 1;
+  const int threads = 32 * wc * wr;
   // even row strides need a padded window (coarser pads for strides of 32 or 64 samples,
   // complex float signals with real taps)
   int pad = (geo.S % 2) ? 0 : 4;
@@ -617,13 +623,13 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
     return pad ? win + (win >> pad) + 1 : (win + 3 * G16 - 1) / G16 * G16;
   };
   auto smem_for = [&](int rq, int nbuf) -> size_t {
-    const int64_t QC = 32LL * rq * (8 / wc);
+    const int64_t QC = 32LL * rq * wr;
     const int64_t win = (QC - 1) * geo.S + (geo.kmax - geo.kmin) + 1;
     const int64_t alloc = window_alloc(win);
     return tap_table_bytes<T, XC, HC>(geo.ncg, geo.span) + (size_t)nbuf * (size_t)alloc * sizeof(XT);
   };
   int rq = tc.rq > 0 ? tc.rq : 2;
-  if (sizeof(T) == 8) rq = 1;
+  if (sizeof(T) == 8 || threads > 256) rq = 1;
   int nbuf = tc.nbuf > 0 ? tc.nbuf : 2;
   // two CTAs per SM: prefer double buffering, then fewer rows, then a single buffer
   while (smem_for(rq, nbuf) > 110 * 1024 && (rq > 1 || nbuf > 1)) {
@@ -656,14 +662,14 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
     p.span = geo.span;
     p.kmin = geo.kmin;
     p.rows = geo.rows;
-    p.QC = 32 * rq * (8 / wc);
+    p.QC = 32 * rq * wr;
     p.WC = wc;
     p.tiles_per_row = (geo.rows + p.QC - 1) / p.QC;
     p.ntiles = p.tiles_per_row * batch;
     const int64_t win = (int64_t)(p.QC - 1) * geo.S + (geo.kmax - geo.kmin) + 1;
     p.win = (int32_t)win;
     p.win_alloc = (int32_t)window_alloc(win);
-    return dispatch_rq<T, XC, HC>(p, rq, pad, smem, s);
+    return dispatch_rq<T, XC, HC>(p, rq, pad, smem, s, threads);
   }
   // row tile too large for shared memory: direct form
   const size_t hbytes = (size_t)L * sizeof(HT);
