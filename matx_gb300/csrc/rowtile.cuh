@@ -80,12 +80,14 @@ __host__ __device__ inline size_t tap_table_bytes(int64_t ncg, int64_t span) {
   return taps + (((size_t)ncg * 4 + 15) & ~(size_t)15);
 }
 
-// Padded window layout: one pad element after every 2^PAD elements (PAD = 0: none).  A
-// row stride S that is a multiple of 16, 32 or 64 samples reads conflict-free with PAD =
-// 4, 5 or 6 respectively (lanes read rows q*S + k).
+// Window layouts against bank conflicts of the row-strided reads (lanes read rows q*S + k):
+// PAD = 4, 5, 6 put one pad element after every 2^PAD elements (conflict-free for S a
+// multiple of 8, 32, 64); PAD = 1 permutes the low 3 bits of the index by bits 4-6 within
+// each block of 16 (conflict-free for S = 4 mod 8); PAD = 0 is the plain layout.
 template <int PAD>
 __device__ __forceinline__ int smem_idx(int p) {
-  if constexpr (PAD > 0) return p + (p >> PAD);
+  if constexpr (PAD == 1) return p ^ ((p >> 4) & 7);
+  else if constexpr (PAD > 0) return p + (p >> PAD);
   else return p;
 }
 
@@ -575,6 +577,7 @@ template <typename T, bool XC, bool HC>
 inline int dispatch_rq(RsParams &p, int rq, int pad, size_t smem, cudaStream_t s, int threads) {
   if (pad == 0) return dispatch_rq_pad<T, XC, HC, 0>(p, rq, smem, s, threads);
   if constexpr (std::is_same<T, float>::value && XC && !HC) {
+    if (pad == 1) return dispatch_rq_pad<T, XC, HC, 1>(p, rq, smem, s, threads);
     if (pad == 5) return dispatch_rq_pad<T, XC, HC, 5>(p, rq, smem, s, threads);
     if (pad == 6) return dispatch_rq_pad<T, XC, HC, 6>(p, rq, smem, s, threads);
   }
@@ -616,10 +619,12 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
   // even row strides need a padded window (coarser pads for strides of 32 or 64 samples,
   // complex float signals with real taps)
   int pad = (geo.S % 2) ? 0 : 4;
-  if (pad && std::is_same<T, float>::value && XC && !HC) pad = geo.S % 64 == 0 ? 6 : geo.S % 32 == 0 ? 5 : 4;
+  if (pad && std::is_same<T, float>::value && XC && !HC)
+    pad = geo.S % 64 == 0 ? 6 : geo.S % 32 == 0 ? 5 : geo.S % 8 == 0 ? 4 : geo.S % 4 == 0 ? 1 : 4;
   // window buffer: padded layout for even S; for odd S room for the 16-byte-aligned bulk copy
   constexpr int64_t G16 = 16 / (int64_t)sizeof(XT);
   auto window_alloc = [&](int64_t win) -> int64_t {
+    if (pad == 1) return (win + 15) / 16 * 16;  // the permutation stays inside blocks of 16
     return pad ? win + (win >> pad) + 1 : (win + 3 * G16 - 1) / G16 * G16;
   };
   auto smem_for = [&](int rq, int nbuf) -> size_t {
