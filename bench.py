@@ -351,9 +351,10 @@ def run_channelize(args, rank, world, dev):
 
 
 def run_fwdbwd(args, rank, world, dev):
-    """Differentiable resample_poly fp32: 256 rows x 16384 samples uniform[-1,1], a
-    learnable 127-tap filter N(0, 1/127), (up, down) = (3, 2) and (1, 1), loss = MSE
-    against the output of a fixed seeded Kaiser filter; one step = forward + backward."""
+    """Differentiable FIR fp32: 256 rows x 16384 samples uniform[-1,1], a learnable 127-tap
+    filter N(0, 1/127), loss = MSE against the output of a fixed seeded Kaiser filter; one
+    step = forward + backward.  (3, 2) runs resample_poly; the (1, 1) case runs conv1d SAME,
+    since resample_poly at up == down is MatX's identity copy with a zero tap gradient."""
     import torch
     from scipy import signal
     import matx_gb300 as mx
@@ -370,13 +371,14 @@ def run_fwdbwd(args, rank, world, dev):
         h = (torch.randn(L, device=dev, generator=g) / L ** 0.5).requires_grad_(True)
         href = torch.from_numpy(signal.firwin(L, 1.0 / max(up, down, 2), window=("kaiser", 5.0))
                                 .astype(np.float32)).to(dev)
+        conv = (up, down) == (1, 1)
         with torch.no_grad():
-            target = mx.resample_poly(x.detach(), href, up, down)
+            target = mx.conv1d(x.detach(), href, "same") if conv else mx.resample_poly(x.detach(), href, up, down)
 
         def step():
             x.grad = None
             h.grad = None
-            y = ag.resample_poly(x, h, up, down)
+            y = ag.conv1d(x, h, "same") if conv else ag.resample_poly(x, h, up, down)
             loss = torch.mean((y - target) ** 2)
             loss.backward()
         for _ in range(args.warmup):
@@ -384,10 +386,13 @@ def run_fwdbwd(args, rank, world, dev):
         l0 = mx.launch_count()
         ms = _timed(step, steps, lambda: _flush_l2(flushbuf), stream)
         launches = mx.launch_count() - l0
-        fmacs = mac_count(N, L, up, down) * B if (up, down) != (1, 1) else 0
-        macs = 3 * fmacs                       # forward, dL/dx (transposed resampler), dL/dh
-        res[f"{up}/{down}"] = {"ms": ms, "gmacs": (macs / (ms * 1e-3) / 1e9) if macs else None,
-                               "fwd_macs": fmacs, "library_launches_per_step": launches / steps}
+        # conv1d SAME: every output uses the taps that overlap the signal
+        fmacs = (sum(min(L, n + L // 2 + 1, N - n + L // 2) for n in range(N)) * B if conv
+                 else mac_count(N, L, up, down) * B)
+        macs = 3 * fmacs                       # forward, dL/dx (transposed pass), dL/dh
+        key = "conv1d_same" if conv else f"{up}/{down}"
+        res[key] = {"ms": ms, "gmacs": macs / (ms * 1e-3) / 1e9, "fwd_macs": fmacs,
+                    "library_launches_per_step": launches / steps}
         total_macs += macs
         total_ms += ms
         if (up, down) == (3, 2):
@@ -413,8 +418,8 @@ def run_fwdbwd(args, rank, world, dev):
             "value": total_macs / (total_ms * 1e-3) / 1e9, "unit": "GMAC/s", "n_gpus": world, "steps": steps,
             "warmup": args.warmup, "ms_per_step": total_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform[-1,1]; N(0,1/127) taps)",
-            "config": {"workload": "differentiable resample_poly 256x16384 f32, 127 taps, (3,2) and (1,1); "
-                                   "MSE loss, torch.autograd through the hand-written adjoint",
+            "config": {"workload": "differentiable FIR 256x16384 f32, 127 taps: resample_poly (3,2) and "
+                                   "conv1d SAME; MSE loss, torch.autograd through the hand-written adjoints",
                        "l2": "flushed (256 MB write) before every timed step"},
             "per_ratio": res}
     if rank == 0:

@@ -22,6 +22,9 @@
 // holds every part of one tile); warps 8-11 (one per TMEM lane quarter, lane = output
 // phase) store the tile's outputs as whole (complex) values.  Every wait on an mbarrier is bounded; a wait that gives up sets the kernel's
 // status word.
+#include <cstdio>
+#include <cstdlib>
+
 #include "common.cuh"
 #include "tc.cuh"
 #include "tc_wide.h"
@@ -266,7 +269,8 @@ __global__ void __launch_bounds__(kTwThreads, 1) tc_wide_kernel(const TwParams p
   } else if (warp == 0) {
     // ================= MMA issuer =================
     // every TMEM column the MMAs touch lies inside the allocation (checked once)
-    const bool geom_ok = p.NR % 16 == 0 && p.Kp % 32 == 0 && p.wcol0 >= 2 * NPARTS * p.NR &&
+    const bool geom_ok = p.NR % 16 == 0 && p.Kp % 32 == 0 && (p.nsets == 1 || p.nsets == 2) &&
+                         p.wcol0 >= p.nsets * NPARTS * p.NR &&
                          p.wcol0 + p.terms * (p.Kp / 2) <= p.tmem_cols && (p.terms == 1 || p.terms == 3);
     if (lane == 0 && !geom_ok) s_fail = 1;
     if (lane == 0 && geom_ok) {
@@ -279,11 +283,12 @@ __global__ void __launch_bounds__(kTwThreads, 1) tc_wide_kernel(const TwParams p
       for (int64_t s = 0; s < nstages; ++s) {
         const int64_t i = s / NPARTS;
         const int part = (int)(s - i * NPARTS);
-        const int slot = (int)(s & 1), tset = (int)(i & 1);
+        const int slot = (int)(s & 1), tset = (int)(i % p.nsets);
         if (!tc::mbar_wait(&op_full[slot], (uint32_t)((s >> 1) & 1))) { s_fail = 1; break; }
         // accumulator set tset holds every part of tile i; it is free once the epilogue has
-        // drained tile i - 2
-        if (part == 0 && i >= 2 && !tc::mbar_wait(&tm_empty[tset], (uint32_t)(((i - 2) >> 1) & 1))) {
+        // drained tile i - nsets
+        if (part == 0 && i >= p.nsets &&
+            !tc::mbar_wait(&tm_empty[tset], (uint32_t)(((i - p.nsets) / p.nsets) & 1))) {
           s_fail = 1;
           break;
         }
@@ -310,8 +315,8 @@ __global__ void __launch_bounds__(kTwThreads, 1) tc_wide_kernel(const TwParams p
     const int j = 32 * quarter + lane;
     const uint32_t lane_base = (uint32_t)(32 * quarter) << 16;
     for (int64_t i = 0; i < my_tiles; ++i) {
-      const int tset = (int)(i & 1);
-      if (quarter == 0 && lane == 0) s_eok = tc::mbar_wait(&tm_full[tset], (uint32_t)((i >> 1) & 1)) ? 1 : 0;
+      const int tset = (int)(i % p.nsets);
+      if (quarter == 0 && lane == 0) s_eok = tc::mbar_wait(&tm_full[tset], (uint32_t)((i / p.nsets) & 1)) ? 1 : 0;
       tw_named_sync(2, 128);
       if (!s_eok) {
         s_fail = 1;
@@ -388,30 +393,53 @@ TwPlan plan_tc_wide(int64_t up, int64_t down, int64_t Lo, int64_t c, int even, i
   const int ES = xc ? 8 : 4, G = 16 / ES;
   const size_t kMaxSmem = 225 * 1024;
   const int nparts = xc ? 2 : 1;
-  for (int nraw : {2, 1}) {
-    for (int NR : {128, 112, 96, 80, 64}) {
-      const int64_t win = 64LL * (NR - 1) + p.Kp;
-      const size_t xarr = ((size_t)win * 2 + 1023) / 1024 * 1024;
-      const int64_t raw_elems = (win + 3 * G - 1) / G * G;
-      const size_t smem = 1024 + (size_t)2 * p.terms * xarr + (size_t)nraw * raw_elems * ES;
-      const int wcols = p.terms * p.Kp / 2;
-      if (smem > kMaxSmem || 2 * nparts * NR + wcols > 512) continue;
-      p.NR = NR;
-      p.nraw = nraw;
-      p.win = (int32_t)win;
-      p.xarr = (int32_t)xarr;
-      p.raw_elems = (int32_t)raw_elems;
-      p.wcol0 = 2 * nparts * NR;
-      uint32_t cols = 32;
-      while (cols < (uint32_t)(p.wcol0 + wcols)) cols <<= 1;
-      p.tmem_cols = (int32_t)cols;
-      p.rows = (out_len + p.Nt - 1) / p.Nt;
-      p.tiles_per_row = (p.rows + NR - 1) / NR;
-      p.ntiles = p.tiles_per_row * batch;
-      pl.smem = smem;
-      pl.ok = true;
-      return pl;
+  // Candidates: two TMEM accumulator sets (the epilogue of one tile overlaps the MMAs of the
+  // next) or one set with more rows per MMA; a single set counts 0.8 of its rows, the
+  // measured cost of the serialised epilogue.  Two raw slots before one.
+  // GBFIR_TC_WIDE_SHAPE="sets,raw,rows" restricts the candidates to one shape (for tuning)
+  int want[3] = {0, 0, 0};
+  if (const char* env = getenv("GBFIR_TC_WIDE_SHAPE"))
+    if (sscanf(env, "%d,%d,%d", &want[0], &want[1], &want[2]) != 3) want[0] = want[1] = want[2] = 0;
+  int best_score = 0;
+  TwParams best{};
+  size_t best_smem = 0;
+  for (int nsets : {2, 1}) {
+    for (int nraw : {2, 1}) {
+      for (int NR : {128, 112, 96, 80, 64}) {
+        const int64_t win = 64LL * (NR - 1) + p.Kp;
+        const size_t xarr = ((size_t)win * 2 + 1023) / 1024 * 1024;
+        const int64_t raw_elems = (win + 3 * G - 1) / G * G;
+        const size_t smem = 1024 + (size_t)2 * p.terms * xarr + (size_t)nraw * raw_elems * ES;
+        const int wcols = p.terms * p.Kp / 2;
+        if (smem > kMaxSmem || nsets * nparts * NR + wcols > 512) continue;
+        if (want[0] && (nsets != want[0] || nraw != want[1] || NR != want[2])) continue;
+        const int score = (nsets == 2 ? 10 * NR : 8 * NR) + (nraw == 2 ? 1 : 0);
+        if (score <= best_score) continue;
+        TwParams q = p;
+        q.NR = NR;
+        q.nraw = nraw;
+        q.nsets = nsets;
+        q.win = (int32_t)win;
+        q.xarr = (int32_t)xarr;
+        q.raw_elems = (int32_t)raw_elems;
+        q.wcol0 = nsets * nparts * NR;
+        uint32_t cols = 32;
+        while (cols < (uint32_t)(q.wcol0 + wcols)) cols <<= 1;
+        q.tmem_cols = (int32_t)cols;
+        q.rows = (out_len + q.Nt - 1) / q.Nt;
+        q.tiles_per_row = (q.rows + NR - 1) / NR;
+        q.ntiles = q.tiles_per_row * batch;
+        best = q;
+        best_smem = smem;
+        best_score = score;
+      }
     }
+  }
+  if (best_score > 0) {
+    p = best;
+    pl.smem = best_smem;
+    pl.ok = true;
+    return pl;
   }
   snprintf(pl.why, sizeof(pl.why), "a band of %d taps does not fit next to the accumulators", p.Kp);
   return pl;

@@ -15,12 +15,13 @@ struct TwParams {
   int64_t out_bstride, out_len;
   int64_t up, down;
   int32_t Nt;         // outputs per row = 64*up/down (<= 128)
-  int32_t NR;         // rows per tile = MMA N (64, 96 or 128)
+  int32_t NR;         // rows per tile = MMA N (64..128)
   int32_t Kp;         // K band, multiple of 32
   int64_t k0;         // band start relative to 64*q
   int32_t terms;      // 1 or 3
   int32_t fp16;       // 1: fp16 operands (one term), 0: bf16
   int32_t nraw;       // raw window slots (1 or 2)
+  int32_t nsets;      // TMEM accumulator sets (1 or 2), each holding every part of one tile
   int32_t win;        // elements of xs per tile = 64*(NR-1) + Kp
   int32_t raw_elems;  // elements per raw slot
   int32_t xarr;       // bytes per swizzled term array (multiple of 1024)
