@@ -532,7 +532,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="use the built-in tile heuristic")
     ap.add_argument("--tiles", default="",
                     help="fixed row tiles instead of tuning, e.g. '3/2=4,2,4,2;4/5=2,1,1,2' "
-                         "(rows_per_thread, col_warps, group, buffers; profiling cases)")
+                         "(rows_per_thread, col_warps, group, buffers [+4: TMA-store epilogue]; profiling cases)")
     ap.add_argument("--ratios", default="3/2,4/5,160/147", help="comma-separated up/down list (profiling cases)")
     ap.add_argument("--workload", default="resample",
                     choices=["resample", "ragged", "conv1d", "channelize", "fwdbwd"],
@@ -595,14 +595,15 @@ def main():
             u, d = (int(v) for v in r.split("/"))
             tile = tuple(int(v) for v in t.split(","))
             autotune.register(u, d, len(taps_np[RATIOS.index((u, d))]), tile)
-            tiles[r] = {"rows_per_thread": tile[0], "col_warps": tile[1], "group": tile[2], "buffers": tile[3],
-                        "fixed": True}
+            tiles[r] = {"rows_per_thread": tile[0], "col_warps": tile[1], "group": tile[2], "buffers": tile[3] & 3,
+                        "tma_store": bool(tile[3] & 4), "fixed": True}
     elif not args.no_tune and prec == "fp32":
         from matx_gb300 import autotune
         for (u, d), h, o in zip(RATIOS, taps, outs):
             r = autotune.tune_resample(x, h, u, d, out=o, use_cache=False)
             tiles[f"{u}/{d}"] = {"rows_per_thread": r.best[0], "col_warps": r.best[1], "group": r.best[2],
-                                 "buffers": r.best[3], "ms": r.best_ms, "heuristic_ms": r.default_ms}
+                                 "buffers": r.best[3] & 3, "tma_store": bool(r.best[3] & 4), "ms": r.best_ms,
+                                 "heuristic_ms": r.default_ms}
 
     for _ in range(args.warmup):
         step()

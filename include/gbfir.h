@@ -246,9 +246,12 @@ GBFIR_API int gbfir_ragged_resample(const gbfir_ragged_desc *device_descs, int64
 
 /* Override the tile shape the dispatcher picks for resample_poly (autotuner
  * hook; no MatX counterpart).  rows_per_thread in {1,2,4}, col_warps in
- * {1,2,4,8}, group (outputs per row = group*up) >= 1, buffers in {1,2}
- * (2 = prefetch the next input window while computing).  Zero for a field keeps
- * the built-in heuristic for it.  Process-wide setting, not thread-safe. */
+ * {1,2,4,8} (or 9..16 with one row per thread), group (outputs per row =
+ * group*up) >= 1, buffers in {1,2} (2 = prefetch the next input window while
+ * computing), plus 4 to write the outputs through shared memory and TMA tensor
+ * stores (complex float signals with real taps, rows of 2, 4 or >= 8 even
+ * outputs; other cases store directly).  Zero for a field keeps the built-in
+ * heuristic for it.  Process-wide setting, not thread-safe. */
 GBFIR_API int gbfir_set_resample_tile(int32_t rows_per_thread, int32_t col_warps,
                             int32_t group, int32_t buffers);
 

@@ -8,7 +8,10 @@ the fastest:
   col_warps       (phases per CTA = 8 * col_warps per pass)     1, 2, 4, 8; 9..16 dividing
                                                                 the super-groups (one row slice)
   group           (outputs per tile row = group * up)           multiples giving up*group % 4 == 0
-  buffers         (prefetch the next input window or not)       1, 2
+  buffers         (prefetch the next input window or not)       1, 2; plus 4 to send the
+                                                                outputs through shared memory
+                                                                and TMA tensor stores (complex
+                                                                float signal, real taps)
 
 The winner is registered in the library (gbfir_resample_tile_register), so every
 later call with the same reduced (up, down) and filter length uses it, and it is
@@ -47,8 +50,9 @@ def _key(x: torch.Tensor, h: torch.Tensor, up: int, down: int) -> str:
     return f"{name}|{x.dtype}|{h.dtype}|{up // g}/{down // g}|L{h.shape[-1]}|N{nbucket}|B{x.numel() // x.shape[-1]}"
 
 
-def candidates(up: int, down: int):
+def candidates(up: int, down: int, tma_store: bool = False):
     g = math.gcd(up, down)
+    nbufs = (1, 2, 5, 6) if tma_store else (1, 2)
     u = up // g
     g0 = 4 // math.gcd(u, 4)
     groups = sorted({g0 * m for m in (1, 2, 4, 8) if g0 * m <= 64})
@@ -58,7 +62,7 @@ def candidates(up: int, down: int):
                 nsg = (u * grp + 7) // 8
                 if wc > max(1, nsg):
                     continue
-                for nb in (1, 2):
+                for nb in nbufs:
                     yield (rq, wc, grp, nb)
     # one row slice of 9..16 column warps that divide the super-groups evenly (one row per
     # thread): balanced warps where 1, 2, 4 or 8 leave some with an extra super-group
@@ -66,7 +70,7 @@ def candidates(up: int, down: int):
         nsg = (u * grp + 7) // 8
         for wc in range(9, 17):
             if nsg % wc == 0:
-                for nb in (1, 2):
+                for nb in nbufs:
                     yield (1, wc, grp, nb)
 
 
@@ -126,7 +130,8 @@ def tune_resample(x: torch.Tensor, h: torch.Tensor, up: int, down: int, *, reps:
     default_ms = _time(run, reps)
     table = []
     try:
-        for tile in candidates(up, down):
+        tma_store = x.dtype == torch.complex64 and not h.is_complex()
+        for tile in candidates(up, down, tma_store):
             set_resample_tile(*tile)
             try:
                 ms = _time(run, reps)

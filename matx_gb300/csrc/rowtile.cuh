@@ -18,7 +18,10 @@
 // With rev = 1 the taps are read reversed (he[Lo-1-tp]); with up and down
 // swapped this computes the transposed resampler used by the adjoint.
 #pragma once
+#include <cuda.h>
+
 #include <algorithm>
+#include <cstring>
 
 #include "common.cuh"
 #include "tc.cuh"
@@ -56,6 +59,19 @@ struct RsParams {
   double scale;      // output scale (up for resample_poly)
   int32_t rev;       // read taps reversed
   int32_t nbuf;      // 2: prefetch the next tile's window while computing; 1: single buffer
+  int32_t ostore;    // 1: outputs leave through shared memory and TMA tensor stores
+  int32_t ost_rb;    // bytes of one row of a stored box (16, 32 or 64)
+  int32_t stg_off;   // byte offset of the store staging area in dynamic shared memory
+  int64_t rows_full; // rows holding Nt outputs (the tensor map's row count)
+};
+
+// Output staging of one warp for the TMA-store epilogue: two buffers of 32 rows x ost_rb
+// bytes, alternating; `n` counts the boxes this warp has stored.
+struct OutStage {
+  const void *map;  // CUtensorMap over (2*Nt floats, rows_full, batch)
+  unsigned char *buf;
+  int n;
+  int64_t b;
 };
 
 template <typename T, bool HC>
@@ -136,7 +152,7 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a
 template <int RQ, int PAD>
 __device__ __forceinline__ void rowtile_compute_c2(const RsParams &p, const float2 *cur,
                                                    const unsigned char *table_raw, float2 *orow, int64_t q0, int wr,
-                                                   int wc, int lane, float scale, int woff) {
+                                                   int wc, int lane, float scale, int woff, OutStage &os) {
   using TV = TapVec<float, false>;
   const TV *table = reinterpret_cast<const TV *>(table_raw);
   const int *goff = tap_goff(p, table_raw, sizeof(TV));
@@ -215,7 +231,35 @@ __device__ __forceinline__ void rowtile_compute_c2(const RsParams &p, const floa
       const int64_t left = p.out_len - n0;
       const int nv = left < ncol ? (left > 0 ? (int)left : 0) : ncol;
       float2 *dst = orow + n0;
-      if (nv == 8 && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0)) {
+      if (os.buf) {
+        // stage the warp's 32 rows x 8 phases (swizzled like the tensor map: 16-byte chunk
+        // u of row r at chunk u ^ f(r), conflict-free), then one lane stores the box; rows
+        // past rows_full are clipped by the map and the one partial row is stored here
+        unsigned char *buf = os.buf + (os.n & 1) * 2048;
+        if (lane == 0 && os.n >= 2) tc::bulk_wait_read<1>();
+        __syncwarp();
+        const int rb = p.ost_rb;
+        const int sw = rb == 64 ? ((lane >> 1) & 3) : rb == 32 ? ((lane >> 2) & 1) : 0;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          if (u * 16 < rb) {
+            const float2 lo = mul2(acc[i][2 * u], sc), hi = mul2(acc[i][2 * u + 1], sc);
+            *reinterpret_cast<float4 *>(buf + lane * rb + ((u ^ sw) << 4)) = make_float4(lo.x, lo.y, hi.x, hi.y);
+          }
+        }
+        tc::fence_async_smem();
+        __syncwarp();
+        if (lane == 0) {
+          tc::tma_store_3d(os.map, buf, 2 * j0, (int)(q0 + rbase - lane + 32 * i), (int)os.b);
+          tc::bulk_commit();
+        }
+        os.n++;
+        if (q0 + rbase + 32 * i == p.rows_full) {
+#pragma unroll
+          for (int jj = 0; jj < 8; jj++)
+            if (jj < nv) dst[jj] = mul2(acc[i][jj], sc);
+        }
+      } else if (nv == 8 && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0)) {
         float4 *d4 = reinterpret_cast<float4 *>(dst);
 #pragma unroll
         for (int u = 0; u < 4; u++) {
@@ -239,9 +283,9 @@ template <typename T, bool XC, bool HC, int RQ, int PAD>
 __device__ __forceinline__ void rowtile_compute(const RsParams &p, const typename val_of<T, XC>::type *cur,
                                                 const unsigned char *table_raw,
                                                 typename val_of<T, XC || HC>::type *orow, int64_t q0, int wr, int wc,
-                                                int lane, T scale, int woff) {
+                                                int lane, T scale, int woff, OutStage &os) {
   if constexpr (std::is_same<T, float>::value && XC && !HC) {
-    rowtile_compute_c2<RQ, PAD>(p, cur, table_raw, orow, q0, wr, wc, lane, scale, woff);
+    rowtile_compute_c2<RQ, PAD>(p, cur, table_raw, orow, q0, wr, wc, lane, scale, woff, os);
   } else {
     using XT = typename val_of<T, XC>::type;
     constexpr bool OC = XC || HC;
@@ -318,10 +362,21 @@ __device__ __forceinline__ void rowtile_compute(const RsParams &p, const typenam
   }
 }
 
+// Same, with every output stored directly (no staging).
+template <typename T, bool XC, bool HC, int RQ, int PAD>
+__device__ __forceinline__ void rowtile_compute(const RsParams &p, const typename val_of<T, XC>::type *cur,
+                                                const unsigned char *table_raw,
+                                                typename val_of<T, XC || HC>::type *orow, int64_t q0, int wr, int wc,
+                                                int lane, T scale, int woff) {
+  OutStage none{nullptr, nullptr, 0, 0};
+  rowtile_compute<T, XC, HC, RQ, PAD>(p, cur, table_raw, orow, q0, wr, wc, lane, scale, woff, none);
+}
+
 // 256 threads (8 warps) per CTA, or up to 512 (one row slice of 9..16 column warps) with one
 // row per thread.
 template <typename T, bool XC, bool HC, int RQ, int PAD>
-__global__ void __launch_bounds__(RQ == 1 ? 512 : 256) resample_rowtile(const RsParams p) {
+__global__ void __launch_bounds__(RQ == 1 ? 512 : 256)
+    resample_rowtile(const RsParams p, const __grid_constant__ CUtensorMap omap) {
   using XT = typename val_of<T, XC>::type;
   using HT = typename val_of<T, HC>::type;
   using OT = typename val_of<T, XC || HC>::type;
@@ -343,6 +398,16 @@ __global__ void __launch_bounds__(RQ == 1 ? 512 : 256) resample_rowtile(const Rs
   const int wr = wid / p.WC, wc = wid - wr * p.WC;
   const T scale = T(p.scale);
   const bool dbuf = p.nbuf == 2;
+  // TMA-store epilogue: each warp's two staging buffers, 1024-byte aligned (the swizzle
+  // pattern repeats every 512 bytes)
+  OutStage ostage{&omap, nullptr, 0, 0};
+  if constexpr (std::is_same<T, float>::value && XC && !HC) {
+    if (p.ostore) {
+      unsigned char *base = smem_raw + p.stg_off;
+      base += (1024 - (tc::smem_u32(base) & 1023)) & 1023;
+      ostage.buf = base + wid * 4096;
+    }
+  }
 
   if constexpr (PAD > 0) {
     // Even row stride: the window is stored with one pad element per 16 (bank-conflict
@@ -383,7 +448,8 @@ __global__ void __launch_bounds__(RQ == 1 ? 512 : 256) resample_rowtile(const Rs
       const int64_t b = tile / p.tiles_per_row;
       const int64_t q0 = (tile - b * p.tiles_per_row) * p.QC;
       OT *orow = op + b * p.out_bstride;
-      rowtile_compute<T, XC, HC, RQ, PAD>(p, cur, table, orow, q0, wr, wc, lane, scale, 0);
+      ostage.b = b;
+      rowtile_compute<T, XC, HC, RQ, PAD>(p, cur, table, orow, q0, wr, wc, lane, scale, 0, ostage);
       __syncthreads();
       if (!dbuf && next < p.ntiles) {
         issue_loads(next, xbuf0);
@@ -465,11 +531,32 @@ __global__ void __launch_bounds__(RQ == 1 ? 512 : 256) resample_rowtile(const Rs
       const int a = origin(tile, b, w0);
       const int64_t q0 = (tile - b * p.tiles_per_row) * p.QC;
       OT *orow = op + b * p.out_bstride;
-      rowtile_compute<T, XC, HC, RQ, PAD>(p, cur, table, orow, q0, wr, wc, lane, scale, a);
+      ostage.b = b;
+      rowtile_compute<T, XC, HC, RQ, PAD>(p, cur, table, orow, q0, wr, wc, lane, scale, a, ostage);
       __syncthreads();
       if (!dbuf && next < p.ntiles) issue_window(next, xbuf0, &s_bar[0]);
     }
   }
+  // the staged boxes are read and written before the CTA's shared memory goes away
+  if (ostage.buf && lane == 0) tc::bulk_wait_all();
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (the library does not
+// link the driver, so it loads where no GPU driver is installed); null if unavailable.
+using TensorMapEncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                       const cuuint64_t *, const cuuint32_t *, const cuuint32_t *,
+                                       CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                       CUtensorMapFloatOOBfill);
+inline TensorMapEncodeFn tensor_map_encoder() {
+  static TensorMapEncodeFn fn = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<TensorMapEncodeFn>(f);
+  }();
+  return fn;
 }
 
 // Host planning shared by the forward launch and the ragged planner.
@@ -549,7 +636,7 @@ __global__ void __launch_bounds__(256) resample_direct(const RsParams p, int h_i
 }
 
 template <typename T, bool XC, bool HC, int RQ, int PAD>
-inline int launch_rowtile(RsParams &p, size_t smem, cudaStream_t s, int threads) {
+inline int launch_rowtile(RsParams &p, const CUtensorMap &omap, size_t smem, cudaStream_t s, int threads) {
   auto fn = resample_rowtile<T, XC, HC, RQ, PAD>;
   int rc = ensure_smem((const void *)fn, smem, "resample_poly");
   if (rc) return rc;
@@ -558,36 +645,39 @@ inline int launch_rowtile(RsParams &p, size_t smem, cudaStream_t s, int threads)
   if (occ < 1) GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly: tile needs %zu B of shared memory", smem);
   int64_t grid = (int64_t)num_sms() * occ;
   if (grid > p.ntiles) grid = p.ntiles;
-  fn<<<(unsigned)grid, (unsigned)threads, smem, s>>>(p);
+  fn<<<(unsigned)grid, (unsigned)threads, smem, s>>>(p, omap);
   return check_launch("resample_poly");
 }
 
 template <typename T, bool XC, bool HC, int PAD>
-inline int dispatch_rq_pad(RsParams &p, int rq, size_t smem, cudaStream_t s, int threads) {
-  if (rq == 1) return launch_rowtile<T, XC, HC, 1, PAD>(p, smem, s, threads);
+inline int dispatch_rq_pad(RsParams &p, const CUtensorMap &m, int rq, size_t smem, cudaStream_t s, int threads) {
+  if (rq == 1) return launch_rowtile<T, XC, HC, 1, PAD>(p, m, smem, s, threads);
   if constexpr (sizeof(T) == 4) {
-    if (rq == 2) return launch_rowtile<T, XC, HC, 2, PAD>(p, smem, s, threads);
-    return launch_rowtile<T, XC, HC, 4, PAD>(p, smem, s, threads);
+    if (rq == 2) return launch_rowtile<T, XC, HC, 2, PAD>(p, m, smem, s, threads);
+    return launch_rowtile<T, XC, HC, 4, PAD>(p, m, smem, s, threads);
   }
-  return launch_rowtile<T, XC, HC, 1, PAD>(p, smem, s, threads);
+  return launch_rowtile<T, XC, HC, 1, PAD>(p, m, smem, s, threads);
 }
 
 // pad: 0 (odd row stride) or the pad shift 4, 5, 6 of the window layout
 template <typename T, bool XC, bool HC>
-inline int dispatch_rq(RsParams &p, int rq, int pad, size_t smem, cudaStream_t s, int threads) {
-  if (pad == 0) return dispatch_rq_pad<T, XC, HC, 0>(p, rq, smem, s, threads);
+inline int dispatch_rq(RsParams &p, const CUtensorMap &m, int rq, int pad, size_t smem, cudaStream_t s,
+                       int threads) {
+  if (pad == 0) return dispatch_rq_pad<T, XC, HC, 0>(p, m, rq, smem, s, threads);
   if constexpr (std::is_same<T, float>::value && XC && !HC) {
-    if (pad == 1) return dispatch_rq_pad<T, XC, HC, 1>(p, rq, smem, s, threads);
-    if (pad == 5) return dispatch_rq_pad<T, XC, HC, 5>(p, rq, smem, s, threads);
-    if (pad == 6) return dispatch_rq_pad<T, XC, HC, 6>(p, rq, smem, s, threads);
+    if (pad == 1) return dispatch_rq_pad<T, XC, HC, 1>(p, m, rq, smem, s, threads);
+    if (pad == 5) return dispatch_rq_pad<T, XC, HC, 5>(p, m, rq, smem, s, threads);
+    if (pad == 6) return dispatch_rq_pad<T, XC, HC, 6>(p, m, rq, smem, s, threads);
   }
-  return dispatch_rq_pad<T, XC, HC, 4>(p, rq, smem, s, threads);
+  return dispatch_rq_pad<T, XC, HC, 4>(p, m, rq, smem, s, threads);
 }
 
 // Tile shape knobs: rq rows per thread (1, 2, 4), wc column warps (1..8), G row
 // grouping.  Zero picks the built-in heuristic.
 struct TileChoice {
   int rq = 0, wc = 0, nbuf = 0;
+  int ostore = -1;  // 1: TMA-store epilogue where the output layout allows it, 0: direct
+                    // stores, -1: the epilogue for rows of 8 or more outputs
   int64_t group = 0;
 };
 
@@ -627,11 +717,19 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
     if (pad == 1) return (win + 15) / 16 * 16;  // the permutation stays inside blocks of 16
     return pad ? win + (win >> pad) + 1 : (win + 3 * G16 - 1) / G16 * G16;
   };
+  // TMA-store epilogue (complex float outputs): rows of an even Nt >= 8 (64-byte boxes), 4
+  // or 2 (32, 16), a 16-byte aligned output with an even batch stride, at least one whole row
+  const int64_t rows_full = out_len / geo.Nt;
+  int ost_rb = geo.Nt >= 8 ? 64 : geo.Nt == 4 ? 32 : geo.Nt == 2 ? 16 : 0;
+  const bool ostore = (tc.ostore == 1 || (tc.ostore < 0 && geo.Nt >= 8)) && std::is_same<T, float>::value && XC && !HC && geo.Nt % 2 == 0 &&
+                      ost_rb > 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0 &&
+                      (batch == 1 || out_bstride % 2 == 0) && rows_full >= 1;
+  const size_t stg_bytes = ostore ? 1024 + (size_t)(threads / 32) * 4096 : 0;
   auto smem_for = [&](int rq, int nbuf) -> size_t {
     const int64_t QC = 32LL * rq * wr;
     const int64_t win = (QC - 1) * geo.S + (geo.kmax - geo.kmin) + 1;
     const int64_t alloc = window_alloc(win);
-    return tap_table_bytes<T, XC, HC>(geo.ncg, geo.span) + (size_t)nbuf * (size_t)alloc * sizeof(XT);
+    return tap_table_bytes<T, XC, HC>(geo.ncg, geo.span) + (size_t)nbuf * (size_t)alloc * sizeof(XT) + stg_bytes;
   };
   int rq = tc.rq > 0 ? tc.rq : 2;
   if (sizeof(T) == 8 || threads > 256) rq = 1;
@@ -674,7 +772,29 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
     const int64_t win = (int64_t)(p.QC - 1) * geo.S + (geo.kmax - geo.kmin) + 1;
     p.win = (int32_t)win;
     p.win_alloc = (int32_t)window_alloc(win);
-    return dispatch_rq<T, XC, HC>(p, rq, pad, smem, s, threads);
+    CUtensorMap omap;
+    memset(&omap, 0, sizeof(omap));
+    if (ostore) {
+      // the output as (2*Nt floats, rows_full rows, batch); boxes of 32 rows x ost_rb bytes
+      const cuuint64_t dims[3] = {(cuuint64_t)(2 * geo.Nt), (cuuint64_t)rows_full, (cuuint64_t)batch};
+      const cuuint64_t strides[2] = {(cuuint64_t)(geo.Nt * 8),
+                                     (cuuint64_t)((batch > 1 ? out_bstride : rows_full * geo.Nt) * 8)};
+      const cuuint32_t box[3] = {(cuuint32_t)(ost_rb / 4), 32, 1}, es[3] = {1, 1, 1};
+      const CUtensorMapSwizzle sw = ost_rb == 64   ? CU_TENSOR_MAP_SWIZZLE_64B
+                                    : ost_rb == 32 ? CU_TENSOR_MAP_SWIZZLE_32B
+                                                   : CU_TENSOR_MAP_SWIZZLE_NONE;
+      const TensorMapEncodeFn enc = tensor_map_encoder();
+      const CUresult r = enc == nullptr ? CUDA_ERROR_NOT_SUPPORTED : enc(&omap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, out, dims, strides, box,
+                                                es, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+                                                CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r == CUDA_SUCCESS) {
+        p.ostore = 1;
+        p.ost_rb = ost_rb;
+        p.rows_full = rows_full;
+        p.stg_off = (int32_t)(smem - stg_bytes);
+      }
+    }
+    return dispatch_rq<T, XC, HC>(p, omap, rq, pad, smem, s, threads);
   }
   // row tile too large for shared memory: direct form
   const size_t hbytes = (size_t)L * sizeof(HT);

@@ -70,6 +70,24 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst_smem, const void *src_gm
                : "memory");
 }
 
+// TMA tensor store shared -> global of one 3-D box (coordinates in elements, innermost
+// first; the innermost times the element size a multiple of 16 bytes, none negative),
+// tracked by the issuing thread's bulk groups.
+__device__ __forceinline__ void tma_store_3d(const void *tmap, const void *src_smem, int x, int y, int z) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+                   reinterpret_cast<uint64_t>(tmap)),
+               "r"(smem_u32(src_smem)), "r"(x), "r"(y), "r"(z)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// at most N of this thread's bulk groups still reading shared memory
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
+// all of this thread's bulk groups complete
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 // ---- proxy / tcgen05 ordering fences ---------------------------------------------------
 // generic-proxy shared-memory writes -> visible to the tensor core (async proxy)
 __device__ __forceinline__ void fence_async_smem() {

@@ -222,6 +222,33 @@ def test_resample_tile_overrides_agree(mx, orc):
             mx.set_resample_tile(0, 0, 0, 0)
 
 
+@pytest.mark.parametrize("case", [
+    # (up, down, batch, N, tile): rows of Nt = 24, 4, 2, 160, 20 outputs, whole and partial last rows
+    (3, 2, 2, 20001, (4, 2, 8, 1)), (3, 2, 3, 20000, (2, 1, 8, 2)), (4, 5, 1, 20003, (2, 1, 1, 2)),
+    (4, 5, 2, 20000, (4, 1, 1, 1)), (1, 2, 2, 9999, (2, 2, 2, 2)), (160, 147, 2, 20000, (1, 10, 1, 1)),
+    (160, 147, 1, 20011, (1, 8, 1, 2)), (5, 4, 2, 20002, (2, 2, 0, 1)), (2, 1, 3, 7777, (4, 1, 0, 2)),
+])
+def test_resample_tma_store_epilogue(mx, orc, case):
+    """Buffers + 4 sends the outputs through shared memory and TMA tensor stores: the result
+    equals the direct stores bit for bit (same arithmetic) and the oracle within FP32_TOL;
+    rows past the last whole row and odd batch strides take the direct stores."""
+    import torch
+    up, down, B, N, (rq, wc, g, nb) = case
+    rng = np.random.default_rng(seed_of("tma_store", *case[:4]))
+    x = (rng.standard_normal((B, N)) + 1j * rng.standard_normal((B, N))).astype(np.complex64)
+    h = kaiser_filter(up, down).astype(np.float32)
+    try:
+        mx.set_resample_tile(rq, wc, g, nb)
+        y_direct = mx.resample_poly(dev(x), dev(h), up, down)
+        mx.set_resample_tile(rq, wc, g, nb | 4)
+        y_tma = mx.resample_poly(dev(x), dev(h), up, down)
+        torch.cuda.synchronize()
+    finally:
+        mx.set_resample_tile(0, 0, 0, 0)
+    assert torch.equal(y_tma, y_direct), case
+    assert rel_l2(host(y_tma), orc.resample_poly(x, h, up, down)) < FP32_TOL, case
+
+
 @pytest.mark.parametrize("updown", [(3, 2), (4, 5), (160, 147)])
 def test_resample_config_rows(mx, orc, updown):
     # C2 at full size: 64 x 2^20 complex Gaussian; sampled rows against the oracle,
