@@ -7,6 +7,7 @@
  * rules and error classes:
  *
  *   gbfir_conv1d           include/matx/transforms/conv.h:467-532 (conv1d_impl)
+ *   gbfir_conv1d_axis      include/matx/operators/conv.h:263-274 (conv1d with an axis)
  *                          include/matx/transforms/conv.h:402-451 (operand swap)
  *                          include/matx/transforms/conv.h:175-224 (direct CUDA path)
  *                          include/matx/transforms/corr.h:60-69   (corr = conv with reverse(conj(h)))
@@ -115,6 +116,20 @@ typedef struct gbfir_buf {
  *  returns GBFIR_ERR_NOT_SUPPORTED for other operands. */
 GBFIR_API int gbfir_conv1d(gbfir_buf out, gbfir_buf in, gbfir_buf h, int32_t mode,
                  int32_t is_corr, int32_t precision, gbfir_stream_t stream);
+
+/* conv1d / corr along a strided axis.  Signal (b, i), b < out.batch, i < inner, is
+ *  in[b*in.batch_stride + n*in_step + i], n < in.len (in.batch_stride 0 broadcasts one
+ *  block); its output is out[b*out.batch_stride + m*out_step + i], m < out.len.  A
+ *  contiguous [batch][len][inner] tensor has in_step = inner; a slice of a wider one a
+ *  larger step.  This is MatX's conv1d(a, h, {axis}, mode)
+ *  (include/matx/operators/conv.h:263-274) and the permuted-view conv1d of the radar
+ *  three-pulse canceller (examples/simple_radar_pipeline.h:321-327) without
+ *  materialising the permutation.  Output lengths, the SAME start and corr as
+ *  gbfir_conv1d; h is one row; out_step >= inner.  FP32 / FP64 only (other precisions:
+ *  GBFIR_ERR_NOT_SUPPORTED). */
+GBFIR_API int gbfir_conv1d_axis(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t inner,
+                                int64_t in_step, int64_t out_step, int32_t mode,
+                                int32_t is_corr, int32_t precision, gbfir_stream_t stream);
 
 /* Polyphase resampler: out[b] = up * (upsample-by-up, filter with h,
  * downsample-by-down)(in[b]), with the scipy centring of

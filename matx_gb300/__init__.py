@@ -111,8 +111,71 @@ def set_resample_tile(rows_per_thread: int = 0, col_warps: int = 0, group: int =
     _lib.check(_lib.load().gbfir_set_resample_tile(rows_per_thread, col_warps, group, buffers))
 
 
+def _olen(m: int, N: int, L: int) -> int:
+    if m == 0:
+        return N + L - 1
+    if m == 1:
+        return max(N, L)
+    return max(N, L) - min(N, L) + 1
+
+
+def _axis_layout(t: torch.Tensor, a: int):
+    """Signals of t along dimension a as base + o*ostride + n*step + i: returns
+    (inner_dim, inner, step, outer_dims, outer, ostride), or None when the other
+    dimensions do not fold into one unit-stride inner index and one outer index."""
+    dims = [d for d in range(t.dim()) if d != a and t.shape[d] > 1]
+    unit = [d for d in dims if t.stride(d) == 1]
+    d_in = unit[-1] if unit else None
+    rest = sorted((d for d in dims if d != d_in), key=lambda d: -t.stride(d))
+    for u, v in zip(rest, rest[1:]):
+        if t.stride(u) != t.stride(v) * t.shape[v]:
+            return None
+    inner = t.shape[d_in] if d_in is not None else 1
+    outer = math.prod(t.shape[d] for d in rest)
+    return d_in, inner, t.stride(a), rest, outer, (t.stride(rest[-1]) if rest else 0)
+
+
+def _empty_like_order(t: torch.Tensor, shape, dtype) -> torch.Tensor:
+    """A fresh tensor of `shape` whose dimensions are laid out in t's stride order."""
+    order = sorted(range(t.dim()), key=lambda d: (-t.stride(d), d))
+    base = torch.empty([shape[d] for d in order], dtype=dtype, device=t.device)
+    return base.permute([order.index(d) for d in range(t.dim())])
+
+
+def _conv1d_axis(x, h, m, a, out, corr):
+    """conv1d of a 1-D filter along dimension a of x in place of its layout
+    (gbfir_conv1d_axis): no transpose is materialised when the other dimensions fold into
+    one unit-stride inner index and one outer index."""
+    lib = _lib.load()
+    double = _out_dtype(x, h) in (torch.float64, torch.complex128)
+    x = _rows(_cast(x, double), "conv1d x")
+    h = _prep_in(_cast(h, double), "conv1d h")
+    if h.dim() != 1:
+        raise GbfirError(2, "conv1d (axis): the filter must be 1-D")
+    lx = _axis_layout(x, a)
+    if lx is None:
+        x = x.contiguous()  # MatX's shim materialises such views the same way
+        lx = _axis_layout(x, a)
+    N, L = x.shape[a], h.shape[0]
+    oshape = list(x.shape)
+    oshape[a] = _olen(m, N, L)
+    odt = _out_dtype(x, h)
+    if out is None:
+        out = _empty_like_order(x, oshape, odt)
+    elif list(out.shape) != oshape or out.dtype != odt or not out.is_cuda:
+        raise ValueError(f"conv1d (axis): out must be a {odt} CUDA tensor of shape {oshape}")
+    lo = _axis_layout(out, a)
+    if lo is None or lo[0] != lx[0] or lo[3] != lx[3] or (lo[0] is not None and lo[2] < lo[1]):
+        raise ValueError("conv1d (axis): out must have the layout of the input along the other dimensions")
+    d_in, inner, sx, _, outer, ox = lx
+    bx = _lib.Buf(x.data_ptr(), outer, N, ox, _DT[x.dtype])
+    bo = _lib.Buf(out.data_ptr(), outer, oshape[a], lo[5], _DT[out.dtype])
+    _lib.check(lib.gbfir_conv1d_axis(bo, bx, _buf(h, "conv1d h"), inner, sx, lo[2], m, int(corr), 0, _stream()))
+    return out
+
+
 def conv1d(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torch.Tensor | None = None,
-           precision="fp32", _corr: bool = False) -> torch.Tensor:
+           precision="fp32", axis: int = -1, _corr: bool = False) -> torch.Tensor:
     """Direct 1-D convolution (MatX conv1d with MATX_C_METHOD_DIRECT).
 
     Output length: N+L-1 (FULL), max(N,L) (SAME), max(N,L)-min(N,L)+1 (VALID).
@@ -120,9 +183,21 @@ def conv1d(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torc
     broadcast across the other's batch (conv.h:467-532).  ``precision`` "bf16",
     "fp16" or "bf16x3" runs the Toeplitz MMA form on the tensor cores (a real
     float32 filter shared by all rows, signal at least as long as the filter).
+    ``axis`` convolves another dimension with a 1-D filter (MatX's
+    conv1d(a, b, {axis}, mode), operators/conv.h:263-274); so does a last dimension that
+    is a transposed view of a contiguous tensor (the radar three-pulse canceller's
+    permuted view, examples/simple_radar_pipeline.h:321-327): the data is not moved, and
+    the result is the same kind of view.
     """
-    lib = _lib.load()
     m = _mode(mode)
+    nd = max(x.dim(), 1)
+    if x.dim() > 1 and h.dim() == 1 and x.is_cuda and _prec(precision) == 0:
+        a = axis % nd
+        if a != nd - 1 or x.stride(-1) != 1:
+            return _conv1d_axis(x, h, m, a, out, _corr)
+    elif axis % nd != nd - 1:
+        raise GbfirError(2, "conv1d: an axis other than the last needs a 1-D filter and FP32")
+    lib = _lib.load()
     double = _out_dtype(x, h) in (torch.float64, torch.complex128)
     x = _prep_in(_cast(x, double), "conv1d x")
     h = _prep_in(_cast(h, double), "conv1d h")
@@ -145,9 +220,9 @@ def conv1d(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torc
 
 
 def corr(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torch.Tensor | None = None,
-         precision="fp32"):
+         precision="fp32", axis: int = -1):
     """Direct correlation: corr(x, h) = conv1d(x, reverse(conj(h))) (corr.h:67)."""
-    return conv1d(x, h, mode, out=out, precision=precision, _corr=True)
+    return conv1d(x, h, mode, out=out, precision=precision, axis=axis, _corr=True)
 
 
 def resample_out_len(n: int, up: int, down: int) -> int:

@@ -55,7 +55,8 @@ def candidates(up: int, down: int, tma_store: bool = False):
     nbufs = (1, 2, 5, 6) if tma_store else (1, 2)
     u = up // g
     g0 = 4 // math.gcd(u, 4)
-    groups = sorted({g0 * m for m in (1, 2, 4, 8) if g0 * m <= 64})
+    # odd multiples too: they keep an odd row stride (TMA window copies) for odd down
+    groups = sorted({g0 * m for m in (1, 2, 3, 4, 5, 7, 8) if g0 * m <= 64})
     for rq in (1, 2, 4):
         for wc in (1, 2, 4, 8):
             for grp in groups:

@@ -15,6 +15,8 @@
 namespace gbfir {
 
 int conv1d_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int mode, int is_corr, cudaStream_t s);
+int conv1d_axis_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t inner, int64_t in_step,
+                   int64_t out_step, int mode, int is_corr, cudaStream_t s);
 int resample_poly_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t up, int64_t down,
                      cudaStream_t s);
 int channelize_poly_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t M, int64_t D,
@@ -148,6 +150,52 @@ int gbfir_conv1d(gbfir_buf out, gbfir_buf in, gbfir_buf h, int32_t mode, int32_t
     return conv1d_fp(out, in, h, mode, is_corr != 0, reinterpret_cast<cudaStream_t>(stream));
   } catch (...) {
     GBFIR_FAIL(GBFIR_ERR_CUDA, "conv1d: internal exception");
+  }
+}
+
+int gbfir_conv1d_axis(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t inner, int64_t in_step, int64_t out_step,
+                      int32_t mode, int32_t is_corr, int32_t precision, gbfir_stream_t stream) {
+  try {
+    GBFIR_TRY(check_buf(h, "conv1d (axis) h", false));
+    if (out.ptr == nullptr || in.ptr == nullptr) GBFIR_FAIL(GBFIR_ERR_NULL_POINTER, "conv1d (axis): null pointer");
+    if (out.batch < 1 || in.batch < 1) GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "conv1d (axis): batch must be >= 1");
+    if (out.len < 1 || in.len < 1) GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "conv1d (axis): lengths must be >= 1");
+    if (dtype_size(out.dtype) == 0 || dtype_size(in.dtype) == 0)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_TYPE, "conv1d (axis): unknown dtype");
+    GBFIR_TRY(check_types(out, in, h, "conv1d (axis)", false));
+    GBFIR_TRY(check_precision(precision, "conv1d (axis)"));
+    if (precision != GBFIR_PREC_FP32)
+      GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "conv1d (axis): only the FP32/FP64 form is built");
+    if (mode < GBFIR_MODE_FULL || mode > GBFIR_MODE_VALID)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "conv1d (axis): unknown mode %d", (int)mode);
+    if (inner < 1) GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "conv1d (axis): inner count must be >= 1");
+    if (in_step < 1 || out_step < 1)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "conv1d (axis): sample steps must be >= 1");
+    if (h.batch != 1) GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "conv1d (axis): the filter must be one row");
+    if (in.batch != 1 && in.batch != out.batch)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "conv1d (axis): batch sizes do not match (out %lld, in %lld)",
+                 (long long)out.batch, (long long)in.batch);
+    // output signals must not overlap: inner positions within one step, blocks apart
+    if (inner > 1 && out.len > 1 && out_step < inner)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "conv1d (axis): output step %lld below the inner count %lld",
+                 (long long)out_step, (long long)inner);
+    if (out.batch > 1 && out.batch_stride < (out.len - 1) * out_step + inner)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "conv1d (axis): output batch stride shorter than a block");
+    if (in.batch > 1 && in.batch_stride < 0)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "conv1d (axis): negative input batch stride");
+    const size_t ia = in.dtype == GBFIR_C128 ? 16 : dtype_size(in.dtype);
+    const size_t oa = out.dtype == GBFIR_C128 ? 16 : dtype_size(out.dtype);
+    if (reinterpret_cast<uintptr_t>(in.ptr) % ia || reinterpret_cast<uintptr_t>(out.ptr) % oa)
+      GBFIR_FAIL(GBFIR_ERR_ALIGNMENT, "conv1d (axis): pointer not aligned to its element type");
+    const int64_t mx = std::max(in.len, h.len), mn = std::min(in.len, h.len);
+    const int64_t want = mode == GBFIR_MODE_FULL ? in.len + h.len - 1 : mode == GBFIR_MODE_SAME ? mx : mx - mn + 1;
+    if (out.len != want)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "conv1d (axis): output length %lld, expected %lld", (long long)out.len,
+                 (long long)want);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return conv1d_axis_fp(out, in, h, inner, in_step, out_step, mode, is_corr != 0, s);
+  } catch (...) {
+    GBFIR_FAIL(GBFIR_ERR_CUDA, "conv1d (axis): internal exception");
   }
 }
 

@@ -95,6 +95,25 @@ def test_conv_validation(lib):
     assert lib.gbfir_conv1d(buf(79, dtype=0), buf(64, dtype=2), buf(16, dtype=0), 0, 0, 0, None) == 4
 
 
+def test_conv_axis_validation(lib):
+    # 4 blocks of [64][10], 16 taps: FULL needs 79 x 10 per block
+    def f(o, i, h, mode=0, inner=10, si=10, so=10, prec=0):
+        return lib.gbfir_conv1d_axis(o, i, h, inner, si, so, mode, 0, prec, None)
+    x = lambda n=64, b=4, st=None: buf(n, batch=b, dtype=0, stride=n * 10 if st is None else st)
+    h = buf(16, dtype=0)
+    assert f(x(79), x(), h, mode=3) == 1
+    assert f(x(80), x(), h) == 3
+    assert f(x(79), x(), h, inner=0) == 1
+    assert f(x(79), x(), h, si=0) == 1
+    assert f(x(79), x(), buf(16, batch=4, dtype=0)) == 2
+    assert f(x(79), x(b=3), h) == 2
+    # output signals that would overlap: a step below the inner count, blocks too close
+    assert f(x(79), x(), h, so=9) == 1
+    assert f(x(79, st=779), x(), h) == 1
+    # tensor-core forms are not built for the axis form
+    assert f(x(79), x(), h, prec=1) == 5
+
+
 def test_channelize_validation(lib):
     # D > M
     assert lib.gbfir_channelize_poly(buf(16 * 8), buf(128), buf(64, dtype=0), 8, 9, 0, None) == 1
