@@ -349,6 +349,88 @@ def run_mti(args, rank, world, dev):
     return 0
 
 
+def run_filter(args, rank, world, dev):
+    """MatX filter() with recursive coefficients: 64 rows x 2^20 real f32 through the
+    reference test's second-order section (h_rec {0.4, -0.1}, h_nonrec {2, 1})."""
+    import torch
+    import matx_gb300 as mx
+    B, N = 64, 1 << 20
+    g = torch.Generator(device=dev).manual_seed(61 + rank)
+    x = torch.rand(B, N, device=dev, generator=g) * 2 - 1
+    y = torch.empty_like(x)
+    flushbuf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    steps = max(3, min(args.steps, 100))
+    run = lambda: mx.filter(x, [0.4, -0.1], [2.0, 1.0], out=y)
+    for _ in range(args.warmup):
+        run()
+    l0 = mx.launch_count()
+    ms = _timed(run, steps, lambda: _flush_l2(flushbuf), stream)
+    launches = mx.launch_count() - l0
+    err = None
+    try:
+        import oracle
+        oracle.build()
+        r = oracle.iir_filter(x[:2].cpu().numpy().astype(np.float64), [0.4, -0.1], [2.0, 1.0])
+        err = float(np.linalg.norm(y[:2].cpu().numpy() - r) / np.linalg.norm(r))
+    except Exception as e:  # noqa: BLE001
+        err = {"unavailable": str(e)[:160]}
+    nbytes = 2 * B * N * 4  # read x once, write y once (the kernels read x twice)
+    line = {"metric": "IIR filter() GB/s (64 x 2^20 f32, 2 recursive + 2 non-recursive coefficients)",
+            "value": nbytes / (ms * 1e-3) / 1e9, "unit": "GB/s", "n_gpus": world, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform[-1,1])",
+            "config": {"workload": "filter(x, {0.4,-0.1}, {2,1}) on 64x2^20 f32",
+                       "l2": "flushed (256 MB write) before every timed launch"},
+            "hbm_frac": nbytes / (ms * 1e-3) / 1e9 / _peak(), "gsamples_per_s": B * N / (ms * 1e-3) / 1e9,
+            "hbm_frac_of_traffic": 3 * B * N * 4 / (ms * 1e-3) / 1e9 / _peak(),
+            "rel_l2_vs_fp64_rows01": err, "gpu_launches": launches}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_upfirdn(args, rank, world, dev):
+    """downsample(conv1d(upsample(x, 3), h, FULL), 2) on 64 x 2^20 c64 with a 61-tap Kaiser
+    sinc in one polyphase pass, beside the literal three-step composition (zero-stuffed
+    signal, conv1d, strided slice) through this library's own kernels."""
+    import torch
+    from scipy import signal
+    import matx_gb300 as mx
+    B, N, up, down = 64, 1 << 20, 3, 2
+    g = torch.Generator(device=dev).manual_seed(71 + rank)
+    x = torch.randn(B, N, dtype=torch.complex64, device=dev, generator=g)
+    h = torch.from_numpy(signal.firwin(61, 1.0 / 3, window=("kaiser", 5.0)).astype(np.float32)).to(dev)
+    y = mx.upfirdn(x, h, up, down, "full")
+    flushbuf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    steps = max(3, min(args.steps, 50))
+    run = lambda: mx.upfirdn(x, h, up, down, "full", out=y)
+    for _ in range(args.warmup):
+        run()
+    l0 = mx.launch_count()
+    ms = _timed(run, steps, lambda: _flush_l2(flushbuf), stream)
+    launches = mx.launch_count() - l0
+    run3 = lambda: mx.downsample(mx.conv1d(mx.upsample(x, up), h, "full"), down)
+    for _ in range(2):
+        y3 = run3()
+    ms3 = _timed(run3, max(3, steps // 5), lambda: _flush_l2(flushbuf), stream)
+    same = bool(torch.allclose(y3, y, rtol=1e-5, atol=1e-5))
+    macs = B * y.shape[-1] * 61 / up  # each output meets about L/up nonzero upsampled samples
+    nbytes = B * 8 * (N + y.shape[-1]) + 4 * 61
+    line = {"metric": "upfirdn GMAC/s (downsample(conv1d(upsample(x,3),h),2), c64, useful MACs)",
+            "value": macs / (ms * 1e-3) / 1e9, "unit": "GMAC/s", "n_gpus": world, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded complex Gaussian; Kaiser sinc)",
+            "config": {"workload": "upfirdn 64x2^20 c64, up 3, down 2, 61 taps, FULL",
+                       "l2": "flushed (256 MB write) before every timed launch"},
+            "hbm_frac": nbytes / (ms * 1e-3) / 1e9 / _peak(), "composition_ms": ms3, "vs_composition": ms3 / ms,
+            "composition_matches": same, "gpu_launches": launches}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_channelize(args, rank, world, dev):
     """channelize_poly c64, maximally decimated: 4 rows x 2^24 samples, M = 64 with a
     64x32 Kaiser sinc prototype and M = 256 with 16 taps per channel; FP32 and the
@@ -592,7 +674,7 @@ def main():
                          "(rows_per_thread, col_warps, group, buffers [+4: TMA-store epilogue]; profiling cases)")
     ap.add_argument("--ratios", default="3/2,4/5,160/147", help="comma-separated up/down list (profiling cases)")
     ap.add_argument("--workload", default="resample",
-                    choices=["resample", "ragged", "conv1d", "channelize", "fwdbwd", "mti"],
+                    choices=["resample", "ragged", "conv1d", "channelize", "fwdbwd", "mti", "filter", "upfirdn"],
                     help="secondary workloads, each printing its own JSON line: ragged (4096 uneven signals "
                          "in one persistent launch), conv1d (8x2^20 FULL), channelize (4x2^24, M=64/256), "
                          "fwdbwd (256x16384 forward + backward)")
@@ -622,6 +704,10 @@ def main():
         return run_conv1d(args, rank, world, dev)
     if args.workload == "channelize":
         return run_channelize(args, rank, world, dev)
+    if args.workload == "filter":
+        return run_filter(args, rank, world, dev)
+    if args.workload == "upfirdn":
+        return run_upfirdn(args, rank, world, dev)
     if args.workload == "mti":
         return run_mti(args, rank, world, dev)
     if args.workload == "fwdbwd":

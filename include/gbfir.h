@@ -7,10 +7,14 @@
  * rules and error classes:
  *
  *   gbfir_conv1d           include/matx/transforms/conv.h:467-532 (conv1d_impl)
- *   gbfir_conv1d_axis      include/matx/operators/conv.h:263-274 (conv1d with an axis)
  *                          include/matx/transforms/conv.h:402-451 (operand swap)
  *                          include/matx/transforms/conv.h:175-224 (direct CUDA path)
  *                          include/matx/transforms/corr.h:60-69   (corr = conv with reverse(conj(h)))
+ *   gbfir_conv1d_axis      include/matx/operators/conv.h:263-274 (conv1d with an axis)
+ *   gbfir_upsample / gbfir_downsample   include/matx/operators/updownsample.h:254-279
+ *   gbfir_upfirdn          downsample(conv1d(upsample(.)), .) of the same operators
+ *   gbfir_filter           include/matx/transforms/filter.h:159-188 (filter(): FIR-only
+ *                          conv1d SAME, or the recursive filter of kernels/filter.cuh:44)
  *   gbfir_resample_poly    include/matx/transforms/resample_poly.h:299-354 (resample_poly_impl)
  *                          include/matx/transforms/resample_poly.h:64-210  (CUDA dispatcher)
  *   gbfir_channelize_poly  include/matx/transforms/channelize_poly.h:724-849 (CUDA impl incl. the
@@ -141,6 +145,40 @@ GBFIR_API int gbfir_conv1d_axis(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_
  *  precision != FP32 runs the Toeplitz MMA form on the tensor cores for float32 /
  *  complex64 signals and real float32 taps; rates whose 8-sample rows need more than
  *  256 MMA columns (for example 160/147) return GBFIR_ERR_NOT_SUPPORTED. */
+/* MatX filter(in, h_rec, h_nonrec) along rows (include/matx/operators/filter.h:177-181,
+ *  include/matx/transforms/filter.h:159-188).  h_rec / h_nonrec are HOST arrays of
+ *  num_rec (0..4) / num_nonrec (1..4) coefficients of coef_dtype (MatX passes
+ *  cuda::std::array by value; at most 4 of each, kernels/filter.cuh:29-30):
+ *    num_rec == 0: conv1d(in, h_nonrec, SAME) (transforms/filter.h:185), len >= num_nonrec;
+ *    else y[n] = sum_{j<num_nonrec} h_nonrec[j] x[n-j] + sum_{k<num_rec} h_rec[k] y[n-1-k],
+ *    zero initial state (kernels/filter.cuh:44; test/00_operators/filter_test.cu:19-47).
+ *  out.len == in.len; out complex iff in or the coefficients are complex; all single or all
+ *  double.  The recursive form needs `workspace` (device, 16-byte aligned) of
+ *  gbfir_filter_workspace_size(out.batch, len, out.dtype) bytes (GBFIR_ERR_WORKSPACE if
+ *  missing or short); no device memory is allocated. */
+GBFIR_API size_t gbfir_filter_workspace_size(int64_t batch, int64_t len, int32_t out_dtype);
+GBFIR_API int gbfir_filter(gbfir_buf out, gbfir_buf in, const void *h_rec, int32_t num_rec,
+                           const void *h_nonrec, int32_t num_nonrec, int32_t coef_dtype,
+                           void *workspace, size_t workspace_bytes, gbfir_stream_t stream);
+
+/* MatX's upsample(in, dim, n) / downsample(in, dim, n) along rows
+ *  (include/matx/operators/updownsample.h:254-279): upsample writes in[i/n] where n
+ *  divides i and 0 elsewhere, out.len = in.len*n; downsample writes in[i*n],
+ *  out.len = ceil(in.len/n).  Same dtype in and out; `in` one row or out.batch rows. */
+GBFIR_API int gbfir_upsample(gbfir_buf out, gbfir_buf in, int64_t n, gbfir_stream_t stream);
+GBFIR_API int gbfir_downsample(gbfir_buf out, gbfir_buf in, int64_t n, gbfir_stream_t stream);
+
+/* downsample(conv1d(upsample(in, up), h, mode), down) in one polyphase pass that forms
+ *  neither the zero-stuffed signal nor the discarded outputs:
+ *    out[m] = sum_k in[k] * h[start + m*down - k*up],
+ *  start = the conv1d mode offset for the upsampled length N*up (0 FULL, (Lmin-1)/2 or
+ *  Lmin/2-1 SAME, Lmin-1 VALID, Lmin = min(N*up, L)), out.len = ceil(conv length / down)
+ *  (operators/updownsample.h:254-279 around transforms/conv.h:402-532).  No x-up scale
+ *  and no even-length lead zero (those are resample_poly's).  h is one row; FP32 / FP64
+ *  only (other precisions: GBFIR_ERR_NOT_SUPPORTED). */
+GBFIR_API int gbfir_upfirdn(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t up, int64_t down,
+                            int32_t mode, int32_t precision, gbfir_stream_t stream);
+
 GBFIR_API int gbfir_resample_poly(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t up,
                         int64_t down, int32_t precision, gbfir_stream_t stream);
 

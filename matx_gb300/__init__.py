@@ -29,7 +29,8 @@ _MODE_NAMES = {"full": 0, "same": 1, "valid": 2}
 
 __all__ = ["conv1d", "corr", "resample_poly", "channelize_poly", "GbfirError",
            "MATX_C_MODE_FULL", "MATX_C_MODE_SAME", "MATX_C_MODE_VALID", "launch_count",
-           "resample_out_len", "set_resample_tile"]
+           "resample_out_len", "set_resample_tile", "upsample", "downsample", "upfirdn", "filter",
+           "iir_filter"]
 
 _DT = {torch.float32: _lib.GBFIR_F32, torch.complex64: _lib.GBFIR_C64,
        torch.float64: _lib.GBFIR_F64, torch.complex128: _lib.GBFIR_C128}
@@ -223,6 +224,97 @@ def corr(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torch.
          precision="fp32", axis: int = -1):
     """Direct correlation: corr(x, h) = conv1d(x, reverse(conj(h))) (corr.h:67)."""
     return conv1d(x, h, mode, out=out, precision=precision, axis=axis, _corr=True)
+
+
+def _along_last(x: torch.Tensor, dim: int):
+    """x with `dim` moved last and made unit-stride, and the inverse move for the result."""
+    d = dim % max(x.dim(), 1)
+    if d == x.dim() - 1:
+        return _prep_in(x, "x"), (lambda y: y)
+    return x.movedim(d, -1).contiguous(), (lambda y: y.movedim(-1, d))
+
+
+def _updown(x: torch.Tensor, n: int, dim: int, up: bool) -> torch.Tensor:
+    what = "upsample" if up else "downsample"
+    if n < 1:
+        raise GbfirError(1, f"{what}: the rate must be >= 1")
+    xl, back = _along_last(_rows(x, what), dim)
+    N = xl.shape[-1]
+    olen = N * n if up else (N + n - 1) // n
+    out = torch.empty(*xl.shape[:-1], olen, dtype=xl.dtype, device=xl.device)
+    fn = _lib.load().gbfir_upsample if up else _lib.load().gbfir_downsample
+    _lib.check(fn(_buf(out, f"{what} out"), _buf(xl, f"{what} x"), n, _stream()))
+    return back(out)
+
+
+def upsample(x: torch.Tensor, n: int, dim: int = -1) -> torch.Tensor:
+    """MatX upsample(x, dim, n): n-fold zero stuffing along `dim`, x[i/n] where n divides i
+    (operators/updownsample.h:254-257); the result has n times the samples."""
+    return _updown(x, n, dim, True)
+
+
+def downsample(x: torch.Tensor, n: int, dim: int = -1) -> torch.Tensor:
+    """MatX downsample(x, dim, n): every n-th sample along `dim`, ceil(N/n) of them
+    (operators/updownsample.h:268-279, a strided slice)."""
+    return _updown(x, n, dim, False)
+
+
+def upfirdn(x: torch.Tensor, h: torch.Tensor, up: int = 1, down: int = 1, mode=MATX_C_MODE_FULL, *,
+            out: torch.Tensor | None = None) -> torch.Tensor:
+    """downsample(conv1d(upsample(x, up), h, mode), down) along the last dimension in one
+    polyphase pass (gbfir_upfirdn): out[m] = sum_k x[k] h[start + m*down - k*up], start the
+    conv1d mode offset of the upsampled length; no zero-stuffed signal is formed and no
+    discarded output is computed.  h is 1-D."""
+    m = _mode(mode)
+    if up < 1 or down < 1:
+        raise GbfirError(1, "upfirdn: up and down must be >= 1")
+    double = _out_dtype(x, h) in (torch.float64, torch.complex128)
+    x = _prep_in(_cast(x, double), "upfirdn x")
+    h = _prep_in(_cast(h, double), "upfirdn h")
+    if h.dim() != 1:
+        raise GbfirError(2, "upfirdn: the filter must be 1-D")
+    olen = -(-_olen(m, x.shape[-1] * up, h.shape[0]) // down)
+    if out is None:
+        out = torch.empty(*x.shape[:-1], olen, dtype=_out_dtype(x, h), device=x.device)
+    _lib.check(_lib.load().gbfir_upfirdn(_buf(out, "upfirdn out"), _buf(x, "upfirdn x"), _buf(h, "upfirdn h"),
+                                         up, down, m, 0, _stream()))
+    return out
+
+
+def iir_filter(x: torch.Tensor, h_rec, h_nonrec, *, out: torch.Tensor | None = None) -> torch.Tensor:
+    """MatX filter(x, h_rec, h_nonrec) along the last dimension (transforms/filter.h:159-188):
+    with no recursive coefficients conv1d(x, h_nonrec, SAME); else the causal recurrence
+    y[n] = sum_j h_nonrec[j] x[n-j] + sum_k h_rec[k] y[n-1-k] from a zero state.  At most 4
+    coefficients of each kind (host sequences, as MatX's cuda::std::array arguments)."""
+    import numpy as np
+    a = np.asarray(h_rec.cpu() if isinstance(h_rec, torch.Tensor) else h_rec).ravel()
+    b = np.asarray(h_nonrec.cpu() if isinstance(h_nonrec, torch.Tensor) else h_nonrec).ravel()
+    x = _prep_in(x, "filter x")
+    dbl = x.dtype in (torch.float64, torch.complex128)
+    cc = np.iscomplexobj(a) or np.iscomplexobj(b)
+    cdt = (np.complex128 if dbl else np.complex64) if cc else (np.float64 if dbl else np.float32)
+    ac, bc = np.ascontiguousarray(a.astype(cdt)), np.ascontiguousarray(b.astype(cdt))
+    coef_dt = {np.float32: _lib.GBFIR_F32, np.complex64: _lib.GBFIR_C64, np.float64: _lib.GBFIR_F64,
+               np.complex128: _lib.GBFIR_C128}[cdt]
+    odt = x.dtype
+    if cc and not x.is_complex():
+        odt = torch.complex128 if dbl else torch.complex64
+    if out is None:
+        out = torch.empty(x.shape, dtype=odt, device=x.device)
+    lib = _lib.load()
+    ob = _buf(out, "filter out")
+    ws = None
+    nbytes = 0
+    if a.size:
+        nbytes = int(lib.gbfir_filter_workspace_size(ob.batch, x.shape[-1], _DT[odt]))
+        ws = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=x.device)
+    _lib.check(lib.gbfir_filter(ob, _buf(x, "filter x"), ac.ctypes.data if a.size else None, int(a.size),
+                                bc.ctypes.data, int(b.size), coef_dt, ws.data_ptr() if ws is not None else None,
+                                nbytes, _stream()))
+    return out
+
+
+filter = iir_filter  # MatX's name for it
 
 
 def resample_out_len(n: int, up: int, down: int) -> int:

@@ -17,6 +17,12 @@ namespace gbfir {
 int conv1d_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int mode, int is_corr, cudaStream_t s);
 int conv1d_axis_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t inner, int64_t in_step,
                    int64_t out_step, int mode, int is_corr, cudaStream_t s);
+int updown_fp(const gbfir_buf &out, const gbfir_buf &in, int64_t n, bool up, cudaStream_t s);
+size_t filter_workspace_bytes(int64_t batch, int64_t len, int32_t out_dtype);
+int filter_fp(const gbfir_buf &out, const gbfir_buf &in, const void *a, int na, const void *b, int nb,
+              int32_t coef_dtype, void *workspace, cudaStream_t s);
+int upfirdn_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t up, int64_t down, int mode,
+               cudaStream_t s);
 int resample_poly_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t up, int64_t down,
                      cudaStream_t s);
 int channelize_poly_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t M, int64_t D,
@@ -196,6 +202,114 @@ int gbfir_conv1d_axis(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t inner, i
     return conv1d_axis_fp(out, in, h, inner, in_step, out_step, mode, is_corr != 0, s);
   } catch (...) {
     GBFIR_FAIL(GBFIR_ERR_CUDA, "conv1d (axis): internal exception");
+  }
+}
+
+size_t gbfir_filter_workspace_size(int64_t batch, int64_t len, int32_t out_dtype) {
+  if (batch < 1 || len < 1 || dtype_size(out_dtype) == 0) return 0;
+  return filter_workspace_bytes(batch, len, out_dtype);
+}
+
+int gbfir_filter(gbfir_buf out, gbfir_buf in, const void *h_rec, int32_t num_rec, const void *h_nonrec,
+                 int32_t num_nonrec, int32_t coef_dtype, void *workspace, size_t workspace_bytes,
+                 gbfir_stream_t stream) {
+  try {
+    GBFIR_TRY(check_buf(out, "filter out", false));
+    GBFIR_TRY(check_buf(in, "filter in", true));
+    if (dtype_size(coef_dtype) == 0) GBFIR_FAIL(GBFIR_ERR_INVALID_TYPE, "filter: unknown coefficient dtype");
+    if (dtype_double(in.dtype) != dtype_double(out.dtype) || dtype_double(in.dtype) != dtype_double(coef_dtype))
+      GBFIR_FAIL(GBFIR_ERR_INVALID_TYPE, "filter: operands must all be single or all be double precision");
+    const bool oc = dtype_complex(in.dtype) || dtype_complex(coef_dtype);
+    if (dtype_complex(out.dtype) != oc)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_TYPE, "filter: output must be %s", oc ? "complex" : "real");
+    if (num_rec < 0 || num_nonrec < 1)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "filter: need >= 0 recursive and >= 1 non-recursive coefficients");
+    if (num_rec > 4 || num_nonrec > 4)
+      GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "filter: at most 4 recursive and 4 non-recursive coefficients");
+    if ((num_rec > 0 && h_rec == nullptr) || h_nonrec == nullptr)
+      GBFIR_FAIL(GBFIR_ERR_NULL_POINTER, "filter: null coefficient array");
+    if (in.batch != 1 && in.batch != out.batch)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "filter: batch sizes do not match (out %lld, in %lld)",
+                 (long long)out.batch, (long long)in.batch);
+    if (out.len != in.len)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "filter: output length %lld, expected %lld", (long long)out.len,
+                 (long long)in.len);
+    if (num_rec == 0 && in.len < num_nonrec)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "filter: FIR-only filter (conv1d SAME) needs len >= %d", (int)num_nonrec);
+    if (num_rec > 0) {
+      if (out.batch > 65535) GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "filter: at most 65535 rows per call");
+      const size_t need = filter_workspace_bytes(out.batch, in.len, out.dtype);
+      if (workspace == nullptr || workspace_bytes < need)
+        GBFIR_FAIL(GBFIR_ERR_WORKSPACE, "filter: workspace of %zu bytes needed", need);
+      if (reinterpret_cast<uintptr_t>(workspace) % 16)
+        GBFIR_FAIL(GBFIR_ERR_ALIGNMENT, "filter: workspace not 16-byte aligned");
+    }
+    return filter_fp(out, in, h_rec, num_rec, h_nonrec, num_nonrec, coef_dtype, workspace,
+                     reinterpret_cast<cudaStream_t>(stream));
+  } catch (...) {
+    GBFIR_FAIL(GBFIR_ERR_CUDA, "filter: internal exception");
+  }
+}
+
+static int updown_entry(gbfir_buf out, gbfir_buf in, int64_t n, bool up, gbfir_stream_t stream) {
+  const char *what = up ? "upsample" : "downsample";
+  GBFIR_TRY(check_buf(out, what, false));
+  GBFIR_TRY(check_buf(in, what, true));
+  if (out.dtype != in.dtype) GBFIR_FAIL(GBFIR_ERR_INVALID_TYPE, "%s: input and output types differ", what);
+  if (n < 1) GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "%s: the rate must be >= 1", what);
+  if (in.batch != 1 && in.batch != out.batch)
+    GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "%s: batch sizes do not match (out %lld, in %lld)", what,
+               (long long)out.batch, (long long)in.batch);
+  const int64_t want = up ? in.len * n : (in.len + n - 1) / n;
+  if (out.len != want)
+    GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "%s: output length %lld, expected %lld", what, (long long)out.len,
+               (long long)want);
+  return updown_fp(out, in, n, up, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int gbfir_upsample(gbfir_buf out, gbfir_buf in, int64_t n, gbfir_stream_t stream) {
+  try {
+    return updown_entry(out, in, n, true, stream);
+  } catch (...) {
+    GBFIR_FAIL(GBFIR_ERR_CUDA, "upsample: internal exception");
+  }
+}
+
+int gbfir_downsample(gbfir_buf out, gbfir_buf in, int64_t n, gbfir_stream_t stream) {
+  try {
+    return updown_entry(out, in, n, false, stream);
+  } catch (...) {
+    GBFIR_FAIL(GBFIR_ERR_CUDA, "downsample: internal exception");
+  }
+}
+
+int gbfir_upfirdn(gbfir_buf out, gbfir_buf in, gbfir_buf h, int64_t up, int64_t down, int32_t mode, int32_t precision,
+                  gbfir_stream_t stream) {
+  try {
+    GBFIR_TRY(check_buf(out, "upfirdn out", false));
+    GBFIR_TRY(check_buf(in, "upfirdn in", true));
+    GBFIR_TRY(check_buf(h, "upfirdn h", false));
+    GBFIR_TRY(check_types(out, in, h, "upfirdn", false));
+    GBFIR_TRY(check_precision(precision, "upfirdn"));
+    if (precision != GBFIR_PREC_FP32)
+      GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "upfirdn: only the FP32/FP64 form is built");
+    if (up < 1 || down < 1) GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "upfirdn: up and down must be >= 1");
+    if (mode < GBFIR_MODE_FULL || mode > GBFIR_MODE_VALID)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "upfirdn: unknown mode %d", (int)mode);
+    if (h.batch != 1) GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "upfirdn: the filter must be one row");
+    if (in.batch != 1 && in.batch != out.batch)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "upfirdn: batch sizes do not match (out %lld, in %lld)",
+                 (long long)out.batch, (long long)in.batch);
+    const int64_t Nu = in.len * up;
+    const int64_t mx = std::max(Nu, h.len), mn = std::min(Nu, h.len);
+    const int64_t clen = mode == GBFIR_MODE_FULL ? Nu + h.len - 1 : mode == GBFIR_MODE_SAME ? mx : mx - mn + 1;
+    const int64_t want = (clen + down - 1) / down;
+    if (out.len != want)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "upfirdn: output length %lld, expected %lld", (long long)out.len,
+                 (long long)want);
+    return upfirdn_fp(out, in, h, up, down, mode, reinterpret_cast<cudaStream_t>(stream));
+  } catch (...) {
+    GBFIR_FAIL(GBFIR_ERR_CUDA, "upfirdn: internal exception");
   }
 }
 

@@ -96,15 +96,25 @@ __host__ __device__ inline size_t tap_table_bytes(int64_t ncg, int64_t span) {
   return taps + (((size_t)ncg * 4 + 15) & ~(size_t)15);
 }
 
-// Window layouts against bank conflicts of the row-strided reads (lanes read rows q*S + k):
-// PAD = 4, 5, 6 put one pad element after every 2^PAD elements (conflict-free for S a
-// multiple of 8, 32, 64); PAD = 1 permutes the low 3 bits of the index by bits 4-6 within
-// each block of 16 (conflict-free for S = 4 mod 8); PAD = 0 is the plain layout.
+// Window layouts against bank conflicts of the row-strided reads (lanes read rows q*S + k;
+// a 64-bit shared load is served per half-warp, so 16 lanes at stride S must hit distinct
+// 8-byte slots of 128 bytes).  PAD = 10 + t, t = ctz(S) (1..7): XOR the low min(t, 4) bits
+// of the index with the bits from max(t, 4) up, a permutation inside each block of 16
+// elements that is conflict-free for every even S below 256; PAD = 1 is the t = 3 form;
+// PAD = 4, 5, 6 put one pad element after every 2^PAD elements (the other element types);
+// PAD = 0 is the plain layout (odd S).
 template <int PAD>
 __device__ __forceinline__ int smem_idx(int p) {
-  if constexpr (PAD == 1) return p ^ ((p >> 4) & 7);
-  else if constexpr (PAD > 0) return p + (p >> PAD);
-  else return p;
+  if constexpr (PAD > 10) {
+    constexpr int t = PAD - 10, sh = t > 4 ? t : 4, m = (1 << (t < 4 ? t : 4)) - 1;
+    return p ^ ((p >> sh) & m);
+  } else if constexpr (PAD == 1) {
+    return p ^ ((p >> 4) & 7);
+  } else if constexpr (PAD > 0) {
+    return p + (p >> PAD);
+  } else {
+    return p;
+  }
 }
 
 // table[g*span + kk] holds the 4 taps he[c + (4g+jj)*down - (kl0(g)+kk)*up] (reversed when
@@ -410,9 +420,9 @@ __global__ void __launch_bounds__(RQ == 1 ? 512 : 256)
   }
 
   if constexpr (PAD > 0) {
-    // Even row stride: the window is stored with one pad element per 16 (bank-conflict
-    // free row-strided reads), which a bulk copy cannot produce; stage it with cp.async
-    // (zero-filled outside the signal).
+    // Even row stride: the window is stored in a bank-conflict-free layout (an element
+    // permutation inside blocks of 16, or one pad per 16), which a bulk copy cannot
+    // produce; stage it with cp.async (zero-filled outside the signal).
     auto issue_loads = [&](int64_t tile, XT *buf) {
       const int64_t b = tile / p.tiles_per_row;
       const int64_t q0 = (tile - b * p.tiles_per_row) * p.QC;
@@ -665,9 +675,15 @@ inline int dispatch_rq(RsParams &p, const CUtensorMap &m, int rq, int pad, size_
                        int threads) {
   if (pad == 0) return dispatch_rq_pad<T, XC, HC, 0>(p, m, rq, smem, s, threads);
   if constexpr (std::is_same<T, float>::value && XC && !HC) {
-    if (pad == 1) return dispatch_rq_pad<T, XC, HC, 1>(p, m, rq, smem, s, threads);
-    if (pad == 5) return dispatch_rq_pad<T, XC, HC, 5>(p, m, rq, smem, s, threads);
-    if (pad == 6) return dispatch_rq_pad<T, XC, HC, 6>(p, m, rq, smem, s, threads);
+    switch (pad) {
+      case 11: return dispatch_rq_pad<T, XC, HC, 11>(p, m, rq, smem, s, threads);
+      case 12: return dispatch_rq_pad<T, XC, HC, 12>(p, m, rq, smem, s, threads);
+      case 13: return dispatch_rq_pad<T, XC, HC, 13>(p, m, rq, smem, s, threads);
+      case 14: return dispatch_rq_pad<T, XC, HC, 14>(p, m, rq, smem, s, threads);
+      case 15: return dispatch_rq_pad<T, XC, HC, 15>(p, m, rq, smem, s, threads);
+      case 16: return dispatch_rq_pad<T, XC, HC, 16>(p, m, rq, smem, s, threads);
+      default: return dispatch_rq_pad<T, XC, HC, 17>(p, m, rq, smem, s, threads);
+    }
   }
   return dispatch_rq_pad<T, XC, HC, 4>(p, m, rq, smem, s, threads);
 }
@@ -706,15 +722,18 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
   // for 9..16, so the CTA has 8 warps or wc of them
   const int wr = wc <= 8 ? 8 / wc : 1;
   const int threads = 32 * wc * wr;
-  // even row strides need a padded window (coarser pads for strides of 32 or 64 samples,
-  // complex float signals with real taps)
+  // even row strides need a conflict-free window layout: the XOR permutation for ctz(S)
+  // (complex float signals with real taps), one pad per 16 elements otherwise
   int pad = (geo.S % 2) ? 0 : 4;
-  if (pad && std::is_same<T, float>::value && XC && !HC)
-    pad = geo.S % 64 == 0 ? 6 : geo.S % 32 == 0 ? 5 : geo.S % 8 == 0 ? 4 : geo.S % 4 == 0 ? 1 : 4;
+  if (pad && std::is_same<T, float>::value && XC && !HC) {
+    int t = 0;
+    while (t < 7 && ((geo.S >> t) & 1) == 0) t++;
+    pad = 10 + t;
+  }
   // window buffer: padded layout for even S; for odd S room for the 16-byte-aligned bulk copy
   constexpr int64_t G16 = 16 / (int64_t)sizeof(XT);
   auto window_alloc = [&](int64_t win) -> int64_t {
-    if (pad == 1) return (win + 15) / 16 * 16;  // the permutation stays inside blocks of 16
+    if (pad == 1 || pad > 10) return (win + 15) / 16 * 16;  // the permutations stay inside blocks of 16
     return pad ? win + (win >> pad) + 1 : (win + 3 * G16 - 1) / G16 * G16;
   };
   // TMA-store epilogue (complex float outputs): rows of an even Nt >= 8 (64-byte boxes), 4

@@ -52,6 +52,7 @@ def lib():
                 _p, _p, _i64, _i64, _p, _i64, _i64, _i64, _i64, _int, _int, _int]
             getattr(L, "oracle_resample_poly_bwd" + suf).argtypes = [
                 _p, _p, _p, _i64, _p, _i64, _p, _i64, _i64, _i64, _i64, _int]
+            getattr(L, "oracle_iir_filter" + suf).argtypes = [_p, _p, _i64, _i64, _p, _int, _p, _int, _int, _int]
             getattr(L, "oracle_conv1d_bwd" + suf).argtypes = [
                 _p, _p, _p, _i64, _p, _i64, _p, _i64, _i64, _int, _int]
         L.oracle_max_threads.restype = _int
@@ -189,6 +190,32 @@ def conv1d_bwd(gy, x, h, mode: int, nthreads: int = 1):
     if rc:
         raise ValueError(f"oracle_conv1d_bwd failed ({rc})")
     return dx, dh
+
+
+def iir_filter(x, h_rec, h_nonrec, double: bool = True):
+    """MatX filter(x, h_rec, h_nonrec) on rows: conv1d SAME with h_nonrec when h_rec is
+    empty (transforms/filter.h:185), else the causal recurrence
+    y[n] = sum_j h_nonrec[j] x[n-j] + sum_k h_rec[k] y[n-1-k] (kernels/filter.cuh)."""
+    a = np.asarray(h_rec)
+    b = np.asarray(h_nonrec)
+    if a.size == 0:
+        return conv1d(x, b, 1, double=double)
+    xs, xc = _prep(x, double)
+    cc = np.iscomplexobj(a) or np.iscomplexobj(b)
+    ct = (np.complex128 if double else np.complex64) if cc else (np.float64 if double else np.float32)
+    ac, bc = np.ascontiguousarray(a.astype(ct)), np.ascontiguousarray(b.astype(ct))
+    B, N = xs.shape
+    oc = xc or cc
+    if cc and not xc:
+        xs = np.ascontiguousarray(xs.astype(np.complex128 if double else np.complex64))
+        xc = True
+    odt = (np.complex128 if double else np.complex64) if oc else (np.float64 if double else np.float32)
+    out = np.empty((B, N), dtype=odt)
+    rc = getattr(lib(), "oracle_iir_filter" + _suffix(double))(
+        _ptr(out), _ptr(xs), N, B, _ptr(ac), a.size, _ptr(bc), b.size, int(xc), int(cc))
+    if rc:
+        raise ValueError(f"oracle_iir_filter failed ({rc})")
+    return out
 
 
 # ---- MatX HostExecutor (reference) wrappers ---------------------------------

@@ -412,6 +412,50 @@ int FN(oracle_conv1d_bwd)(T *dx, T *dh, const T *gy, int64_t out_len,
   return 0;
 }
 
+/* ---------------------------------------------------------------------------
+ * Recursive filter() (MatX filter(in, h_rec, h_nonrec) with h_rec non-empty):
+ *   y[n] = sum_{j<nb} b[j] x[n-j] + sum_{k<na} a[k] y[n-1-k],  zero initial state,
+ * one row at a time, in order.  This is the recurrence MatX's RecursiveFilter
+ * solves in parallel (include/matx/kernels/filter.cuh:44-, correction factors of
+ * include/matx/transforms/filter.h:206-250) and the sequential loop its own test
+ * checks it against (test/00_operators/filter_test.cu:19-47).  x / y complex when
+ * xc or cc; coefficients complex when cc.  (MatX's FIR-only filter is conv1d SAME,
+ * transforms/filter.h:185: the oracle wrapper routes it to oracle_conv1d.)
+ * ------------------------------------------------------------------------- */
+int FN(oracle_iir_filter)(T *out, const T *x, int64_t N, int64_t B, const T *a, int na, const T *b, int nb,
+                          int xc, int cc) {
+  if (N <= 0 || B <= 0 || na < 0 || nb < 0) return 1;
+  const int oc = xc || cc;
+  for (int64_t r = 0; r < B; r++) {
+    const T *xr = x + r * N * (xc ? 2 : 1);
+    T *yr = out + r * N * (oc ? 2 : 1);
+    for (int64_t n = 0; n < N; n++) {
+      T sr = 0, si = 0;
+      for (int j = 0; j < nb; j++) {
+        if (n - j < 0) continue;
+        const T xre = xc ? xr[2 * (n - j)] : xr[n - j], xim = xc ? xr[2 * (n - j) + 1] : 0;
+        const T cre = cc ? b[2 * j] : b[j], cim = cc ? b[2 * j + 1] : 0;
+        sr += xre * cre - xim * cim;
+        si += xre * cim + xim * cre;
+      }
+      for (int k = 0; k < na; k++) {
+        if (n - 1 - k < 0) continue;
+        const T yre = oc ? yr[2 * (n - 1 - k)] : yr[n - 1 - k], yim = oc ? yr[2 * (n - 1 - k) + 1] : 0;
+        const T cre = cc ? a[2 * k] : a[k], cim = cc ? a[2 * k + 1] : 0;
+        sr += yre * cre - yim * cim;
+        si += yre * cim + yim * cre;
+      }
+      if (oc) {
+        yr[2 * n] = sr;
+        yr[2 * n + 1] = si;
+      } else {
+        yr[n] = sr;
+      }
+    }
+  }
+  return 0;
+}
+
 #undef FN
 #undef CAT
 #undef CAT_

@@ -114,6 +114,38 @@ def test_conv_axis_validation(lib):
     assert f(x(79), x(), h, prec=1) == 5
 
 
+def test_updown_validation(lib):
+    assert lib.gbfir_upsample(buf(31, dtype=0), buf(10, dtype=0), 3, None) == 3
+    assert lib.gbfir_upsample(buf(30, dtype=1), buf(10, dtype=0), 3, None) == 4
+    assert lib.gbfir_downsample(buf(3, dtype=0), buf(10, dtype=0), 3, None) == 3
+    assert lib.gbfir_downsample(buf(4, dtype=0), buf(10, dtype=0), 0, None) == 1
+    # upfirdn: FULL of the 3x upsampled 64 samples with 16 taps is 207, then ceil(/2) = 104
+    f = lambda o, mode=0, up=3, dn=2, prec=0: lib.gbfir_upfirdn(o, buf(64, dtype=0), buf(16, dtype=0), up, dn,
+                                                               mode, 0 if prec == 0 else prec, None)
+    assert f(buf(105, dtype=0)) == 3
+    assert f(buf(97, dtype=0), mode=1) == 3        # SAME: ceil(192 / 2) = 96
+    assert f(buf(104, dtype=0), up=0) == 1
+    assert f(buf(104, dtype=0), mode=4) == 1
+    assert f(buf(104, dtype=0), prec=1) == 5
+
+
+def test_filter_validation(lib):
+    a = (ctypes.c_float * 4)(0.4, -0.1, 0, 0)
+    b = (ctypes.c_float * 4)(2.0, 1.0, 0, 0)
+    f = lambda o, i, na=2, nb=2, cdt=0, ws=None, wsb=0: lib.gbfir_filter(o, i, a, na, b, nb, cdt, ws, wsb, None)
+    x = buf(1000, batch=3, dtype=0)
+    assert lib.gbfir_filter_workspace_size(3, 1000, 0) == 3 * 1 * 4 * 4
+    assert lib.gbfir_filter_workspace_size(3, 8193, 1) == 3 * 2 * 4 * 8
+    assert f(buf(999, batch=3, dtype=0), x) == 3
+    assert f(buf(1000, batch=3, dtype=1), x) == 4           # real in, real taps -> real out
+    assert f(buf(1000, batch=3, dtype=0), x, na=5) == 5
+    assert f(buf(1000, batch=3, dtype=0), x, nb=0) == 1
+    assert f(buf(1000, batch=3, dtype=0), x) == 9            # no workspace for the recursive form
+    assert f(buf(1000, batch=3, dtype=0), x, ws=FAKE, wsb=47) == 9
+    assert f(buf(3, dtype=0), buf(3, dtype=0), na=0, nb=4) == 3   # FIR-only: conv1d SAME size rule
+    assert f(buf(1000, batch=3, dtype=2), x) == 4           # mixed precision
+
+
 def test_channelize_validation(lib):
     # D > M
     assert lib.gbfir_channelize_poly(buf(16 * 8), buf(128), buf(64, dtype=0), 8, 9, 0, None) == 1

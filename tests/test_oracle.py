@@ -234,3 +234,45 @@ def test_adjoint_oracle_matches_matx_built_gradients(oracle_mod):
     for up, down in ((3, 2), (2, 3), (4, 5)):
         dx, _ = oracle_mod.resample_poly_bwd(z[f"rs_{up}_{down}__gy"], x, h, up, down)
         assert rel_l2(dx, z[f"rs_{up}_{down}__dx"]) < 1e-12
+
+
+def _filter_test_regression_expected(batches, n, h_rec, h_nonrec):
+    """The sequential loop of MatX's own IIR test (test/00_operators/filter_test.cu:19-47)."""
+    x = np.array([[((((i + 11 * b) % 23) - 11)) / 7.0 for i in range(n)] for b in range(batches)])
+    exp = np.zeros((batches, n))
+    for b in range(batches):
+        for i in range(n):
+            y = 0.0
+            for nr, c in enumerate(h_nonrec):
+                if i >= nr:
+                    y += c * x[b, i - nr]
+            for r, c in enumerate(h_rec):
+                if i >= r + 1:
+                    y += c * exp[b, i - r - 1]
+            exp[b, i] = y
+    return x, exp
+
+
+def test_oracle_iir_matches_reference_test(oracle_mod):
+    # IIRNonMultipleOfChunkSize: 3 rows of 8192 + 37 samples, h_rec {0.4, -0.1}, h_nonrec {2, 1}
+    x, exp = _filter_test_regression_expected(3, 8192 + 37, (0.4, -0.1), (2.0, 1.0))
+    y = oracle_mod.iir_filter(x, [0.4, -0.1], [2.0, 1.0])
+    assert np.max(np.abs(y - exp)) < 1e-12
+    yf = oracle_mod.iir_filter(x.astype(np.float32), np.float32([0.4, -0.1]), np.float32([2.0, 1.0]), double=False)
+    assert np.max(np.abs(yf - exp)) < 1e-2  # the reference test's float tolerance
+
+
+def test_oracle_iir_matches_lfilter(oracle_mod):
+    signal = pytest.importorskip("scipy.signal")
+    rng = np.random.default_rng(seed_of("iir_lfilter"))
+    for na, nb, cplx in ((1, 1, False), (4, 4, True), (3, 2, True), (2, 4, False)):
+        a = rng.uniform(-0.3, 0.3, na) + (1j * rng.uniform(-0.2, 0.2, na) if cplx else 0)
+        b = rng.standard_normal(nb) + (1j * rng.standard_normal(nb) if cplx else 0)
+        x = rng.standard_normal((2, 3000)) + (1j * rng.standard_normal((2, 3000)) if cplx else 0)
+        y = oracle_mod.iir_filter(x, a, b)
+        r = signal.lfilter(b, np.concatenate([[1.0], -a]), x, axis=-1)
+        assert np.max(np.abs(y - r)) < 1e-9 * np.max(np.abs(r)), (na, nb, cplx)
+    # FIR only: conv1d SAME (transforms/filter.h:185)
+    x = rng.standard_normal((2, 500))
+    assert np.array_equal(oracle_mod.iir_filter(x, [], [1.0, -2.0, 1.0]),
+                          oracle_mod.conv1d(x, np.array([1.0, -2.0, 1.0]), 1))
