@@ -121,19 +121,18 @@ __device__ __forceinline__ IV<T, OC> iir_load(const IirParams &p, const void *ro
   return v;
 }
 
-// v <- M v for the (na x na) matrix M (complex entries when CC)
-template <typename T, bool OC, bool CC>
-__device__ __forceinline__ void matvec(const IirParams &p, int lv, IV<T, OC> (&v)[kIirMaxCoef], int na) {
-  IV<T, OC> r[kIirMaxCoef];
+// v <- M v for the (CAP x CAP) matrix M (complex entries when CC)
+template <typename T, bool OC, bool CC, int CAP>
+__device__ __forceinline__ void matvec(const IirParams &p, int lv, IV<T, OC> (&v)[kIirMaxCoef]) {
+  IV<T, OC> r[CAP];
 #pragma unroll
-  for (int i = 0; i < kIirMaxCoef; i++) {
+  for (int i = 0; i < CAP; i++) {
     r[i] = IV<T, OC>::zero();
 #pragma unroll
-    for (int j = 0; j < kIirMaxCoef; j++)
-      if (i < na && j < na) r[i] = cmad<T, OC, CC>(r[i], IirC<T>::m(p, lv, i, j), v[j]);
+    for (int j = 0; j < CAP; j++) r[i] = cmad<T, OC, CC>(r[i], IirC<T>::m(p, lv, i, j), v[j]);
   }
 #pragma unroll
-  for (int i = 0; i < kIirMaxCoef; i++) v[i] = r[i];
+  for (int i = 0; i < CAP; i++) v[i] = r[i];
 }
 
 // Shared staging of one CTA's 8192 samples: chunk t (32 elements of ES bytes) sits at
@@ -187,32 +186,29 @@ __device__ __forceinline__ void read_chunk(const unsigned char *sm, IV<T, OC> (&
   }
 }
 
-// The chunk's recurrence from entry state s (s[k] = y[c-1-k]); halo[i] = x[c-1-i].  WRITE
-// replaces xr[j] by y[c+j].
-template <typename T, bool OC, bool CC, bool WRITE>
+// The chunk's recurrence from entry state s (s[k] = y[c-1-k]); halo[i] = x[c-1-i].  CAP
+// coefficients of each kind, zero-padded (no per-sample tests).  WRITE replaces xr[j] by y[c+j].
+template <typename T, bool OC, bool CC, int CAP, bool WRITE>
 __device__ __forceinline__ void run_chunk(const IirParams &p, IV<T, OC> (&xr)[kIirChunk],
                                           const IV<T, OC> (&halo)[kIirMaxCoef - 1], IV<T, OC> (&s)[kIirMaxCoef]) {
   using V = IV<T, OC>;
-  V xw[kIirMaxCoef];  // xw[i] = x[n - i]
+  V xw[CAP];  // xw[i] = x[n - i]
 #pragma unroll
-  for (int i = 1; i < kIirMaxCoef; i++) xw[i] = halo[i - 1];
+  for (int i = 1; i < CAP; i++) xw[i] = halo[i - 1];
 #pragma unroll
   for (int j = 0; j < kIirChunk; j++) {
     xw[0] = xr[j];
     // the feed-forward part first: only the feedback terms sit on the recurrence chain
-    V w = V::zero();
+    V y = V::zero();
 #pragma unroll
-    for (int i = 0; i < kIirMaxCoef; i++)
-      if (i < p.nb) w = cmad<T, OC, CC>(w, IirC<T>::b(p, i), xw[i]);
-    V y = w;
+    for (int i = 0; i < CAP; i++) y = cmad<T, OC, CC>(y, IirC<T>::b(p, i), xw[i]);
 #pragma unroll
-    for (int k = kIirMaxCoef - 1; k >= 0; k--)
-      if (k < p.na) y = cmad<T, OC, CC>(y, IirC<T>::a(p, k), s[k]);
+    for (int k = CAP - 1; k >= 0; k--) y = cmad<T, OC, CC>(y, IirC<T>::a(p, k), s[k]);
 #pragma unroll
-    for (int k = kIirMaxCoef - 1; k > 0; k--) s[k] = s[k - 1];
+    for (int k = CAP - 1; k > 0; k--) s[k] = s[k - 1];
     s[0] = y;
 #pragma unroll
-    for (int i = kIirMaxCoef - 1; i > 0; i--) xw[i] = xw[i - 1];
+    for (int i = CAP - 1; i > 0; i--) xw[i] = xw[i - 1];
     if constexpr (WRITE) xr[j] = y;
   }
 }
@@ -220,13 +216,13 @@ __device__ __forceinline__ void run_chunk(const IirParams &p, IV<T, OC> (&xr)[kI
 // One CTA = 256 chunks of one row: each thread runs its chunk from a zero entry, the CTA
 // scans the chunk maps (the carry injected into chunk 0); APPLY reruns each chunk from its
 // true entry state and writes y, else the CTA's zero-entry final state goes to the workspace.
-template <typename T, bool XC, bool OC, bool CC, bool APPLY>
+template <typename T, bool XC, bool OC, bool CC, int CAP, bool APPLY>
 __global__ void __launch_bounds__(kIirThreads) iir_block(const IirParams p, int vec) {
   using V = IV<T, OC>;
   using XE = typename val_of<T, XC>::type;
   using OE = typename val_of<T, OC>::type;
   constexpr int XES = (int)sizeof(XE), OES = (int)sizeof(OE);
-  __shared__ V sh[kIirThreads * kIirMaxCoef];  // scan exchange
+  __shared__ V sh[kIirThreads * CAP];  // scan exchange
   extern __shared__ __align__(16) unsigned char stg[];  // 256 chunks of 32 * OES + 16 bytes
   const int64_t row = blockIdx.y, blk = blockIdx.x;
   const int tid = threadIdx.x;
@@ -237,7 +233,7 @@ __global__ void __launch_bounds__(kIirThreads) iir_block(const IirParams p, int 
   V xr[kIirChunk], halo[kIirMaxCoef - 1];
   read_chunk<T, XC, OC>(stg, xr);
 #pragma unroll
-  for (int i = 0; i < kIirMaxCoef - 1; i++) {
+  for (int i = 0; i < CAP - 1; i++) {
     if (tid > 0) {
       const XE e = *reinterpret_cast<const XE *>(stg + stg_off<XES>(tid * kIirChunk - 1 - i));
       halo[i] = V::zero();
@@ -253,51 +249,51 @@ __global__ void __launch_bounds__(kIirThreads) iir_block(const IirParams p, int 
   }
   V s[kIirMaxCoef];
 #pragma unroll
-  for (int k = 0; k < kIirMaxCoef; k++) s[k] = V::zero();
-  run_chunk<T, OC, CC, false>(p, xr, halo, s);
+  for (int k = 0; k < CAP; k++) s[k] = V::zero();
+  run_chunk<T, OC, CC, CAP, false>(p, xr, halo, s);
   // inclusive scan of the chunk maps: G_t = M G_{t-1} + g_t
   V carry[kIirMaxCoef];
   V *wsb = reinterpret_cast<V *>(p.ws) + (row * p.nblk + blk) * kIirMaxCoef;
 #pragma unroll
-  for (int k = 0; k < kIirMaxCoef; k++) carry[k] = APPLY ? wsb[k] : V::zero();
+  for (int k = 0; k < CAP; k++) carry[k] = APPLY ? wsb[k] : V::zero();
   if (APPLY && tid == 0) {
     V mc[kIirMaxCoef];
 #pragma unroll
-    for (int k = 0; k < kIirMaxCoef; k++) mc[k] = carry[k];
-    matvec<T, OC, CC>(p, 0, mc, p.na);
+    for (int k = 0; k < CAP; k++) mc[k] = carry[k];
+    matvec<T, OC, CC, CAP>(p, 0, mc);
 #pragma unroll
-    for (int k = 0; k < kIirMaxCoef; k++) s[k] = vadd<T, OC>(s[k], mc[k]);
+    for (int k = 0; k < CAP; k++) s[k] = vadd<T, OC>(s[k], mc[k]);
   }
 #pragma unroll 1
   for (int lv = 0; lv < 8; lv++) {
     const int d = 1 << lv;
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < kIirMaxCoef; k++) sh[k * kIirThreads + tid] = s[k];
+    for (int k = 0; k < CAP; k++) sh[k * kIirThreads + tid] = s[k];
     __syncthreads();
     if (tid >= d) {
       V o[kIirMaxCoef];
 #pragma unroll
-      for (int k = 0; k < kIirMaxCoef; k++) o[k] = sh[k * kIirThreads + tid - d];
-      matvec<T, OC, CC>(p, lv, o, p.na);
+      for (int k = 0; k < CAP; k++) o[k] = sh[k * kIirThreads + tid - d];
+      matvec<T, OC, CC, CAP>(p, lv, o);
 #pragma unroll
-      for (int k = 0; k < kIirMaxCoef; k++) s[k] = vadd<T, OC>(s[k], o[k]);
+      for (int k = 0; k < CAP; k++) s[k] = vadd<T, OC>(s[k], o[k]);
     }
   }
   if constexpr (!APPLY) {
     if (tid == kIirThreads - 1) {
 #pragma unroll
-      for (int k = 0; k < kIirMaxCoef; k++) wsb[k] = s[k];
+      for (int k = 0; k < CAP; k++) wsb[k] = s[k];
     }
   } else {
     // entry state of chunk t = G_{t-1} (the carry for chunk 0)
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < kIirMaxCoef; k++) sh[k * kIirThreads + tid] = s[k];
+    for (int k = 0; k < CAP; k++) sh[k * kIirThreads + tid] = s[k];
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < kIirMaxCoef; k++) s[k] = tid ? sh[k * kIirThreads + tid - 1] : carry[k];
-    run_chunk<T, OC, CC, true>(p, xr, halo, s);
+    for (int k = 0; k < CAP; k++) s[k] = tid ? sh[k * kIirThreads + tid - 1] : carry[k];
+    run_chunk<T, OC, CC, CAP, true>(p, xr, halo, s);
     // drain through the staging buffer: the chunks in place, then coalesced rows
     __syncthreads();  // every lane has read its samples and its neighbour's halo
     unsigned char *mine = stg + tid * (32 * OES + 16);
@@ -331,7 +327,7 @@ __global__ void __launch_bounds__(kIirThreads) iir_block(const IirParams p, int 
 
 // One CTA per row: ws[row][j] <- the carry into CTA j, from the CTAs' zero-entry final
 // states (staged in shared memory, then one thread walks them in order).
-template <typename T, bool OC, bool CC>
+template <typename T, bool OC, bool CC, int CAP>
 __global__ void iir_carries(const IirParams p) {
   using V = IV<T, OC>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -344,17 +340,17 @@ __global__ void iir_carries(const IirParams p) {
   if (threadIdx.x == 0) {
     V cur[kIirMaxCoef];
 #pragma unroll
-    for (int k = 0; k < kIirMaxCoef; k++) cur[k] = V::zero();
+    for (int k = 0; k < CAP; k++) cur[k] = V::zero();
     for (int64_t j = 0; j < p.nblk; j++) {
       V f[kIirMaxCoef];
 #pragma unroll
-      for (int k = 0; k < kIirMaxCoef; k++) {
+      for (int k = 0; k < CAP; k++) {
         f[k] = st[j * kIirMaxCoef + k];
         st[j * kIirMaxCoef + k] = cur[k];
       }
-      matvec<T, OC, CC>(p, 8, cur, p.na);
+      matvec<T, OC, CC, CAP>(p, 8, cur);
 #pragma unroll
-      for (int k = 0; k < kIirMaxCoef; k++) cur[k] = vadd<T, OC>(cur[k], f[k]);
+      for (int k = 0; k < CAP; k++) cur[k] = vadd<T, OC>(cur[k], f[k]);
     }
   }
   __syncthreads();
@@ -362,7 +358,7 @@ __global__ void iir_carries(const IirParams p) {
 }
 
 // FIR-only filter(): conv1d SAME with the (at most 4) host coefficients, one output per thread.
-template <typename T, bool OC, bool CC>
+template <typename T, bool OC, bool CC, int CAP>
 __global__ void fir_same(const IirParams p, int start) {
   using V = IV<T, OC>;
   const int64_t total = p.N * p.batch;
@@ -372,8 +368,7 @@ __global__ void fir_same(const IirParams p, int start) {
                        row * p.x_bstride * (int64_t)sizeof(T) * ((OC && p.xc) ? 2 : 1);
     V y = V::zero();
 #pragma unroll
-    for (int i = 0; i < kIirMaxCoef; i++)
-      if (i < p.nb) y = cmad<T, OC, CC>(y, IirC<T>::b(p, i), iir_load<T, OC>(p, xrow, n + start - i));
+    for (int i = 0; i < CAP; i++) y = cmad<T, OC, CC>(y, IirC<T>::b(p, i), iir_load<T, OC>(p, xrow, n + start - i));
     T *yrow = reinterpret_cast<T *>(p.y) + row * p.y_bstride * (OC ? 2 : 1);
     if constexpr (OC) {
       yrow[2 * n] = y.re;
@@ -407,7 +402,7 @@ size_t filter_workspace_bytes(int64_t batch, int64_t len, int32_t out_dtype) {
   return (size_t)batch * (size_t)nblk * kIirMaxCoef * dtype_size(out_dtype);
 }
 
-template <typename T, bool XC, bool OC, bool CC>
+template <typename T, bool XC, bool OC, bool CC, int CAP>
 static int launch_filter(IirParams &p, cudaStream_t s) {
   if (p.na == 0) {
     // conv1d SAME start for Lmin = nb (the signal is at least as long as the filter)
@@ -416,7 +411,7 @@ static int launch_filter(IirParams &p, cudaStream_t s) {
     int64_t grid = (total + 255) / 256;
     const int64_t cap = (int64_t)num_sms() * 16;
     if (grid > cap) grid = cap;
-    fir_same<T, OC, CC><<<(unsigned)(grid < 1 ? 1 : grid), 256, 0, s>>>(p, start);
+    fir_same<T, OC, CC, CAP><<<(unsigned)(grid < 1 ? 1 : grid), 256, 0, s>>>(p, start);
     return check_launch("filter (FIR)");
   }
   using V = IV<T, OC>;
@@ -424,9 +419,9 @@ static int launch_filter(IirParams &p, cudaStream_t s) {
   if (p.batch > 65535) GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "filter: at most 65535 rows per call");
   const size_t csmem = (size_t)p.nblk * kIirMaxCoef * sizeof(V);
   const size_t bsmem = (size_t)kIirThreads * (32 * oes + 16);
-  int rc = ensure_smem((const void *)iir_carries<T, OC, CC>, csmem, "filter");
-  if (!rc) rc = ensure_smem((const void *)iir_block<T, XC, OC, CC, false>, bsmem, "filter");
-  if (!rc) rc = ensure_smem((const void *)iir_block<T, XC, OC, CC, true>, bsmem, "filter");
+  int rc = ensure_smem((const void *)iir_carries<T, OC, CC, CAP>, csmem, "filter");
+  if (!rc) rc = ensure_smem((const void *)iir_block<T, XC, OC, CC, CAP, false>, bsmem, "filter");
+  if (!rc) rc = ensure_smem((const void *)iir_block<T, XC, OC, CC, CAP, true>, bsmem, "filter");
   if (rc) return rc;
   // coalesced 16-byte fills and drains when every row start is 16-byte aligned
   const int vec = (reinterpret_cast<uintptr_t>(p.x) % 16 == 0 && reinterpret_cast<uintptr_t>(p.y) % 16 == 0 &&
@@ -434,13 +429,13 @@ static int launch_filter(IirParams &p, cudaStream_t s) {
                       ? 1
                       : 0;
   const dim3 grid((unsigned)p.nblk, (unsigned)p.batch);
-  iir_block<T, XC, OC, CC, false><<<grid, kIirThreads, bsmem, s>>>(p, vec);
+  iir_block<T, XC, OC, CC, CAP, false><<<grid, kIirThreads, bsmem, s>>>(p, vec);
   rc = check_launch("filter (IIR block states)");
   if (rc) return rc;
-  iir_carries<T, OC, CC><<<(unsigned)p.batch, 128, csmem, s>>>(p);
+  iir_carries<T, OC, CC, CAP><<<(unsigned)p.batch, 128, csmem, s>>>(p);
   rc = check_launch("filter (IIR carries)");
   if (rc) return rc;
-  iir_block<T, XC, OC, CC, true><<<grid, kIirThreads, bsmem, s>>>(p, vec);
+  iir_block<T, XC, OC, CC, CAP, true><<<grid, kIirThreads, bsmem, s>>>(p, vec);
   return check_launch("filter (IIR)");
 }
 
@@ -474,14 +469,16 @@ int filter_fp(const gbfir_buf &out, const gbfir_buf &in, const void *a, int na, 
   };
   for (int i = 0; i < na; i++) coef(a, i, p.a[i]);
   for (int i = 0; i < nb; i++) coef(b, i, p.b[i]);
+  // kernels run CAP = 2 or 4 coefficients of each kind, zero-padded
+  const int cap = (na <= 2 && nb <= 2) ? 2 : 4;
   if (na > 0) {
-    // companion matrix of y[n] = w[n] + sum_k a[k] y[n-1-k] on s = (y[n], ..., y[n-na+1])
+    // companion matrix of y[n] = w[n] + sum_k a[k] y[n-1-k] on s = (y[n], ..., y[n-cap+1])
     CMat A{};
     for (int k = 0; k < na; k++) {
       A.v[0][k][0] = p.a[k][0];
       A.v[0][k][1] = p.a[k][1];
     }
-    for (int i = 1; i < na; i++) A.v[i][i - 1][0] = 1.0;
+    for (int i = 1; i < cap; i++) A.v[i][i - 1][0] = 1.0;
     CMat M = A;
     for (int i = 0; i < 5; i++) M = cmat_mul(M, M);  // A^32
     for (int lv = 0; lv < 9; lv++) {
@@ -496,18 +493,21 @@ int filter_fp(const gbfir_buf &out, const gbfir_buf &in, const void *a, int na, 
       for (int lv = 0; lv < 9; lv++)
         for (int j = 0; j < kIirMaxCoef; j++) p.fmpow[lv][i][j][c] = (float)p.mpow[lv][i][j][c];
     }
-  const bool oc = dtype_complex(out.dtype), xc = dtype_complex(in.dtype);
-  if (dtype_double(in.dtype)) {
-    if (xc && cc) return launch_filter<double, true, true, true>(p, s);
-    if (xc) return launch_filter<double, true, true, false>(p, s);
-    if (cc) return launch_filter<double, false, true, true>(p, s);
-    return launch_filter<double, false, false, false>(p, s);
-  }
-  if (xc && cc) return launch_filter<float, true, true, true>(p, s);
-  if (xc) return launch_filter<float, true, true, false>(p, s);
-  if (cc) return launch_filter<float, false, true, true>(p, s);
-  (void)oc;
-  return launch_filter<float, false, false, false>(p, s);
+  const bool xc = dtype_complex(in.dtype);
+  auto go = [&](auto capv) -> int {
+    constexpr int C = decltype(capv)::value;
+    if (dtype_double(in.dtype)) {
+      if (xc && cc) return launch_filter<double, true, true, true, C>(p, s);
+      if (xc) return launch_filter<double, true, true, false, C>(p, s);
+      if (cc) return launch_filter<double, false, true, true, C>(p, s);
+      return launch_filter<double, false, false, false, C>(p, s);
+    }
+    if (xc && cc) return launch_filter<float, true, true, true, C>(p, s);
+    if (xc) return launch_filter<float, true, true, false, C>(p, s);
+    if (cc) return launch_filter<float, false, true, true, C>(p, s);
+    return launch_filter<float, false, false, false, C>(p, s);
+  };
+  return cap == 2 ? go(std::integral_constant<int, 2>{}) : go(std::integral_constant<int, 4>{});
 }
 
 }  // namespace gbfir
