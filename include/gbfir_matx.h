@@ -6,10 +6,14 @@
 //     (y   = matx::conv1d(x, h, MATX_C_MODE_FULL)).run(exec);
 //     (y   = matx::corr(x, h, MATX_C_MODE_FULL, MATX_C_METHOD_DIRECT)).run(exec);
 //     (Y   = matx::channelize_poly(x, h, M, D)).run(exec);
+//     (y   = matx::filter(x, h_rec, h_nonrec)).run(exec);
 //
 // How: MatX's operator classes call resample_poly_impl / conv1d_impl / corr_impl /
-// channelize_poly_impl unqualified from their Exec() (operators/resample_poly.h:113-120,
-// operators/conv.h:178-188, operators/corr.h:170-180, operators/channelize_poly.h:117-134).
+// channelize_poly_impl / filter_impl unqualified from their Exec() (operators/resample_poly.h:
+// 113-120, operators/conv.h:178-188, operators/corr.h:170-180, operators/channelize_poly.h:
+// 117-134, operators/filter.h:97-101).  conv1d / corr of a 1-D filter over a view whose last
+// dimension is strided (conv1d with an axis, or a permuted view as in the radar
+// three-pulse canceller) run in place of the view's layout (gbfir_conv1d_axis).
 // This header adds, in namespace matx, overloads with the same parameter lists and
 // stronger constraints — a CUDA executor and MatX tensor operands of float, double,
 // complex<float> or complex<double> — so C++20 overload resolution selects them (the
@@ -117,6 +121,76 @@ struct Staged {
 
 inline gbfir_stream_t stream_of(cudaStream_t s) { return reinterpret_cast<gbfir_stream_t>(s); }
 
+// A rank >= 2 operand whose last dimension is strided, as signals
+// x[o*ostride + n*step + i]: one unit-stride inner dimension, the others folding into one outer
+// stride (MatX's permuted views, e.g. the radar three-pulse canceller's).
+struct AxisLayout {
+  gbfir_buf buf{};
+  index_t inner = 1, step = 1;
+  int inner_dim = -1, nouter = 0, outer_dims[8] = {};
+};
+template <typename Op>
+bool describe_axis(const Op &t, AxisLayout &l) {
+  constexpr int R = remove_cvref_t<Op>::Rank();
+  if constexpr (R < 2 || R > 9) {
+    return false;
+  } else {
+    if (t.Size(R - 1) <= 1 || t.Stride(R - 1) == 1) return false;
+    l.step = t.Stride(R - 1);
+    l.inner_dim = -1;
+    for (int i = R - 2; i >= 0; i--)
+      if (t.Size(i) > 1 && t.Stride(i) == 1) {
+        l.inner_dim = i;
+        break;
+      }
+    if (l.inner_dim < 0) return false;
+    l.nouter = 0;
+    for (int i = 0; i < R - 1; i++)
+      if (i != l.inner_dim && t.Size(i) > 1) l.outer_dims[l.nouter++] = i;
+    for (int a = 1; a < l.nouter; a++)  // by stride, largest first
+      for (int c = a; c > 0 && t.Stride(l.outer_dims[c]) > t.Stride(l.outer_dims[c - 1]); c--) {
+        const int tmp = l.outer_dims[c];
+        l.outer_dims[c] = l.outer_dims[c - 1];
+        l.outer_dims[c - 1] = tmp;
+      }
+    index_t outer = 1;
+    for (int a = 0; a < l.nouter; a++) {
+      outer *= t.Size(l.outer_dims[a]);
+      if (a + 1 < l.nouter &&
+          t.Stride(l.outer_dims[a]) != t.Stride(l.outer_dims[a + 1]) * t.Size(l.outer_dims[a + 1]))
+        return false;
+    }
+    l.inner = t.Size(l.inner_dim);
+    l.buf.ptr = const_cast<void *>(static_cast<const void *>(t.Data()));
+    l.buf.batch = outer;
+    l.buf.len = t.Size(R - 1);
+    l.buf.batch_stride = outer > 1 ? t.Stride(l.outer_dims[l.nouter - 1]) : 0;
+    l.buf.dtype = dtype_of<typename remove_cvref_t<Op>::value_type>();
+    return true;
+  }
+}
+
+// conv1d / corr of a 1-D filter along a strided last dimension, in place of the views' layout;
+// false when the operands do not have that form (the caller then stages them).
+template <typename OutputType, typename In1Type, typename In2Type, typename Executor>
+bool conv_axis(OutputType &o, const In1Type &i1, const In2Type &i2, matxConvCorrMode_t mode, int is_corr,
+               const Executor &exec) {
+  if constexpr (remove_cvref_t<In2Type>::Rank() != 1 ||
+                remove_cvref_t<In1Type>::Rank() != remove_cvref_t<OutputType>::Rank()) {
+    return false;
+  } else {
+    AxisLayout lo, li;
+    if (!describe_axis(o, lo) || !describe_axis(i1, li)) return false;
+    if (lo.inner_dim != li.inner_dim || lo.nouter != li.nouter) return false;
+    for (int a = 0; a < lo.nouter; a++)
+      if (lo.outer_dims[a] != li.outer_dims[a]) return false;
+    Staged<In2Type, Executor> h(i2, exec);
+    check(gbfir_conv1d_axis(lo.buf, li.buf, h.buf, li.inner, li.step, lo.step, static_cast<int32_t>(mode),
+                            is_corr, GBFIR_PREC_FP32, stream_of(exec.getStream())));
+    return true;
+  }
+}
+
 }  // namespace gbfir_shim
 
 // ---- resample_poly ------------------------------------------------------------------
@@ -162,6 +236,7 @@ inline void conv1d_impl(OutputType o, const In1Type &i1, const In2Type &i2, matx
     }
     return;
   }
+  if (gbfir_shim::conv_axis(o, i1, i2, mode, 0, exec)) return;  // strided-axis views, no transpose
   gbfir_shim::Staged<OutputType, Executor> out(o, exec);
   gbfir_shim::Staged<In1Type, Executor> a(i1, exec);
   gbfir_shim::Staged<In2Type, Executor> b(i2, exec);
@@ -178,11 +253,38 @@ template <typename OutputTensor, typename In1Type, typename In2Type, typename Ex
 __MATX_INLINE__ void corr_impl(OutputTensor o, const In1Type i1, const In2Type i2, matxConvCorrMode_t mode,
                                [[maybe_unused]] matxConvCorrMethod_t method, const Executor &exec) {
   MATX_NVTX_START("gbfir corr", matx::MATX_NVTX_LOG_API)
+  if (gbfir_shim::conv_axis(o, i1, i2, mode, 1, exec)) return;
   gbfir_shim::Staged<OutputTensor, Executor> out(o, exec);
   gbfir_shim::Staged<In1Type, Executor> a(i1, exec);
   gbfir_shim::Staged<In2Type, Executor> b(i2, exec);
   gbfir_shim::check(gbfir_conv1d(out.buf, a.buf, b.buf, static_cast<int32_t>(mode), 1, GBFIR_PREC_FP32,
                                  gbfir_shim::stream_of(exec.getStream())));
+  if (out.buf.ptr != static_cast<const void *>(o.Data())) (o = out.tmp).run(exec);
+}
+
+// ---- filter() --------------------------------------------------------------------------------
+// Replaces transforms/filter.h:456-495: without recursive coefficients conv1d SAME
+// (filter.h:185), else the recursive filter, with a workspace from MatX's allocator.
+template <size_t NR, size_t NNR, typename OutType, typename InType, typename FilterType>
+  requires gbfir_shim::routable_tensor<OutType> && gbfir_shim::routable_tensor<InType> &&
+           (gbfir_shim::dtype_of<FilterType>() >= 0) && (NR <= 4) && (NNR >= 1) && (NNR <= 4)
+void filter_impl(OutType &o, const InType &i, const cuda::std::array<FilterType, NR> h_rec,
+                 const cuda::std::array<FilterType, NNR> h_nonrec, const cudaExecutor &exec) {
+  MATX_NVTX_START("gbfir filter", matx::MATX_NVTX_LOG_API)
+  gbfir_shim::Staged<OutType, cudaExecutor> out(o, exec);
+  gbfir_shim::Staged<InType, cudaExecutor> x(i, exec);
+  const cudaStream_t stream = exec.getStream();
+  void *ws = nullptr;
+  size_t need = 0;
+  if constexpr (NR > 0) {
+    need = gbfir_filter_workspace_size(out.buf.batch, x.buf.len, out.buf.dtype);
+    matxAlloc(&ws, need, MATX_ASYNC_DEVICE_MEMORY, stream);
+  }
+  const int rc = gbfir_filter(out.buf, x.buf, NR > 0 ? static_cast<const void *>(h_rec.data()) : nullptr,
+                              static_cast<int32_t>(NR), h_nonrec.data(), static_cast<int32_t>(NNR),
+                              gbfir_shim::dtype_of<FilterType>(), ws, need, gbfir_shim::stream_of(stream));
+  if (ws != nullptr) matxFree(ws, stream);
+  gbfir_shim::check(rc);
   if (out.buf.ptr != static_cast<const void *>(o.Data())) (o = out.tmp).run(exec);
 }
 

@@ -16,8 +16,10 @@
 // the powers M^(2^k), which the host forms in FP64.  Three launches, none waiting on
 // another CTA: (1) each CTA's zero-entry final state; (2) per row, the carries into each
 // CTA, in order (M^256 per CTA); (3) each CTA rescans with its carry and writes y.  x is
-// read twice and y written once; each thread holds its 32 samples in registers (16-byte
-// loads and stores; the lines a warp touches are reused from L1 across its 8 loads).
+// read twice and y written once; the CTA's window comes in and goes out as coalesced
+// 16-byte accesses through a padded shared buffer, each thread holds its 32 samples in
+// registers, and the kernels run 2 or 4 coefficients of each kind (zero-padded), fixed at
+// compile time, so no per-sample test is issued.
 #include <cstring>
 
 #include "common.cuh"

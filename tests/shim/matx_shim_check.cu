@@ -1,7 +1,8 @@
 // matx_shim_check.cu — MatX user code, unchanged, routed to libgbfir by gbfir_matx.h.
 //
 // Built by tests/test_shim.py where the MatX headers exist.  The object must
-// reference gbfir_resample_poly / gbfir_conv1d / gbfir_channelize_poly: that
+// reference gbfir_resample_poly / gbfir_conv1d / gbfir_channelize_poly /
+// gbfir_conv1d_axis / gbfir_filter: that
 // proves MatX's own operator classes resolved their *_impl calls to the
 // gbfir overloads.  Run on a GPU host with MatX, it also compares every result
 // with MatX's HostExecutor and returns non-zero on a mismatch.
@@ -58,11 +59,55 @@ int main() {
   auto zr = make_tensor<cuda::std::complex<float>>({B, T, M}, MATX_MANAGED_MEMORY);
   (z = channelize_poly(x, hc, M, M)).run(exec);
   (zr = channelize_poly(x, hc, M, M)).run(host);
+  // radar three-pulse canceller: conv1d SAME over the pulses of a permuted cube
+  // (examples/simple_radar_pipeline.h:321-327); runs on the strided view, no transpose
+  const index_t C = 2, P = 16, S = 300;
+  auto cube = make_tensor<cuda::std::complex<float>>({C, P, S}, MATX_MANAGED_MEMORY);
+  auto tpc = make_tensor<cuda::std::complex<float>>({C, P, S}, MATX_MANAGED_MEMORY);
+  auto tpcr = make_tensor<cuda::std::complex<float>>({C, S, P}, MATX_MANAGED_MEMORY);
+  auto mask = make_tensor<cuda::std::complex<float>>({3}, MATX_MANAGED_MEMORY);
+  mask(0) = {1.f, 0.f};
+  mask(1) = {-2.f, 0.f};
+  mask(2) = {1.f, 0.f};
+  for (index_t a = 0; a < C; a++)
+    for (index_t p = 0; p < P; p++)
+      for (index_t q = 0; q < S; q++) cube(a, p, q) = {float((a + 3 * p + 5 * q) % 9) - 4.f, float((p * q) % 7) - 3.f};
+  auto xv = cube.Permute({0, 2, 1});
+  auto ov = tpc.Permute({0, 2, 1});
+  (ov = conv1d(xv, mask, MATX_C_MODE_SAME)).run(exec);
+  (tpcr = conv1d(xv, mask, MATX_C_MODE_SAME)).run(host);
+
+  // filter(): the reference test's second-order section
+  auto fx = make_tensor<float>({B, N}, MATX_MANAGED_MEMORY);
+  auto fy = make_tensor<float>({B, N}, MATX_MANAGED_MEMORY);
+  for (index_t b = 0; b < B; b++)
+    for (index_t i = 0; i < N; i++) fx(b, i) = float(((i + 11 * b) % 23) - 11) / 7.f;
+  const cuda::std::array<float, 2> h_rec{0.4f, -0.1f}, h_nonrec{2.0f, 1.0f};
+  (fy = filter(fx, h_rec, h_nonrec)).run(exec);
   exec.sync();
+
+  double e5 = 0;
+  for (index_t a = 0; a < C; a++)
+    for (index_t q = 0; q < S; q++)
+      for (index_t p = 0; p < P; p++) {
+        const double d = cuda::std::abs(tpc(a, p, q) - tpcr(a, q, p));
+        e5 = d > e5 ? d : e5;
+      }
+  double e6 = 0;  // the recurrence in double, sequentially
+  for (index_t b = 0; b < B; b++) {
+    double y1 = 0, y2 = 0;
+    for (index_t i = 0; i < N; i++) {
+      const double y = 2.0 * fx(b, i) + (i ? 1.0 * fx(b, i - 1) : 0.0) + 0.4 * y1 - 0.1 * y2;
+      y2 = y1;
+      y1 = y;
+      const double d = cuda::std::abs(fy(b, i) - y);
+      e6 = d > e6 ? d : e6;
+    }
+  }
 
   const double e1 = max_abs_diff(y, yr, B * olen), e2 = max_abs_diff(c, cr, B * (N + L - 1));
   const double e3 = max_abs_diff(r, rr, B * N), e4 = max_abs_diff(z, zr, B * T * M);
-  printf("resample %g conv %g corr %g channelize %g launches %llu\n", e1, e2, e3, e4,
-         (unsigned long long)gbfir_launch_count());
-  return (e1 < 1e-3 && e2 < 1e-3 && e3 < 1e-3 && e4 < 1e-2) ? 0 : 1;
+  printf("resample %g conv %g corr %g channelize %g canceller %g filter %g launches %llu\n", e1, e2, e3, e4, e5,
+         e6, (unsigned long long)gbfir_launch_count());
+  return (e1 < 1e-3 && e2 < 1e-3 && e3 < 1e-3 && e4 < 1e-2 && e5 < 1e-4 && e6 < 1e-2) ? 0 : 1;
 }

@@ -24,5 +24,6 @@ def test_shim_routes_matx_operators(tmp_path):
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-3000:]
     syms = subprocess.run(["nm", "-u", str(obj)], capture_output=True, text=True).stdout
-    for name in ("gbfir_resample_poly", "gbfir_conv1d", "gbfir_channelize_poly"):
+    for name in ("gbfir_resample_poly", "gbfir_conv1d", "gbfir_channelize_poly", "gbfir_conv1d_axis",
+                 "gbfir_filter"):
         assert name in syms, f"{name} not referenced: MatX's operator did not route to the shim"
