@@ -431,6 +431,46 @@ def run_upfirdn(args, rank, world, dev):
     return 0
 
 
+def run_conv_fft(args, rank, world, dev):
+    """FFT-method conv1d SAME of 8 x 2^20 c64 with a 4096-tap Kaiser low-pass, beside the
+    direct method on the same data; the value counts the direct form's MACs (N*L per row)."""
+    import torch
+    from scipy import signal
+    import matx_gb300 as mx
+    B, N, L = 8, 1 << 20, 4096
+    g = torch.Generator(device=dev).manual_seed(81 + rank)
+    x = torch.randn(B, N, dtype=torch.complex64, device=dev, generator=g)
+    h = torch.from_numpy(signal.firwin(L, 0.1, window=("kaiser", 5.0)).astype(np.float32)).to(dev)
+    y = torch.empty(B, N, dtype=torch.complex64, device=dev)
+    flushbuf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    steps = max(3, min(args.steps, 50))
+    run = lambda: mx.conv1d(x, h, "same", out=y, method="fft")
+    for _ in range(args.warmup):
+        run()
+    l0 = mx.launch_count()
+    ms = _timed(run, steps, lambda: _flush_l2(flushbuf), stream)
+    launches = mx.launch_count() - l0
+    yd = torch.empty_like(y)
+    rund = lambda: mx.conv1d(x, h, "same", out=yd)
+    rund()
+    ms_direct = _timed(rund, 3, lambda: _flush_l2(flushbuf), stream)
+    rel = float(torch.linalg.vector_norm(y - yd) / torch.linalg.vector_norm(yd))
+    macs = B * N * L
+    nbytes = B * N * 8 * 2 + 4 * L
+    line = {"metric": "conv1d FFT method GMAC/s (direct-form MACs, c64 x 4096-tap real, SAME)",
+            "value": macs / (ms * 1e-3) / 1e9, "unit": "GMAC/s", "n_gpus": world, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded complex Gaussian; Kaiser low-pass)",
+            "config": {"workload": "conv1d SAME 8x2^20 c64, 4096 taps, MATX_C_METHOD_FFT (overlap-save, 8192-point)",
+                       "l2": "flushed (256 MB write) before every timed launch"},
+            "hbm_frac": nbytes / (ms * 1e-3) / 1e9 / _peak(), "direct_ms": ms_direct, "vs_direct": ms_direct / ms,
+            "rel_l2_vs_direct": rel, "gpu_launches": launches}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_channelize(args, rank, world, dev):
     """channelize_poly c64, maximally decimated: 4 rows x 2^24 samples, M = 64 with a
     64x32 Kaiser sinc prototype and M = 256 with 16 taps per channel; FP32 and the
@@ -674,7 +714,8 @@ def main():
                          "(rows_per_thread, col_warps, group, buffers [+4: TMA-store epilogue]; profiling cases)")
     ap.add_argument("--ratios", default="3/2,4/5,160/147", help="comma-separated up/down list (profiling cases)")
     ap.add_argument("--workload", default="resample",
-                    choices=["resample", "ragged", "conv1d", "channelize", "fwdbwd", "mti", "filter", "upfirdn"],
+                    choices=["resample", "ragged", "conv1d", "channelize", "fwdbwd", "mti", "filter", "upfirdn",
+                             "conv_fft"],
                     help="secondary workloads, each printing its own JSON line: ragged (4096 uneven signals "
                          "in one persistent launch), conv1d (8x2^20 FULL), channelize (4x2^24, M=64/256), "
                          "fwdbwd (256x16384 forward + backward)")
@@ -704,6 +745,8 @@ def main():
         return run_conv1d(args, rank, world, dev)
     if args.workload == "channelize":
         return run_channelize(args, rank, world, dev)
+    if args.workload == "conv_fft":
+        return run_conv_fft(args, rank, world, dev)
     if args.workload == "filter":
         return run_filter(args, rank, world, dev)
     if args.workload == "upfirdn":

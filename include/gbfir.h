@@ -10,6 +10,7 @@
  *                          include/matx/transforms/conv.h:402-451 (operand swap)
  *                          include/matx/transforms/conv.h:175-224 (direct CUDA path)
  *                          include/matx/transforms/corr.h:60-69   (corr = conv with reverse(conj(h)))
+ *   gbfir_conv1d_fft       include/matx/transforms/conv.h:51-172 (the FFT method)
  *   gbfir_conv1d_axis      include/matx/operators/conv.h:263-274 (conv1d with an axis)
  *   gbfir_upsample / gbfir_downsample   include/matx/operators/updownsample.h:254-279
  *   gbfir_upfirdn          downsample(conv1d(upsample(.)), .) of the same operators
@@ -120,6 +121,15 @@ typedef struct gbfir_buf {
  *  returns GBFIR_ERR_NOT_SUPPORTED for other operands. */
 GBFIR_API int gbfir_conv1d(gbfir_buf out, gbfir_buf in, gbfir_buf h, int32_t mode,
                  int32_t is_corr, int32_t precision, gbfir_stream_t stream);
+
+/* FFT-method conv1d / corr (MatX MATX_C_METHOD_FFT, include/matx/transforms/conv.h:51-172):
+ *  the same outputs as gbfir_conv1d up to FP32 rounding, computed by overlap-save with
+ *  transforms of 1024..8192 points in shared memory.  float32 / complex64 operands, h one
+ *  row of at most GBFIR_FFT_CONV_MAX_TAPS taps, the signal at least as long as the
+ *  filter; other operands return GBFIR_ERR_NOT_SUPPORTED. */
+#define GBFIR_FFT_CONV_MAX_TAPS 7169
+GBFIR_API int gbfir_conv1d_fft(gbfir_buf out, gbfir_buf in, gbfir_buf h, int32_t mode,
+                               int32_t is_corr, gbfir_stream_t stream);
 
 /* conv1d / corr along a strided axis.  Signal (b, i), b < out.batch, i < inner, is
  *  in[b*in.batch_stride + n*in_step + i], n < in.len (in.batch_stride 0 broadcasts one

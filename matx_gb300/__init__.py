@@ -176,8 +176,9 @@ def _conv1d_axis(x, h, m, a, out, corr):
 
 
 def conv1d(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torch.Tensor | None = None,
-           precision="fp32", axis: int = -1, _corr: bool = False) -> torch.Tensor:
-    """Direct 1-D convolution (MatX conv1d with MATX_C_METHOD_DIRECT).
+           precision="fp32", axis: int = -1, method="direct", _corr: bool = False) -> torch.Tensor:
+    """1-D convolution (MatX conv1d; ``method`` "direct" = MATX_C_METHOD_DIRECT, "fft" =
+    MATX_C_METHOD_FFT, the overlap-save FFT form for long filters, transforms/conv.h:51-172).
 
     Output length: N+L-1 (FULL), max(N,L) (SAME), max(N,L)-min(N,L)+1 (VALID).
     The operand with more dimensions sets the batch shape; a 1-D operand is
@@ -192,7 +193,11 @@ def conv1d(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torc
     """
     m = _mode(mode)
     nd = max(x.dim(), 1)
-    if x.dim() > 1 and h.dim() == 1 and x.is_cuda and _prec(precision) == 0:
+    if method not in ("direct", "fft"):
+        raise GbfirError(1, f"conv1d: unknown method {method!r}")
+    if method == "fft" and _prec(precision) != 0:
+        raise GbfirError(5, "conv1d: the FFT method is FP32 only")
+    if x.dim() > 1 and h.dim() == 1 and x.is_cuda and _prec(precision) == 0 and method == "direct":
         a = axis % nd
         if a != nd - 1 or x.stride(-1) != 1:
             return _conv1d_axis(x, h, m, a, out, _corr)
@@ -215,15 +220,19 @@ def conv1d(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torc
     odt = _out_dtype(x, h)
     if out is None:
         out = torch.empty(*batch_shape, olen, dtype=odt, device=x.device)
+    if method == "fft":
+        _lib.check(lib.gbfir_conv1d_fft(_buf(out, "conv1d out"), _buf(x, "conv1d x"), _buf(h, "conv1d h"),
+                                        m, int(_corr), _stream()))
+        return out
     _lib.check(lib.gbfir_conv1d(_buf(out, "conv1d out"), _buf(x, "conv1d x"), _buf(h, "conv1d h"),
                                 m, int(_corr), _prec(precision), _stream()))
     return out
 
 
 def corr(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torch.Tensor | None = None,
-         precision="fp32", axis: int = -1):
-    """Direct correlation: corr(x, h) = conv1d(x, reverse(conj(h))) (corr.h:67)."""
-    return conv1d(x, h, mode, out=out, precision=precision, axis=axis, _corr=True)
+         precision="fp32", axis: int = -1, method="direct"):
+    """Correlation: corr(x, h) = conv1d(x, reverse(conj(h))) (corr.h:67)."""
+    return conv1d(x, h, mode, out=out, precision=precision, axis=axis, method=method, _corr=True)
 
 
 def _along_last(x: torch.Tensor, dim: int):

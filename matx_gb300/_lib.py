@@ -51,6 +51,7 @@ _i32, _i64, _p, _sz = ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p, ctypes.c_
 SIGNATURES = [
     ("gbfir_conv1d", ctypes.c_int, [_B, _B, _B, _i32, _i32, _i32, _p]),
     ("gbfir_conv1d_axis", ctypes.c_int, [_B, _B, _B, _i64, _i64, _i64, _i32, _i32, _i32, _p]),
+    ("gbfir_conv1d_fft", ctypes.c_int, [_B, _B, _B, _i32, _i32, _p]),
     ("gbfir_upsample", ctypes.c_int, [_B, _B, _i64, _p]),
     ("gbfir_downsample", ctypes.c_int, [_B, _B, _i64, _p]),
     ("gbfir_upfirdn", ctypes.c_int, [_B, _B, _B, _i64, _i64, _i32, _i32, _p]),

@@ -18,6 +18,8 @@ int conv1d_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int
 int conv1d_axis_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t inner, int64_t in_step,
                    int64_t out_step, int mode, int is_corr, cudaStream_t s);
 int updown_fp(const gbfir_buf &out, const gbfir_buf &in, int64_t n, bool up, cudaStream_t s);
+int conv1d_fft_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int mode, int is_corr,
+                  cudaStream_t s);
 size_t filter_workspace_bytes(int64_t batch, int64_t len, int32_t out_dtype);
 int filter_fp(const gbfir_buf &out, const gbfir_buf &in, const void *a, int na, const void *b, int nb,
               int32_t coef_dtype, void *workspace, cudaStream_t s);
@@ -248,6 +250,35 @@ int gbfir_filter(gbfir_buf out, gbfir_buf in, const void *h_rec, int32_t num_rec
                      reinterpret_cast<cudaStream_t>(stream));
   } catch (...) {
     GBFIR_FAIL(GBFIR_ERR_CUDA, "filter: internal exception");
+  }
+}
+
+int gbfir_conv1d_fft(gbfir_buf out, gbfir_buf in, gbfir_buf h, int32_t mode, int32_t is_corr,
+                     gbfir_stream_t stream) {
+  try {
+    GBFIR_TRY(check_buf(out, "conv1d (FFT) out", false));
+    GBFIR_TRY(check_buf(in, "conv1d (FFT) in", true));
+    GBFIR_TRY(check_buf(h, "conv1d (FFT) h", false));
+    GBFIR_TRY(check_types(out, in, h, "conv1d (FFT)", false));
+    if (dtype_double(in.dtype))
+      GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "conv1d (FFT): float32 / complex64 operands only");
+    if (mode < GBFIR_MODE_FULL || mode > GBFIR_MODE_VALID)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "conv1d (FFT): unknown mode %d", (int)mode);
+    if (h.batch != 1) GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "conv1d (FFT): the filter must be one row");
+    if (in.batch != 1 && in.batch != out.batch)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "conv1d (FFT): batch sizes do not match (out %lld, in %lld)",
+                 (long long)out.batch, (long long)in.batch);
+    if (in.len < h.len) GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "conv1d (FFT): the signal must be at least as long as the filter");
+    if (h.len > GBFIR_FFT_CONV_MAX_TAPS)
+      GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "conv1d (FFT): at most %d taps", (int)GBFIR_FFT_CONV_MAX_TAPS);
+    const int64_t want = mode == GBFIR_MODE_FULL ? in.len + h.len - 1 : mode == GBFIR_MODE_SAME ? in.len
+                                                                      : in.len - h.len + 1;
+    if (out.len != want)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "conv1d (FFT): output length %lld, expected %lld", (long long)out.len,
+                 (long long)want);
+    return conv1d_fft_fp(out, in, h, mode, is_corr != 0, reinterpret_cast<cudaStream_t>(stream));
+  } catch (...) {
+    GBFIR_FAIL(GBFIR_ERR_CUDA, "conv1d (FFT): internal exception");
   }
 }
 

@@ -146,6 +146,16 @@ def test_filter_validation(lib):
     assert f(buf(1000, batch=3, dtype=2), x) == 4           # mixed precision
 
 
+def test_conv_fft_validation(lib):
+    f = lambda o, i, h, mode=0: lib.gbfir_conv1d_fft(o, i, h, mode, 0, None)
+    assert f(buf(100, dtype=1), buf(64, dtype=1), buf(16, dtype=0)) == 3
+    assert f(buf(79, dtype=1), buf(64, dtype=1), buf(16, dtype=0), mode=3) == 1
+    assert f(buf(79, dtype=3), buf(64, dtype=3), buf(16, dtype=2)) == 5            # double: not built
+    assert f(buf(79, dtype=1), buf(64, dtype=1), buf(16, batch=2, dtype=0)) == 5   # batched filter
+    assert f(buf(20063, dtype=1), buf(12894, dtype=1), buf(7170, dtype=0)) == 5    # too many taps
+    assert f(buf(79, dtype=1), buf(16, dtype=1), buf(64, dtype=0)) == 5            # signal shorter
+
+
 def test_channelize_validation(lib):
     # D > M
     assert lib.gbfir_channelize_poly(buf(16 * 8), buf(128), buf(64, dtype=0), 8, 9, 0, None) == 1
