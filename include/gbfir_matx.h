@@ -18,8 +18,8 @@
 // stronger constraints — a CUDA executor and MatX tensor operands of float, double,
 // complex<float> or complex<double> — so C++20 overload resolution selects them (the
 // executor argument brings namespace matx into argument-dependent lookup).  Host
-// executors, operator expressions as inputs, the FFT conv method and other value types
-// keep MatX's own implementation.
+// executors, operator expressions as inputs, FFT convolutions outside the overlap-save
+// kernel's range and other value types keep MatX's own implementation.
 //
 // Each overload keeps the MatX transform's asserts and error classes: a gbfir_status
 // is rethrown as matxException with the matching matxError_t.  Tensors whose batch
@@ -220,7 +220,25 @@ inline void conv1d_impl(OutputType o, const In1Type &i1, const In2Type &i2, matx
                         matxConvCorrMethod_t method, const Executor &exec) {
   MATX_NVTX_START("gbfir conv1d", matx::MATX_NVTX_LOG_API)
   if (method != MATX_C_METHOD_DIRECT) {
-    // FFT method: MatX's own path (conv1d_impl_internal, transforms/conv.h:402-451), with
+    // FFT method: the overlap-save kernel for float / complex<float> rows and one filter row
+    // of at most GBFIR_FFT_CONV_MAX_TAPS taps no longer than the signal (gbfir_conv1d_fft)
+    using V1 = typename remove_cvref_t<In1Type>::value_type;
+    using V2 = typename remove_cvref_t<In2Type>::value_type;
+    constexpr bool single = (std::is_same_v<V1, float> || std::is_same_v<V1, cuda::std::complex<float>>) &&
+                            (std::is_same_v<V2, float> || std::is_same_v<V2, cuda::std::complex<float>>);
+    if constexpr (single && remove_cvref_t<In2Type>::Rank() == 1) {
+      const index_t n = i1.Size(remove_cvref_t<In1Type>::Rank() - 1), l = i2.Size(0);
+      if (n >= l && l <= GBFIR_FFT_CONV_MAX_TAPS) {
+        gbfir_shim::Staged<OutputType, Executor> out(o, exec);
+        gbfir_shim::Staged<In1Type, Executor> a(i1, exec);
+        gbfir_shim::Staged<In2Type, Executor> b(i2, exec);
+        gbfir_shim::check(gbfir_conv1d_fft(out.buf, a.buf, b.buf, static_cast<int32_t>(mode), 0,
+                                           gbfir_shim::stream_of(exec.getStream())));
+        if (out.buf.ptr != static_cast<const void *>(o.Data())) (o = out.tmp).run(exec);
+        return;
+      }
+    }
+    // otherwise MatX's own path (conv1d_impl_internal, transforms/conv.h:402-451), with
     // the lower-rank operand cloned across the batch as conv.h:467-532 does.
     constexpr int R1 = remove_cvref_t<In1Type>::Rank(), R2 = remove_cvref_t<In2Type>::Rank();
     if constexpr (R1 == R2) {

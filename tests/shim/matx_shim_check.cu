@@ -2,7 +2,7 @@
 //
 // Built by tests/test_shim.py where the MatX headers exist.  The object must
 // reference gbfir_resample_poly / gbfir_conv1d / gbfir_channelize_poly /
-// gbfir_conv1d_axis / gbfir_filter: that
+// gbfir_conv1d_axis / gbfir_filter / gbfir_conv1d_fft: that
 // proves MatX's own operator classes resolved their *_impl calls to the
 // gbfir overloads.  Run on a GPU host with MatX, it also compares every result
 // with MatX's HostExecutor and returns non-zero on a mismatch.
@@ -46,6 +46,8 @@ int main() {
   auto cr = make_tensor<cuda::std::complex<float>>({B, N + L - 1}, MATX_MANAGED_MEMORY);
   (c = conv1d(x, h, MATX_C_MODE_FULL)).run(exec);
   (cr = conv1d(x, h, MATX_C_MODE_FULL)).run(host);
+  auto cf = make_tensor<cuda::std::complex<float>>({B, N + L - 1}, MATX_MANAGED_MEMORY);
+  (cf = conv1d(x, h, MATX_C_MODE_FULL, MATX_C_METHOD_FFT)).run(exec);
   auto r = make_tensor<cuda::std::complex<float>>({B, N}, MATX_MANAGED_MEMORY);
   auto rr = make_tensor<cuda::std::complex<float>>({B, N}, MATX_MANAGED_MEMORY);
   (r = corr(x, h, MATX_C_MODE_SAME, MATX_C_METHOD_DIRECT)).run(exec);
@@ -107,7 +109,8 @@ int main() {
 
   const double e1 = max_abs_diff(y, yr, B * olen), e2 = max_abs_diff(c, cr, B * (N + L - 1));
   const double e3 = max_abs_diff(r, rr, B * N), e4 = max_abs_diff(z, zr, B * T * M);
-  printf("resample %g conv %g corr %g channelize %g canceller %g filter %g launches %llu\n", e1, e2, e3, e4, e5,
-         e6, (unsigned long long)gbfir_launch_count());
-  return (e1 < 1e-3 && e2 < 1e-3 && e3 < 1e-3 && e4 < 1e-2 && e5 < 1e-4 && e6 < 1e-2) ? 0 : 1;
+  const double e7 = max_abs_diff(cf, cr, B * (N + L - 1));
+  printf("resample %g conv %g corr %g channelize %g canceller %g filter %g fft-conv %g launches %llu\n", e1, e2,
+         e3, e4, e5, e6, e7, (unsigned long long)gbfir_launch_count());
+  return (e1 < 1e-3 && e2 < 1e-3 && e3 < 1e-3 && e4 < 1e-2 && e5 < 1e-4 && e6 < 1e-2 && e7 < 1e-3) ? 0 : 1;
 }
