@@ -471,6 +471,51 @@ def run_conv_fft(args, rank, world, dev):
     return 0
 
 
+def run_conv2d(args, rank, world, dev):
+    """conv2d SAME of 16 c64 images of 1024 x 1024 with a 16 x 8 c64 filter (the shape of the
+    reference's conv2d tests), seeded Gaussian data."""
+    import torch
+    import matx_gb300 as mx
+    B, H, W, FN, FM = 16, 1024, 1024, 16, 8
+    g = torch.Generator(device=dev).manual_seed(91 + rank)
+    x = torch.randn(B, H, W, dtype=torch.complex64, device=dev, generator=g)
+    h = torch.randn(FN, FM, dtype=torch.complex64, device=dev, generator=g)
+    y = torch.empty_like(x)
+    flushbuf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    steps = max(3, min(args.steps, 50))
+    run = lambda: mx.conv2d(x, h, "same", out=y)
+    for _ in range(args.warmup):
+        run()
+    l0 = mx.launch_count()
+    ms = _timed(run, steps, lambda: _flush_l2(flushbuf), stream)
+    launches = mx.launch_count() - l0
+    err = None
+    try:
+        import oracle
+        oracle.build()
+        xs = x[0, :96, :96].cpu().numpy().astype(np.complex128)
+        r = oracle.conv2d(xs, h.cpu().numpy().astype(np.complex128), 1)
+        # interior outputs of the crop agree with the full image's
+        got = y[0, :96, :96].cpu().numpy()[FN:-FN, FM:-FM]
+        err = float(np.linalg.norm(got - r[FN:-FN, FM:-FM]) / np.linalg.norm(r[FN:-FN, FM:-FM]))
+    except Exception as e:  # noqa: BLE001
+        err = {"unavailable": str(e)[:160]}
+    macs = B * H * W * FN * FM  # complex x complex, 4 real FMAs each
+    nbytes = 2 * B * H * W * 8
+    line = {"metric": "conv2d GMAC/s (c64 x c64, 16 x 8 filter, SAME)", "value": macs / (ms * 1e-3) / 1e9,
+            "unit": "GMAC/s", "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded complex Gaussian)",
+            "config": {"workload": "conv2d SAME 16 x 1024 x 1024 c64, 16 x 8 c64 filter",
+                       "l2": "flushed (256 MB write) before every timed launch"},
+            "fp32_tflops": 8 * macs / (ms * 1e-3) / 1e12, "hbm_frac": nbytes / (ms * 1e-3) / 1e9 / _peak(),
+            "rel_l2_vs_fp64_crop": err, "gpu_launches": launches}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_channelize(args, rank, world, dev):
     """channelize_poly c64, maximally decimated: 4 rows x 2^24 samples, M = 64 with a
     64x32 Kaiser sinc prototype and M = 256 with 16 taps per channel; FP32 and the
@@ -715,7 +760,7 @@ def main():
     ap.add_argument("--ratios", default="3/2,4/5,160/147", help="comma-separated up/down list (profiling cases)")
     ap.add_argument("--workload", default="resample",
                     choices=["resample", "ragged", "conv1d", "channelize", "fwdbwd", "mti", "filter", "upfirdn",
-                             "conv_fft"],
+                             "conv_fft", "conv2d"],
                     help="secondary workloads, each printing its own JSON line: ragged (4096 uneven signals "
                          "in one persistent launch), conv1d (8x2^20 FULL), channelize (4x2^24, M=64/256), "
                          "fwdbwd (256x16384 forward + backward)")
@@ -745,6 +790,8 @@ def main():
         return run_conv1d(args, rank, world, dev)
     if args.workload == "channelize":
         return run_channelize(args, rank, world, dev)
+    if args.workload == "conv2d":
+        return run_conv2d(args, rank, world, dev)
     if args.workload == "conv_fft":
         return run_conv_fft(args, rank, world, dev)
     if args.workload == "filter":

@@ -11,6 +11,7 @@
  *                          include/matx/transforms/conv.h:175-224 (direct CUDA path)
  *                          include/matx/transforms/corr.h:60-69   (corr = conv with reverse(conj(h)))
  *   gbfir_conv1d_fft       include/matx/transforms/conv.h:51-172 (the FFT method)
+ *   gbfir_conv2d           include/matx/transforms/conv.h:548-600 (conv2d_impl, direct)
  *   gbfir_conv1d_axis      include/matx/operators/conv.h:263-274 (conv1d with an axis)
  *   gbfir_upsample / gbfir_downsample   include/matx/operators/updownsample.h:254-279
  *   gbfir_upfirdn          downsample(conv1d(upsample(.)), .) of the same operators
@@ -106,6 +107,15 @@ typedef struct gbfir_buf {
   int32_t dtype;        /* gbfir_dtype                                       */
 } gbfir_buf;
 
+/* `batch` images of rows x cols elements: element (b, r, c) at
+ * ptr + b*batch_stride + r*row_stride + c (batch_stride 0 broadcasts image 0). */
+typedef struct gbfir_buf2d {
+  void *ptr;
+  int64_t batch, rows, cols;
+  int64_t batch_stride, row_stride;
+  int32_t dtype;
+} gbfir_buf2d;
+
 /* ---- forward operators ------------------------------------------------- */
 
 /* Direct 1-D convolution or correlation of every row of `in` with `h`.
@@ -121,6 +131,15 @@ typedef struct gbfir_buf {
  *  returns GBFIR_ERR_NOT_SUPPORTED for other operands. */
 GBFIR_API int gbfir_conv1d(gbfir_buf out, gbfir_buf in, gbfir_buf h, int32_t mode,
                  int32_t is_corr, int32_t precision, gbfir_stream_t stream);
+
+/* Direct conv2d of images with filters (MatX conv2d, include/matx/transforms/conv.h:548-600,
+ *  kernels/conv.cuh:210-402): out[oy][ox] = sum x[oy+fy-dy][ox+fx-dx] * h[N2-1-fy][M2-1-fx],
+ *  dy/dx = N2-1/M2-1 (FULL), N2/2, M2/2 (SAME), 0 (VALID); out rows/cols per axis
+ *  max+min-1 / max / max-min+1; the operand with more elements is the image (conv.h:569-576);
+ *  each operand one image or out.batch of them; out complex if either operand is.  Filters
+ *  up to 64 x 64 (GBFIR_ERR_NOT_SUPPORTED beyond). */
+GBFIR_API int gbfir_conv2d(gbfir_buf2d out, gbfir_buf2d in, gbfir_buf2d h, int32_t mode,
+                           gbfir_stream_t stream);
 
 /* FFT-method conv1d / corr (MatX MATX_C_METHOD_FFT, include/matx/transforms/conv.h:51-172):
  *  the same outputs as gbfir_conv1d up to FP32 rounding, computed by overlap-save with

@@ -7,6 +7,7 @@
 //     (y   = matx::corr(x, h, MATX_C_MODE_FULL, MATX_C_METHOD_DIRECT)).run(exec);
 //     (Y   = matx::channelize_poly(x, h, M, D)).run(exec);
 //     (y   = matx::filter(x, h_rec, h_nonrec)).run(exec);
+//     (z   = matx::conv2d(images, kernel, MATX_C_MODE_SAME)).run(exec);
 //
 // How: MatX's operator classes call resample_poly_impl / conv1d_impl / corr_impl /
 // channelize_poly_impl / filter_impl unqualified from their Exec() (operators/resample_poly.h:
@@ -276,6 +277,92 @@ __MATX_INLINE__ void corr_impl(OutputTensor o, const In1Type i1, const In2Type i
   gbfir_shim::Staged<In1Type, Executor> a(i1, exec);
   gbfir_shim::Staged<In2Type, Executor> b(i2, exec);
   gbfir_shim::check(gbfir_conv1d(out.buf, a.buf, b.buf, static_cast<int32_t>(mode), 1, GBFIR_PREC_FP32,
+                                 gbfir_shim::stream_of(exec.getStream())));
+  if (out.buf.ptr != static_cast<const void *>(o.Data())) (o = out.tmp).run(exec);
+}
+
+// ---- conv2d (direct) ------------------------------------------------------------------------
+// Replaces transforms/conv.h:548-600 for CUDA executors: images of the last two dimensions,
+// the leading ones folding into one batch stride (else MatX's elementwise copy into a
+// contiguous temporary first); filters up to 64 x 64 (larger: MatX's kernel).
+namespace gbfir_shim {
+template <typename Op>
+bool describe2d(const Op &t, gbfir_buf2d &b) {
+  constexpr int R = remove_cvref_t<Op>::Rank();
+  if constexpr (R < 2) {
+    return false;
+  } else {
+    if (t.Size(R - 1) > 1 && t.Stride(R - 1) != 1) return false;
+    index_t batch = 1;
+    for (int i = 0; i < R - 2; i++) batch *= t.Size(i);
+    index_t bstride = 0;
+    int inner = -1;
+    for (int i = R - 3; i >= 0; i--)
+      if (t.Size(i) > 1) {
+        inner = i;
+        break;
+      }
+    if (inner >= 0) {
+      bstride = t.Stride(inner);
+      index_t expect = bstride * t.Size(inner);
+      for (int i = inner - 1; i >= 0; i--) {
+        if (t.Size(i) == 1) continue;
+        if (t.Stride(i) != expect) return false;
+        expect *= t.Size(i);
+      }
+    }
+    b.ptr = const_cast<void *>(static_cast<const void *>(t.Data()));
+    b.batch = batch;
+    b.rows = t.Size(R - 2);
+    b.cols = t.Size(R - 1);
+    b.batch_stride = batch > 1 ? bstride : 0;
+    b.row_stride = t.Size(R - 2) > 1 ? t.Stride(R - 2) : t.Size(R - 1);
+    b.dtype = dtype_of<typename remove_cvref_t<Op>::value_type>();
+    return true;
+  }
+}
+template <typename Op, typename Executor>
+struct Staged2d {
+  using value_type = typename remove_cvref_t<Op>::value_type;
+  static constexpr int R = remove_cvref_t<Op>::Rank();
+  gbfir_buf2d buf{};
+  decltype(make_tensor<value_type>(cuda::std::array<index_t, R>{}, MATX_ASYNC_DEVICE_MEMORY,
+                                   cudaStream_t{})) tmp;
+  Staged2d(const Op &t, const Executor &exec) {
+    if (!describe2d(t, buf)) {
+      cuda::std::array<index_t, R> shape;
+      for (int i = 0; i < R; i++) shape[i] = t.Size(i);
+      (void)(tmp = make_tensor<value_type>(shape, MATX_ASYNC_DEVICE_MEMORY, exec.getStream()));
+      (tmp = t).run(exec);
+      (void)describe2d(tmp, buf);
+    }
+  }
+};
+}  // namespace gbfir_shim
+
+template <typename OutputType, typename In1Type, typename In2Type, typename Executor>
+  requires is_cuda_executor_v<Executor> && gbfir_shim::routable_tensor<OutputType> &&
+           gbfir_shim::routable_tensor<In1Type> && gbfir_shim::routable_tensor<In2Type> &&
+           (remove_cvref_t<In1Type>::Rank() >= 2) && (remove_cvref_t<In2Type>::Rank() >= 2)
+inline void conv2d_impl(OutputType o, const In1Type in1, const In2Type in2, matxConvCorrMode_t mode,
+                        const Executor &exec) {
+  MATX_NVTX_START("gbfir conv2d", matx::MATX_NVTX_LOG_API)
+  constexpr int R1 = remove_cvref_t<In1Type>::Rank(), R2 = remove_cvref_t<In2Type>::Rank();
+  const index_t n1 = in1.Size(R1 - 2) * in1.Size(R1 - 1), n2 = in2.Size(R2 - 2) * in2.Size(R2 - 1);
+  const index_t fil_rows = n1 >= n2 ? in2.Size(R2 - 2) : in1.Size(R1 - 2);
+  const index_t fil_cols = n1 >= n2 ? in2.Size(R2 - 1) : in1.Size(R1 - 1);
+  if constexpr (R1 == R2) {
+    // filters beyond the kernel's 64 x 64: MatX's own direct kernel (same operand order rule)
+    if (fil_rows > 64 || fil_cols > 64) {
+      if (n1 >= n2) detail::matxDirectConv2DInternal(o, in1, in2, mode, exec.getStream());
+      else detail::matxDirectConv2DInternal(o, in2, in1, mode, exec.getStream());
+      return;
+    }
+  }
+  gbfir_shim::Staged2d<OutputType, Executor> out(o, exec);
+  gbfir_shim::Staged2d<In1Type, Executor> a(in1, exec);
+  gbfir_shim::Staged2d<In2Type, Executor> b(in2, exec);
+  gbfir_shim::check(gbfir_conv2d(out.buf, a.buf, b.buf, static_cast<int32_t>(mode),
                                  gbfir_shim::stream_of(exec.getStream())));
   if (out.buf.ptr != static_cast<const void *>(o.Data())) (o = out.tmp).run(exec);
 }

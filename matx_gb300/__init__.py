@@ -30,7 +30,7 @@ _MODE_NAMES = {"full": 0, "same": 1, "valid": 2}
 __all__ = ["conv1d", "corr", "resample_poly", "channelize_poly", "GbfirError",
            "MATX_C_MODE_FULL", "MATX_C_MODE_SAME", "MATX_C_MODE_VALID", "launch_count",
            "resample_out_len", "set_resample_tile", "upsample", "downsample", "upfirdn", "filter",
-           "iir_filter"]
+           "iir_filter", "conv2d"]
 
 _DT = {torch.float32: _lib.GBFIR_F32, torch.complex64: _lib.GBFIR_C64,
        torch.float64: _lib.GBFIR_F64, torch.complex128: _lib.GBFIR_C128}
@@ -233,6 +233,48 @@ def corr(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torch.
          precision="fp32", axis: int = -1, method="direct"):
     """Correlation: corr(x, h) = conv1d(x, reverse(conj(h))) (corr.h:67)."""
     return conv1d(x, h, mode, out=out, precision=precision, axis=axis, method=method, _corr=True)
+
+
+def _buf2d(t: torch.Tensor, name: str) -> _lib.Buf2d:
+    """Images of the last two dimensions; the leading ones must fold into one batch stride."""
+    t = _rows(t, name)
+    if t.dim() < 2:
+        raise ValueError(f"{name}: needs at least two dimensions")
+    if t.stride(-1) != 1:
+        t = t.contiguous()
+    rows, cols = t.shape[-2], t.shape[-1]
+    batch = t.numel() // max(rows * cols, 1)
+    bstride = 0
+    if batch > 1:
+        flat = t.reshape(-1, rows, cols)
+        if flat.data_ptr() != t.data_ptr():
+            raise ValueError(f"{name}: leading dimensions must fold into one batch dimension")
+        bstride = flat.stride(0)
+    return _lib.Buf2d(t.data_ptr(), max(batch, 1), rows, cols, bstride, t.stride(-2) if rows > 1 else cols,
+                      _DT[t.dtype])
+
+
+def conv2d(x: torch.Tensor, h: torch.Tensor, mode=MATX_C_MODE_FULL, *, out: torch.Tensor | None = None):
+    """MatX conv2d (transforms/conv.h:548-600, direct): 2-D convolution of the last two
+    dimensions; sizes per axis max+min-1 (FULL), max (SAME), max-min+1 (VALID); the operand
+    with more elements is the image; either operand may be one image broadcast over the
+    other's batch."""
+    m = _mode(mode)
+    double = _out_dtype(x, h) in (torch.float64, torch.complex128)
+    x = _prep_in(_cast(x, double), "conv2d x")
+    h = _prep_in(_cast(h, double), "conv2d h")
+    if x.dim() < 2 or h.dim() < 2:
+        raise GbfirError(2, "conv2d: operands need at least two dimensions")
+    size = lambda a, b: (a + b - 1) if m == 0 else (max(a, b) if m == 1 else max(a, b) - min(a, b) + 1)
+    oshape = (*(x.shape[:-2] if x.dim() >= h.dim() else h.shape[:-2]),
+              size(x.shape[-2], h.shape[-2]), size(x.shape[-1], h.shape[-1]))
+    if x.dim() > 2 and h.dim() > 2 and x.shape[:-2] != h.shape[:-2]:
+        raise GbfirError(2, "conv2d: batched operands must have the same batch shape")
+    if out is None:
+        out = torch.empty(oshape, dtype=_out_dtype(x, h), device=x.device)
+    _lib.check(_lib.load().gbfir_conv2d(_buf2d(out, "conv2d out"), _buf2d(x, "conv2d x"), _buf2d(h, "conv2d h"),
+                                        m, _stream()))
+    return out
 
 
 def _along_last(x: torch.Tensor, dim: int):

@@ -35,6 +35,12 @@ class Buf(ctypes.Structure):
                 ("batch_stride", ctypes.c_int64), ("dtype", ctypes.c_int32)]
 
 
+class Buf2d(ctypes.Structure):
+    _fields_ = [("ptr", ctypes.c_void_p), ("batch", ctypes.c_int64), ("rows", ctypes.c_int64),
+                ("cols", ctypes.c_int64), ("batch_stride", ctypes.c_int64), ("row_stride", ctypes.c_int64),
+                ("dtype", ctypes.c_int32)]
+
+
 class RaggedDesc(ctypes.Structure):
     _fields_ = [("inp", ctypes.c_void_p), ("out", ctypes.c_void_p), ("h", ctypes.c_void_p),
                 ("in_len", ctypes.c_int64), ("out_len", ctypes.c_int64), ("h_len", ctypes.c_int32),
@@ -52,6 +58,7 @@ SIGNATURES = [
     ("gbfir_conv1d", ctypes.c_int, [_B, _B, _B, _i32, _i32, _i32, _p]),
     ("gbfir_conv1d_axis", ctypes.c_int, [_B, _B, _B, _i64, _i64, _i64, _i32, _i32, _i32, _p]),
     ("gbfir_conv1d_fft", ctypes.c_int, [_B, _B, _B, _i32, _i32, _p]),
+    ("gbfir_conv2d", ctypes.c_int, [Buf2d, Buf2d, Buf2d, _i32, _p]),
     ("gbfir_upsample", ctypes.c_int, [_B, _B, _i64, _p]),
     ("gbfir_downsample", ctypes.c_int, [_B, _B, _i64, _p]),
     ("gbfir_upfirdn", ctypes.c_int, [_B, _B, _B, _i64, _i64, _i32, _i32, _p]),

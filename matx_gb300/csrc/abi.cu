@@ -18,6 +18,7 @@ int conv1d_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int
 int conv1d_axis_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t inner, int64_t in_step,
                    int64_t out_step, int mode, int is_corr, cudaStream_t s);
 int updown_fp(const gbfir_buf &out, const gbfir_buf &in, int64_t n, bool up, cudaStream_t s);
+int conv2d_fp(const gbfir_buf2d &out, const gbfir_buf2d &x, const gbfir_buf2d &h, int mode, cudaStream_t s);
 int conv1d_fft_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int mode, int is_corr,
                   cudaStream_t s);
 size_t filter_workspace_bytes(int64_t batch, int64_t len, int32_t out_dtype);
@@ -250,6 +251,56 @@ int gbfir_filter(gbfir_buf out, gbfir_buf in, const void *h_rec, int32_t num_rec
                      reinterpret_cast<cudaStream_t>(stream));
   } catch (...) {
     GBFIR_FAIL(GBFIR_ERR_CUDA, "filter: internal exception");
+  }
+}
+
+static int check_buf2d(const gbfir_buf2d &b, const char *name, bool allow_broadcast) {
+  if (b.ptr == nullptr) GBFIR_FAIL(GBFIR_ERR_NULL_POINTER, "%s: null pointer", name);
+  const size_t es = dtype_size(b.dtype);
+  if (es == 0) GBFIR_FAIL(GBFIR_ERR_INVALID_TYPE, "%s: unknown dtype %d", name, (int)b.dtype);
+  if (b.batch < 1) GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "%s: batch must be >= 1", name);
+  if (b.rows < 1 || b.cols < 1) GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "%s: empty image", name);
+  const size_t align = (b.dtype == GBFIR_C128) ? 16 : es;
+  if (reinterpret_cast<uintptr_t>(b.ptr) % align)
+    GBFIR_FAIL(GBFIR_ERR_ALIGNMENT, "%s: pointer not aligned to %zu bytes", name, align);
+  if (b.rows > 1 && b.row_stride < b.cols)
+    GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "%s: row stride shorter than a row", name);
+  if (b.batch > 1 && b.batch_stride == 0 && !allow_broadcast)
+    GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "%s: zero batch stride is only allowed for inputs", name);
+  if (b.batch > 1 && b.batch_stride != 0 && b.batch_stride < (b.rows - 1) * b.row_stride + b.cols)
+    GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "%s: batch stride shorter than an image", name);
+  return GBFIR_SUCCESS;
+}
+
+int gbfir_conv2d(gbfir_buf2d out, gbfir_buf2d in, gbfir_buf2d h, int32_t mode, gbfir_stream_t stream) {
+  try {
+    GBFIR_TRY(check_buf2d(out, "conv2d out", false));
+    GBFIR_TRY(check_buf2d(in, "conv2d in", true));
+    GBFIR_TRY(check_buf2d(h, "conv2d h", true));
+    if (dtype_double(in.dtype) != dtype_double(h.dtype) || dtype_double(in.dtype) != dtype_double(out.dtype))
+      GBFIR_FAIL(GBFIR_ERR_INVALID_TYPE, "conv2d: operands must all be single or all be double precision");
+    const bool oc = dtype_complex(in.dtype) || dtype_complex(h.dtype);
+    if (dtype_complex(out.dtype) != oc)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_TYPE, "conv2d: output must be %s", oc ? "complex" : "real");
+    if (mode < GBFIR_MODE_FULL || mode > GBFIR_MODE_VALID)
+      GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "conv2d: unknown mode %d", (int)mode);
+    if ((in.batch != 1 && in.batch != out.batch) || (h.batch != 1 && h.batch != out.batch))
+      GBFIR_FAIL(GBFIR_ERR_INVALID_DIM, "conv2d: batch sizes do not match");
+    auto size = [&](int64_t a, int64_t b) {
+      const int64_t mx = std::max(a, b), mn = std::min(a, b);
+      return mode == GBFIR_MODE_FULL ? a + b - 1 : mode == GBFIR_MODE_SAME ? mx : mx - mn + 1;
+    };
+    if (out.rows != size(in.rows, h.rows) || out.cols != size(in.cols, h.cols))
+      GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "conv2d: output %lld x %lld, expected %lld x %lld", (long long)out.rows,
+                 (long long)out.cols, (long long)size(in.rows, h.rows), (long long)size(in.cols, h.cols));
+    // the operand with more elements is the image (transforms/conv.h:569-576)
+    const bool swap = in.rows * in.cols < h.rows * h.cols;
+    const gbfir_buf2d &img = swap ? h : in, &fil = swap ? in : h;
+    if (fil.rows > img.rows || fil.cols > img.cols)
+      GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "conv2d: the filter must fit inside the image along both axes");
+    return conv2d_fp(out, img, fil, mode, reinterpret_cast<cudaStream_t>(stream));
+  } catch (...) {
+    GBFIR_FAIL(GBFIR_ERR_CUDA, "conv2d: internal exception");
   }
 }
 

@@ -53,6 +53,8 @@ def lib():
             getattr(L, "oracle_resample_poly_bwd" + suf).argtypes = [
                 _p, _p, _p, _i64, _p, _i64, _p, _i64, _i64, _i64, _i64, _int]
             getattr(L, "oracle_iir_filter" + suf).argtypes = [_p, _p, _i64, _i64, _p, _int, _p, _int, _int, _int]
+            getattr(L, "oracle_conv2d" + suf).argtypes = [_p, _i64, _i64, _p, _i64, _i64, _i64, _p, _i64, _i64, _i64,
+                                                        _i64, _int, _int, _int]
             getattr(L, "oracle_conv1d_bwd" + suf).argtypes = [
                 _p, _p, _p, _i64, _p, _i64, _p, _i64, _i64, _int, _int]
         L.oracle_max_threads.restype = _int
@@ -190,6 +192,34 @@ def conv1d_bwd(gy, x, h, mode: int, nthreads: int = 1):
     if rc:
         raise ValueError(f"oracle_conv1d_bwd failed ({rc})")
     return dx, dh
+
+
+def conv2d(x, h, mode: int = 0, double: bool = True):
+    """MatX conv2d of images x [..., N1, M1] with h [N2, M2] (or one filter per image):
+    the larger image by element count is the signal (transforms/conv.h:569-576)."""
+    x = np.asarray(x)
+    h = np.asarray(h)
+    if h.shape[-2] * h.shape[-1] > x.shape[-2] * x.shape[-1]:
+        x, h = h, x
+    xc, hc = np.iscomplexobj(x), np.iscomplexobj(h)
+    rt = np.float64 if double else np.float32
+    ct = np.complex128 if double else np.complex64
+    bshape = x.shape[:-2] if x.ndim >= h.ndim else h.shape[:-2]
+    B = int(np.prod(bshape)) if len(bshape) else 1
+    xs = np.ascontiguousarray(np.broadcast_to(x, tuple(bshape) + x.shape[-2:]).reshape(B, *x.shape[-2:]),
+                              dtype=ct if xc else rt)
+    hs = np.ascontiguousarray(h.reshape(-1, *h.shape[-2:]), dtype=ct if hc else rt)
+    N1, M1 = xs.shape[-2:]
+    N2, M2 = hs.shape[-2:]
+    size = lambda a, b: (a + b - 1) if mode == 0 else (max(a, b) if mode == 1 else max(a, b) - min(a, b) + 1)
+    ON, OM = size(N1, N2), size(M1, M2)
+    out = np.empty((B, ON, OM), dtype=ct if (xc or hc) else rt)
+    rc = getattr(lib(), "oracle_conv2d" + _suffix(double))(
+        _ptr(out), ON, OM, _ptr(xs), N1 * M1, N1, M1, _ptr(hs), N2 * M2 if hs.shape[0] > 1 else 0, N2, M2, B,
+        mode, int(xc), int(hc))
+    if rc:
+        raise ValueError(f"oracle_conv2d failed ({rc})")
+    return out.reshape(tuple(bshape) + (ON, OM))
 
 
 def iir_filter(x, h_rec, h_nonrec, double: bool = True):

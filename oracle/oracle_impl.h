@@ -413,6 +413,64 @@ int FN(oracle_conv1d_bwd)(T *dx, T *dh, const T *gy, int64_t out_len,
 }
 
 /* ---------------------------------------------------------------------------
+ * Direct conv2d of `B` images [N1][M1] with filters [N2][M2] (h_bstride 0: one filter).
+ * Follows MatX's host loop include/matx/transforms/conv.h:325-395: per output
+ * (oy, ox), sum over fy (outer) and fx (inner) of x[oy+fy-dy][ox+fx-dx] *
+ * h[N2-1-fy][M2-1-fx] with detail::madd, x outside the image skipped, dy/dx =
+ * N2-1/M2-1 (FULL), N2/2, M2/2 (SAME), 0 (VALID); output sizes per axis
+ * max+min-1, max, max-min+1 (operators/conv.h:335-357).  The caller passes the
+ * larger image as x (conv.h:569-576 swaps by total size).
+ * ------------------------------------------------------------------------- */
+int FN(oracle_conv2d)(T *out, int64_t ON, int64_t OM, const T *x, int64_t x_bstride, int64_t N1, int64_t M1,
+                      const T *h, int64_t h_bstride, int64_t N2, int64_t M2, int64_t B, int mode, int xc, int hc) {
+  if (N1 <= 0 || M1 <= 0 || N2 <= 0 || M2 <= 0 || B <= 0) return 1;
+  int64_t dy = 0, dx = 0;
+  if (mode == 1) {
+    dy = N2 / 2;
+    dx = M2 / 2;
+  } else if (mode == 0) {
+    dy = N2 - 1;
+    dx = M2 - 1;
+  } else if (mode != 2) {
+    return 2;
+  }
+  const int oc = xc || hc;
+  for (int64_t b = 0; b < B; b++) {
+    const T *xb = x + b * x_bstride * (xc ? 2 : 1);
+    const T *hb = h + b * h_bstride * (hc ? 2 : 1);
+    T *ob = out + b * ON * OM * (oc ? 2 : 1);
+    for (int64_t oy = 0; oy < ON; oy++)
+      for (int64_t ox = 0; ox < OM; ox++) {
+        T sr = 0, si = 0;
+        for (int64_t fy = 0; fy < N2; fy++) {
+          const int64_t iy = oy + fy - dy;
+          if (iy < 0 || iy >= N1) continue;
+          for (int64_t fx = 0; fx < M2; fx++) {
+            const int64_t ix = ox + fx - dx;
+            if (ix < 0 || ix >= M1) continue;
+            const int64_t xi = iy * M1 + ix, hi = (N2 - 1 - fy) * M2 + (M2 - 1 - fx);
+            const T xr = xc ? xb[2 * xi] : xb[xi], xm = xc ? xb[2 * xi + 1] : 0;
+            const T hr = hc ? hb[2 * hi] : hb[hi], hm = hc ? hb[2 * hi + 1] : 0;
+            /* madd order (core/utils.h:165-210): re += xr hr; re -= xi hi; im += xi hr; im += xr hi */
+            sr += xr * hr;
+            sr -= xm * hm;
+            si += xm * hr;
+            si += xr * hm;
+          }
+        }
+        const int64_t o = oy * OM + ox;
+        if (oc) {
+          ob[2 * o] = sr;
+          ob[2 * o + 1] = si;
+        } else {
+          ob[o] = sr;
+        }
+      }
+  }
+  return 0;
+}
+
+/* ---------------------------------------------------------------------------
  * Recursive filter() (MatX filter(in, h_rec, h_nonrec) with h_rec non-empty):
  *   y[n] = sum_{j<nb} b[j] x[n-j] + sum_{k<na} a[k] y[n-1-k],  zero initial state,
  * one row at a time, in order.  This is the recurrence MatX's RecursiveFilter

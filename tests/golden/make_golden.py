@@ -8,9 +8,9 @@ Run once in a container where the MatX source tree is mounted (default
 
 Sources, all from the reference's own test suite:
 
-* conv.npz, resample.npz, channelize.npz — produced by the reference's numpy/scipy
-  generator classes (test/test_vectors/generators/00_transforms.py):
-  ``conv_operators`` (:14-36), ``resample_poly_operators`` (:119-158),
+* conv.npz, conv2d.npz, resample.npz, channelize.npz — produced by the reference's
+  numpy/scipy generator classes (test/test_vectors/generators/00_transforms.py):
+  ``conv_operators`` (:14-36), ``conv2d_operators`` (:38-52), ``resample_poly_operators`` (:119-158),
   ``channelize_poly_operators.channelize`` (:194-247) and
   ``.channelize_oversampled`` (:249-334).  Case shapes follow the reference's
   tests (test/00_transform/ConvCorr.cu:491-835, ResamplePoly.cu:304-529,
@@ -61,6 +61,21 @@ def make_conv(T):
         for k in ("a_op", "b_op", "conv_full", "conv_same", "conv_valid", "corr", "corr_swap"):
             out[f"{key}__{k}"] = np.asarray(r[k])
     np.savez_compressed(os.path.join(HERE, "conv.npz"), **out)
+    return len(cases)
+
+
+def make_conv2d(T):
+    out = {}
+    # ConvCorr.cu:520-830 — a 256 x 128 image against 16 x 8 (even) and 15 x 7 (odd) filters,
+    # float and complex; the swapped call conv2d(filter, image) (:783-787) uses the same vectors.
+    cases = [("f32", np.float32, 16, 8), ("c64", np.complex64, 15, 7), ("f64", np.float64, 16, 8)]
+    for i, (tag, dt, b0, b1) in enumerate(cases):
+        g = T.conv2d_operators(dt, [256, 128, b0, b1])
+        r = g.conv2d()
+        key = f"d{i}_{tag}_{b0}x{b1}"
+        for k in ("a_op", "b_op", "conv_full", "conv_same", "conv_valid"):
+            out[f"{key}__{k}"] = np.asarray(r[k])
+    np.savez_compressed(os.path.join(HERE, "conv2d.npz"), **out)
     return len(cases)
 
 
@@ -227,6 +242,7 @@ def main():
     print("grad refs", make_grad_refs())
     T = _gen()
     print("conv cases", make_conv(T))
+    print("conv2d cases", make_conv2d(T))
     print("resample cases", make_resample(T))
     print("channelize cases", make_channelize(T))
     print("harris", make_harris())

@@ -2,7 +2,7 @@
 //
 // Built by tests/test_shim.py where the MatX headers exist.  The object must
 // reference gbfir_resample_poly / gbfir_conv1d / gbfir_channelize_poly /
-// gbfir_conv1d_axis / gbfir_filter / gbfir_conv1d_fft: that
+// gbfir_conv1d_axis / gbfir_filter / gbfir_conv1d_fft / gbfir_conv2d: that
 // proves MatX's own operator classes resolved their *_impl calls to the
 // gbfir overloads.  Run on a GPU host with MatX, it also compares every result
 // with MatX's HostExecutor and returns non-zero on a mismatch.
@@ -79,6 +79,19 @@ int main() {
   (ov = conv1d(xv, mask, MATX_C_MODE_SAME)).run(exec);
   (tpcr = conv1d(xv, mask, MATX_C_MODE_SAME)).run(host);
 
+  // conv2d SAME of the 4 images (4 x 4096 viewed as 4 x 64 x 64) with a 5 x 3 filter
+  auto img = make_tensor<float>({B, 64, 64}, MATX_MANAGED_MEMORY);
+  auto k2 = make_tensor<float>({5, 3}, MATX_MANAGED_MEMORY);
+  auto c2 = make_tensor<float>({B, 64, 64}, MATX_MANAGED_MEMORY);
+  auto c2r = make_tensor<float>({B, 64, 64}, MATX_MANAGED_MEMORY);
+  for (index_t b = 0; b < B; b++)
+    for (index_t i = 0; i < 64; i++)
+      for (index_t j = 0; j < 64; j++) img(b, i, j) = float((i * 5 + j * 3 + b) % 17) - 8.f;
+  for (index_t i = 0; i < 5; i++)
+    for (index_t j = 0; j < 3; j++) k2(i, j) = float(i * 3 + j) / 7.f - 1.f;
+  (c2 = conv2d(img, k2, MATX_C_MODE_SAME)).run(exec);
+  (c2r = conv2d(img, k2, MATX_C_MODE_SAME)).run(host);
+
   // filter(): the reference test's second-order section
   auto fx = make_tensor<float>({B, N}, MATX_MANAGED_MEMORY);
   auto fy = make_tensor<float>({B, N}, MATX_MANAGED_MEMORY);
@@ -110,7 +123,9 @@ int main() {
   const double e1 = max_abs_diff(y, yr, B * olen), e2 = max_abs_diff(c, cr, B * (N + L - 1));
   const double e3 = max_abs_diff(r, rr, B * N), e4 = max_abs_diff(z, zr, B * T * M);
   const double e7 = max_abs_diff(cf, cr, B * (N + L - 1));
-  printf("resample %g conv %g corr %g channelize %g canceller %g filter %g fft-conv %g launches %llu\n", e1, e2,
-         e3, e4, e5, e6, e7, (unsigned long long)gbfir_launch_count());
-  return (e1 < 1e-3 && e2 < 1e-3 && e3 < 1e-3 && e4 < 1e-2 && e5 < 1e-4 && e6 < 1e-2 && e7 < 1e-3) ? 0 : 1;
+  const double e8 = max_abs_diff(c2, c2r, B * 64 * 64);
+  printf("resample %g conv %g corr %g channelize %g canceller %g filter %g fft-conv %g conv2d %g launches %llu\n",
+         e1, e2, e3, e4, e5, e6, e7, e8, (unsigned long long)gbfir_launch_count());
+  return (e1 < 1e-3 && e2 < 1e-3 && e3 < 1e-3 && e4 < 1e-2 && e5 < 1e-4 && e6 < 1e-2 && e7 < 1e-3 && e8 < 1e-3) ? 0
+                                                                                                          : 1;
 }

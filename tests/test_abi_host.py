@@ -156,6 +156,18 @@ def test_conv_fft_validation(lib):
     assert f(buf(79, dtype=1), buf(16, dtype=1), buf(64, dtype=0)) == 5            # signal shorter
 
 
+def test_conv2d_validation(lib):
+    from matx_gb300._lib import Buf2d
+    img = lambda r, c, b=1, dt=0, bs=None: Buf2d(FAKE, b, r, c, r * c if bs is None else bs, c, dt)
+    f = lambda o, i, h, mode=0: lib.gbfir_conv2d(o, i, h, mode, None)
+    assert f(img(101, 100), img(90, 90), img(11, 11)) == 3              # FULL is 100 x 100
+    assert f(img(100, 100), img(90, 90), img(11, 11), mode=4) == 1
+    assert f(img(90, 90, dt=1), img(90, 90), img(11, 11), mode=1) == 4  # real operands, complex out
+    assert f(img(90, 90), img(90, 90, b=2), img(11, 11), mode=1) == 2   # batch mismatch
+    assert f(img(90, 90, b=2, bs=10), img(90, 90, b=2), img(11, 11), mode=1) == 1  # batch stride too short
+    assert f(img(90, 65), img(90, 40), img(2, 65), mode=1) == 5         # filter wider than the image
+
+
 def test_channelize_validation(lib):
     # D > M
     assert lib.gbfir_channelize_poly(buf(16 * 8), buf(128), buf(64, dtype=0), 8, 9, 0, None) == 1

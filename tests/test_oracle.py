@@ -276,3 +276,26 @@ def test_oracle_iir_matches_lfilter(oracle_mod):
     x = rng.standard_normal((2, 500))
     assert np.array_equal(oracle_mod.iir_filter(x, [], [1.0, -2.0, 1.0]),
                           oracle_mod.conv1d(x, np.array([1.0, -2.0, 1.0]), 1))
+
+
+def test_oracle_conv2d_known_answer(oracle_mod):
+    # ConvCorr.cu:395-440: 3 x 3 ramp against [[1, 2], [3, 4]]
+    x = np.arange(1, 10, dtype=np.float64).reshape(3, 3)
+    h = np.array([[1.0, 2.0], [3.0, 4.0]])
+    full = np.array([[1, 4, 7, 6], [7, 23, 33, 24], [19, 53, 63, 42], [21, 52, 59, 36]], np.float64)
+    assert np.array_equal(oracle_mod.conv2d(x, h, 0), full)
+    assert np.array_equal(oracle_mod.conv2d(x, h, 1), full[:3, :3])
+    assert np.array_equal(oracle_mod.conv2d(x, h, 2), np.array([[23, 33], [53, 63]], np.float64))
+
+
+@pytest.mark.parametrize("case", sorted(load_cases("conv2d.npz")))
+def test_oracle_conv2d_matches_reference_vectors(oracle_mod, case):
+    c = load_cases("conv2d.npz")[case]
+    a, b = c["a_op"], c["b_op"]
+    tol = 1e-12 if a.dtype == np.float64 else 1e-5
+    for mode, key in ((0, "conv_full"), (1, "conv_same"), (2, "conv_valid")):
+        r = oracle_mod.conv2d(a, b, mode)
+        assert r.shape == c[key].shape, (mode, r.shape, c[key].shape)
+        assert rel_l2(r, c[key]) < tol, (case, mode)
+        # the swapped call conv2d(filter, image) gives the same result (ConvCorr.cu:783-787)
+        assert rel_l2(oracle_mod.conv2d(b, a, mode), c[key]) < tol

@@ -25,5 +25,5 @@ def test_shim_routes_matx_operators(tmp_path):
     assert r.returncode == 0, r.stderr[-3000:]
     syms = subprocess.run(["nm", "-u", str(obj)], capture_output=True, text=True).stdout
     for name in ("gbfir_resample_poly", "gbfir_conv1d", "gbfir_channelize_poly", "gbfir_conv1d_axis",
-                 "gbfir_filter", "gbfir_conv1d_fft"):
+                 "gbfir_filter", "gbfir_conv1d_fft", "gbfir_conv2d"):
         assert name in syms, f"{name} not referenced: MatX's operator did not route to the shim"
