@@ -6,7 +6,8 @@ the fastest:
 
   rows_per_thread (outputs per thread along the row direction)  1, 2, 4
   col_warps       (phases per CTA = 8 * col_warps per pass)     1, 2, 4, 8; 9..16 dividing
-                                                                the super-groups (one row slice)
+                                                                the super-groups (one row slice,
+                                                                1 or 2 rows per thread)
   group           (outputs per tile row = group * up)           multiples giving up*group % 4 == 0
   buffers         (prefetch the next input window or not)       1, 2; plus 4 to send the
                                                                 outputs through shared memory
@@ -65,14 +66,15 @@ def candidates(up: int, down: int, tma_store: bool = False):
                     continue
                 for nb in nbufs:
                     yield (rq, wc, grp, nb)
-    # one row slice of 9..16 column warps that divide the super-groups evenly (one row per
-    # thread): balanced warps where 1, 2, 4 or 8 leave some with an extra super-group
+    # one row slice of 9..16 column warps that divide the super-groups evenly (one or two
+    # rows per thread): balanced warps where 1, 2, 4 or 8 leave some with an extra super-group
     for grp in groups:
         nsg = (u * grp + 7) // 8
         for wc in range(9, 17):
             if nsg % wc == 0:
-                for nb in nbufs:
-                    yield (1, wc, grp, nb)
+                for rq in (1, 2):
+                    for nb in nbufs:
+                        yield (rq, wc, grp, nb)
 
 
 def _time(fn, reps: int) -> float:

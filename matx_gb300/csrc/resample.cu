@@ -31,10 +31,10 @@ static std::mutex g_tile_mu;
 static std::unordered_map<TileKey, TileChoice, TileKeyHash> g_tiles;
 
 static bool valid_tile(int rq, int wc, int group, int nbuf) {
-  // column warps: 1, 2, 4, 8 (8/wc row slices per CTA) or 9..16 (one row slice, rows per thread 1)
+  // column warps: 1, 2, 4, 8 (8/wc row slices per CTA) or 9..16 (one row slice, rows per thread 1 or 2)
   // buffers: 1 or 2 window buffers (0 = heuristic), plus 4 for the TMA-store epilogue
   const int nb = nbuf & 3;
-  return (rq == 0 || rq == 1 || rq == 2 || rq == 4) && (wc >= 0 && wc <= 16 && (wc <= 8 ? 8 % (wc ? wc : 1) == 0 : rq == 1)) &&
+  return (rq == 0 || rq == 1 || rq == 2 || rq == 4) && (wc >= 0 && wc <= 16 && (wc <= 8 ? 8 % (wc ? wc : 1) == 0 : rq <= 2)) &&
          group >= 0 && group <= 64 && (nbuf & ~7) == 0 && nb != 3;
 }
 

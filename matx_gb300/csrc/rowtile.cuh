@@ -383,9 +383,9 @@ __device__ __forceinline__ void rowtile_compute(const RsParams &p, const typenam
 }
 
 // 256 threads (8 warps) per CTA, or up to 512 (one row slice of 9..16 column warps) with one
-// row per thread.
+// or two rows per thread.
 template <typename T, bool XC, bool HC, int RQ, int PAD>
-__global__ void __launch_bounds__(RQ == 1 ? 512 : 256)
+__global__ void __launch_bounds__(RQ <= 2 ? 512 : 256)
     resample_rowtile(const RsParams p, const __grid_constant__ CUtensorMap omap) {
   using XT = typename val_of<T, XC>::type;
   using HT = typename val_of<T, HC>::type;
@@ -751,7 +751,8 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
     return tap_table_bytes<T, XC, HC>(geo.ncg, geo.span) + (size_t)nbuf * (size_t)alloc * sizeof(XT) + stg_bytes;
   };
   int rq = tc.rq > 0 ? tc.rq : 2;
-  if (sizeof(T) == 8 || threads > 256) rq = 1;
+  if (sizeof(T) == 8) rq = 1;
+  else if (threads > 256 && rq > 2) rq = 2;  // CTAs of 9-16 column warps: 1 or 2 rows per thread
   int nbuf = tc.nbuf > 0 ? tc.nbuf : 2;
   // two CTAs per SM: prefer double buffering, then fewer rows, then a single buffer
   while (smem_for(rq, nbuf) > 110 * 1024 && (rq > 1 || nbuf > 1)) {

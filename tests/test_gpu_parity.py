@@ -214,7 +214,8 @@ def test_resample_tile_overrides_agree(mx, orc):
         r = orc.resample_poly(x, h, up, down)
         try:
             for rq, wc, g, nb in ((1, 1, 0, 0), (4, 1, 0, 1), (2, 2, 0, 2), (1, 8, 0, 1), (2, 1, 2, 0),
-                                  (1, 4, 4, 2), (4, 2, 16, 1), (1, 10, 0, 1), (1, 12, 8, 2), (1, 16, 32, 1)):
+                                  (1, 4, 4, 2), (4, 2, 16, 1), (1, 10, 0, 1), (1, 12, 8, 2), (1, 16, 32, 1),
+                                  (2, 10, 0, 1), (2, 16, 32, 6)):
                 mx.set_resample_tile(rq, wc, g, nb)
                 y = host(mx.resample_poly(dev(x), dev(h), up, down))
                 assert rel_l2(y, r) < FP32_TOL, (up, down, rq, wc, g, nb)
