@@ -10,16 +10,14 @@
 //
 // Schedule (no MatX counterpart; MatX solves the recurrence with per-position correction
 // factors and a chained block carry): a CTA owns 8192 samples of one row, 32 per thread.
-// With the state s = (y[n], ..., y[n-na+1]) the recurrence is s[n] = A s[n-1] + w[n] e0, A
+// With the state s = (y[n], ..., y[n-c+1]) the recurrence is s[n] = A s[n-1] + w[n] e0, A
 // the companion matrix, so a thread's chunk maps its entry state e to M e + g (M = A^32,
-// g its zero-entry final state) and the CTA's 256 chunks combine by a Kogge-Stone scan with
-// the powers M^(2^k), which the host forms in FP64.  Three launches, none waiting on
-// another CTA: (1) each CTA's zero-entry final state; (2) per row, the carries into each
-// CTA, in order (M^256 per CTA); (3) each CTA rescans with its carry and writes y.  x is
-// read twice and y written once; the CTA's window comes in and goes out as coalesced
-// 16-byte accesses through a padded shared buffer, each thread holds its 32 samples in
-// registers, and the kernels run 2 or 4 coefficients of each kind (zero-padded), fixed at
-// compile time, so no per-sample test is issued.
+// g its zero-entry final state); the CTA's 256 chunks combine by a Kogge-Stone scan with the
+// powers M^(2^k), which the host forms in FP64, and the CTAs of a row by chained carries in
+// one pass (iir_onepass below): x is read once and y written once.  The window comes in and
+// goes out as coalesced 16-byte accesses through a padded shared buffer, each thread holds
+// its 32 samples in registers, and the kernels run 2 or 4 coefficients of each kind
+// (zero-padded), fixed at compile time, so no per-sample test is issued.
 #include <cstring>
 
 #include "common.cuh"
@@ -30,6 +28,7 @@ constexpr int kIirThreads = 256;
 constexpr int kIirChunk = 32;                        // samples per thread
 constexpr int kIirBlock = kIirThreads * kIirChunk;   // samples per CTA
 constexpr int kIirMaxCoef = 4;
+constexpr int kIirPowers = 14;  // M^(2^k), k < 14: chunk scans (k < 8), CTAs (8), look-back windows (8..13)
 
 struct IirParams {
   const void *x;
@@ -39,9 +38,9 @@ struct IirParams {
   int64_t batch, nblk;
   int32_t na, nb, xc;      // xc: the input is complex
   double a[kIirMaxCoef][2], b[kIirMaxCoef][2];
-  double mpow[9][kIirMaxCoef][kIirMaxCoef][2];  // (A^32)^(2^k), k = 0..8 (k = 8: one CTA)
+  double mpow[kIirPowers][kIirMaxCoef][kIirMaxCoef][2];  // (A^32)^(2^k): k = 8 one CTA, 13 32 CTAs
   float fa[kIirMaxCoef][2], fb[kIirMaxCoef][2];  // the same in float (no per-use conversion)
-  float fmpow[9][kIirMaxCoef][kIirMaxCoef][2];
+  float fmpow[kIirPowers][kIirMaxCoef][kIirMaxCoef][2];
   void *ws;                                      // [batch][nblk][4] states (output type)
 };
 
@@ -215,20 +214,52 @@ __device__ __forceinline__ void run_chunk(const IirParams &p, IV<T, OC> (&xr)[kI
   }
 }
 
-// One CTA = 256 chunks of one row: each thread runs its chunk from a zero entry, the CTA
-// scans the chunk maps (the carry injected into chunk 0); APPLY reruns each chunk from its
-// true entry state and writes y, else the CTA's zero-entry final state goes to the workspace.
-template <typename T, bool XC, bool OC, bool CC, int CAP, bool APPLY>
-__global__ void __launch_bounds__(kIirThreads) iir_block(const IirParams p, int vec) {
+// One bounded device status word for the filter's chained carries: 1 if a wait for a
+// predecessor's state gave up since the last read.
+static __device__ int32_t g_iir_status;
+
+int iir_status_take() {
+  int32_t v = 0, zero = 0;
+  if (cudaMemcpyFromSymbol(&v, g_iir_status, sizeof(v)) != cudaSuccess) return -1;
+  cudaMemcpyToSymbol(g_iir_status, &zero, sizeof(zero));
+  return v;
+}
+
+// Single pass over a row with chained carries (decoupled look-back).  CTAs take (row, block)
+// tickets in block-major order from a counter, so every block a CTA waits for took its ticket
+// earlier and never waits on a later one.  Each CTA stages its window, runs its chunks from a
+// zero entry and scans them (the zero-entry inclusive state of every chunk), publishes its
+// block aggregate, then warp 0 looks back over the predecessors 32 at a time: the nearest
+// inclusive state ends the walk and every aggregate in front of it, d blocks back, adds
+// M^(256 d) times itself.  The CTA publishes its own inclusive state, every chunk gets its
+// entry M^(32 t) carry + (its zero-entry exclusive state), and the chunks are rerun from
+// there and written.  A wait that runs past
+// kIirSpinLimit polls records the failure in g_iir_status and proceeds (results then wrong,
+// the launch still ends).
+constexpr uint32_t kIirSpinLimit = 1u << 22;
+
+template <typename T, bool XC, bool OC, bool CC, int CAP>
+__global__ void __launch_bounds__(kIirThreads)
+    iir_onepass(const IirParams p, int vec, unsigned long long *ticket, int *flags, IV<T, OC> *agg,
+                IV<T, OC> *incl) {
   using V = IV<T, OC>;
   using XE = typename val_of<T, XC>::type;
   using OE = typename val_of<T, OC>::type;
   constexpr int XES = (int)sizeof(XE), OES = (int)sizeof(OE);
-  __shared__ V sh[kIirThreads * CAP];  // scan exchange
-  extern __shared__ __align__(16) unsigned char stg[];  // 256 chunks of 32 * OES + 16 bytes
-  const int64_t row = blockIdx.y, blk = blockIdx.x;
+  __shared__ V sh[kIirThreads * CAP];
+  __shared__ V s_agg[CAP], s_carry[CAP];
+  __shared__ unsigned long long s_ticket;
+  extern __shared__ __align__(16) unsigned char stg[];
   const int tid = threadIdx.x;
-  const int64_t c = blk * kIirBlock + (int64_t)tid * kIirChunk;  // the chunk's first sample
+  if (tid == 0) s_ticket = atomicAdd(ticket, 1ULL);
+  __syncthreads();
+  // tickets run block-major (block j of every row, then block j + 1): a block's predecessor
+  // took its ticket a whole column of rows earlier and has usually published its inclusive
+  // state by the time the block looks back
+  const int64_t blk = (int64_t)(s_ticket / (unsigned long long)p.batch);
+  const int64_t row = (int64_t)(s_ticket - (unsigned long long)blk * (unsigned long long)p.batch);
+  const int64_t idx = row * p.nblk + blk;
+  const int64_t c = blk * kIirBlock + (int64_t)tid * kIirChunk;
   const unsigned char *xrow = reinterpret_cast<const unsigned char *>(p.x) + row * p.x_bstride * XES;
   stage_in<T, XC>(p, xrow, blk * kIirBlock, vec != 0, stg);
   __syncthreads();
@@ -251,21 +282,9 @@ __global__ void __launch_bounds__(kIirThreads) iir_block(const IirParams p, int 
   }
   V s[kIirMaxCoef];
 #pragma unroll
-  for (int k = 0; k < CAP; k++) s[k] = V::zero();
+  for (int k = 0; k < kIirMaxCoef; k++) s[k] = V::zero();
   run_chunk<T, OC, CC, CAP, false>(p, xr, halo, s);
-  // inclusive scan of the chunk maps: G_t = M G_{t-1} + g_t
-  V carry[kIirMaxCoef];
-  V *wsb = reinterpret_cast<V *>(p.ws) + (row * p.nblk + blk) * kIirMaxCoef;
-#pragma unroll
-  for (int k = 0; k < CAP; k++) carry[k] = APPLY ? wsb[k] : V::zero();
-  if (APPLY && tid == 0) {
-    V mc[kIirMaxCoef];
-#pragma unroll
-    for (int k = 0; k < CAP; k++) mc[k] = carry[k];
-    matvec<T, OC, CC, CAP>(p, 0, mc);
-#pragma unroll
-    for (int k = 0; k < CAP; k++) s[k] = vadd<T, OC>(s[k], mc[k]);
-  }
+  // zero-entry inclusive states of the chunks: G_t = M G_{t-1} + g_t
 #pragma unroll 1
   for (int lv = 0; lv < 8; lv++) {
     const int d = 1 << lv;
@@ -282,81 +301,146 @@ __global__ void __launch_bounds__(kIirThreads) iir_block(const IirParams p, int 
       for (int k = 0; k < CAP; k++) s[k] = vadd<T, OC>(s[k], o[k]);
     }
   }
-  if constexpr (!APPLY) {
-    if (tid == kIirThreads - 1) {
+  __syncthreads();
 #pragma unroll
-      for (int k = 0; k < CAP; k++) wsb[k] = s[k];
+  for (int k = 0; k < CAP; k++) sh[k * kIirThreads + tid] = s[k];
+  if (tid == kIirThreads - 1) {
+    // publish the block aggregate (for the first block of a row it is the inclusive state)
+#pragma unroll
+    for (int k = 0; k < CAP; k++) {
+      s_agg[k] = s[k];
+      (blk == 0 ? incl : agg)[idx * kIirMaxCoef + k] = s[k];
     }
-  } else {
-    // entry state of chunk t = G_{t-1} (the carry for chunk 0)
-    __syncthreads();
+    __threadfence();
+    atomicExch(&flags[idx], blk == 0 ? 2 : 1);
+  }
+  __syncthreads();
+  V excl[kIirMaxCoef];
 #pragma unroll
-    for (int k = 0; k < CAP; k++) sh[k * kIirThreads + tid] = s[k];
-    __syncthreads();
+  for (int k = 0; k < CAP; k++) excl[k] = tid ? sh[k * kIirThreads + tid - 1] : V::zero();
+  if (tid < 32) {
+    // warp 0 looks back over windows of 32 predecessors: lane l takes block blk-1-l of the
+    // current window; the nearest inclusive state ends the walk, the aggregates in front of
+    // it add M^(256 l) a_l, and each full window of aggregates multiplies the rest by
+    // M^(256*32)
+    const int lane = tid;
+    V carry[kIirMaxCoef];
 #pragma unroll
-    for (int k = 0; k < CAP; k++) s[k] = tid ? sh[k * kIirThreads + tid - 1] : carry[k];
-    run_chunk<T, OC, CC, CAP, true>(p, xr, halo, s);
-    // drain through the staging buffer: the chunks in place, then coalesced rows
-    __syncthreads();  // every lane has read its samples and its neighbour's halo
-    unsigned char *mine = stg + tid * (32 * OES + 16);
+    for (int k = 0; k < CAP; k++) carry[k] = V::zero();
+    bool ok = true;
+    if (blk > 0) {
+      int win = 0;  // windows walked so far (the walk's power is M^(256*32*win))
+      for (int64_t j0 = blk - 1; j0 >= 0; j0 -= 32, win++) {
+        const int64_t j = j0 - lane;
+        int f = 2;  // lanes past block 0 count as "inclusive zero"
+        V v[kIirMaxCoef];
 #pragma unroll
-    for (int j = 0; j < kIirChunk; j++) {
-      OE o;
-      if constexpr (OC) {
-        o.x = xr[j].re;
-        o.y = xr[j].im;
-      } else {
-        o = xr[j].re;
+        for (int k = 0; k < CAP; k++) v[k] = V::zero();
+        if (j >= 0) {
+          volatile int *fl = flags + row * p.nblk + j;
+          f = 0;
+          for (uint32_t it = 0; it < kIirSpinLimit && (f = *fl) == 0; it++) __nanosleep(32);
+          if (f == 0) {
+            ok = false;
+            f = 2;  // give up on this block: treat it as a zero inclusive state
+          } else {
+            __threadfence();
+            const V *src = (f == 2 ? incl : agg) + (row * p.nblk + j) * kIirMaxCoef;
+#pragma unroll
+            for (int k = 0; k < CAP; k++) {
+              if constexpr (OC) {
+                const OE e = __ldcg(reinterpret_cast<const OE *>(src + k));
+                v[k].re = e.x;
+                v[k].im = e.y;
+              } else {
+                v[k].re = __ldcg(reinterpret_cast<const T *>(src + k));
+              }
+            }
+          }
+        }
+        const unsigned inc_mask = __ballot_sync(0xffffffffu, f == 2);
+        const int stop = inc_mask ? __ffs(inc_mask) - 1 : 32;  // lanes <= stop contribute
+        if (lane > stop) {
+#pragma unroll
+          for (int k = 0; k < CAP; k++) v[k] = V::zero();
+        }
+        // M^(256 (32 win + lane)) v
+#pragma unroll
+        for (int b = 0; b < 5; b++)
+          if ((lane >> b) & 1) matvec<T, OC, CC, CAP>(p, 8 + b, v);
+        for (int w = 0; w < win; w++) matvec<T, OC, CC, CAP>(p, 13, v);
+        // sum over the warp
+#pragma unroll
+        for (int k = 0; k < CAP; k++) {
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) {
+            v[k].re += __shfl_xor_sync(0xffffffffu, v[k].re, off);
+            if constexpr (OC) v[k].im += __shfl_xor_sync(0xffffffffu, v[k].im, off);
+          }
+          carry[k] = vadd<T, OC>(carry[k], v[k]);
+        }
+        if (stop < 32) break;
       }
-      *reinterpret_cast<OE *>(mine + j * OES) = o;
+      const bool all_ok = __all_sync(0xffffffffu, ok);
+      if (lane == 0) {
+        if (!all_ok) atomicExch(&g_iir_status, 1);
+        // this block's inclusive state: M^256 carry + aggregate
+        V inc[kIirMaxCoef];
+#pragma unroll
+        for (int k = 0; k < CAP; k++) inc[k] = carry[k];
+        matvec<T, OC, CC, CAP>(p, 8, inc);
+#pragma unroll
+        for (int k = 0; k < CAP; k++) {
+          inc[k] = vadd<T, OC>(inc[k], s_agg[k]);
+          incl[idx * kIirMaxCoef + k] = inc[k];
+        }
+        __threadfence();
+        atomicExch(&flags[idx], 2);
+      }
     }
-    __syncthreads();
-    unsigned char *yrow = reinterpret_cast<unsigned char *>(p.y) + row * p.y_bstride * OES;
-    const int64_t n0 = blk * kIirBlock;
-    if (vec && n0 + kIirBlock <= p.N) {
-      constexpr int PPC = 32 * OES / 16;
-      float4 *dst = reinterpret_cast<float4 *>(yrow + n0 * OES);
-#pragma unroll 4
-      for (int q = tid; q < kIirBlock * OES / 16; q += kIirThreads)
-        dst[q] = *reinterpret_cast<const float4 *>(stg + (q / PPC) * (32 * OES + 16) + (q % PPC) * 16);
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < CAP; k++) s_carry[k] = carry[k];
+    }
+  }
+  __syncthreads();
+  // entry of chunk t: M^(32 t) carry + its zero-entry exclusive state
+#pragma unroll
+  for (int k = 0; k < CAP; k++) s[k] = s_carry[k];
+#pragma unroll
+  for (int lv = 0; lv < 8; lv++)
+    if ((tid >> lv) & 1) matvec<T, OC, CC, CAP>(p, lv, s);
+#pragma unroll
+  for (int k = 0; k < CAP; k++) s[k] = vadd<T, OC>(s[k], excl[k]);
+  run_chunk<T, OC, CC, CAP, true>(p, xr, halo, s);
+  // drain through the staging buffer: the chunks in place, then coalesced rows
+  __syncthreads();
+  unsigned char *mine = stg + tid * (32 * OES + 16);
+#pragma unroll
+  for (int j = 0; j < kIirChunk; j++) {
+    OE o;
+    if constexpr (OC) {
+      o.x = xr[j].re;
+      o.y = xr[j].im;
     } else {
-      OE *dst = reinterpret_cast<OE *>(yrow);
-      for (int e = tid; e < kIirBlock; e += kIirThreads)
-        if (n0 + e < p.N) dst[n0 + e] = *reinterpret_cast<const OE *>(stg + stg_off<OES>(e));
+      o = xr[j].re;
     }
-  }
-}
-
-// One CTA per row: ws[row][j] <- the carry into CTA j, from the CTAs' zero-entry final
-// states (staged in shared memory, then one thread walks them in order).
-template <typename T, bool OC, bool CC, int CAP>
-__global__ void iir_carries(const IirParams p) {
-  using V = IV<T, OC>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  V *st = reinterpret_cast<V *>(smem_raw);
-  const int64_t row = blockIdx.x;
-  V *ws = reinterpret_cast<V *>(p.ws) + row * p.nblk * kIirMaxCoef;
-  const int64_t n = p.nblk * kIirMaxCoef;
-  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) st[e] = ws[e];
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    V cur[kIirMaxCoef];
-#pragma unroll
-    for (int k = 0; k < CAP; k++) cur[k] = V::zero();
-    for (int64_t j = 0; j < p.nblk; j++) {
-      V f[kIirMaxCoef];
-#pragma unroll
-      for (int k = 0; k < CAP; k++) {
-        f[k] = st[j * kIirMaxCoef + k];
-        st[j * kIirMaxCoef + k] = cur[k];
-      }
-      matvec<T, OC, CC, CAP>(p, 8, cur);
-#pragma unroll
-      for (int k = 0; k < CAP; k++) cur[k] = vadd<T, OC>(cur[k], f[k]);
-    }
+    *reinterpret_cast<OE *>(mine + j * OES) = o;
   }
   __syncthreads();
-  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) ws[e] = st[e];
+  unsigned char *yrow = reinterpret_cast<unsigned char *>(p.y) + row * p.y_bstride * OES;
+  const int64_t n0 = blk * kIirBlock;
+  if (vec && n0 + kIirBlock <= p.N) {
+    constexpr int PPC = 32 * OES / 16;
+    float4 *dst = reinterpret_cast<float4 *>(yrow + n0 * OES);
+#pragma unroll 4
+    for (int q = tid; q < kIirBlock * OES / 16; q += kIirThreads)
+      dst[q] = *reinterpret_cast<const float4 *>(stg + (q / PPC) * (32 * OES + 16) + (q % PPC) * 16);
+  } else {
+    OE *dst = reinterpret_cast<OE *>(yrow);
+    for (int e = tid; e < kIirBlock; e += kIirThreads)
+      if (n0 + e < p.N) dst[n0 + e] = *reinterpret_cast<const OE *>(stg + stg_off<OES>(e));
+  }
 }
 
 // FIR-only filter(): conv1d SAME with the (at most 4) host coefficients, one output per thread.
@@ -399,9 +483,13 @@ CMat cmat_mul(const CMat &a, const CMat &b) {
 }
 }  // namespace
 
+// Workspace of the recursive form: the ticket counter (16 bytes), one flag per (row, block),
+// then the blocks' aggregate and inclusive states (4 values each).
+static size_t iir_flag_bytes(int64_t batch, int64_t nblk) { return ((size_t)batch * nblk * 4 + 15) & ~(size_t)15; }
+
 size_t filter_workspace_bytes(int64_t batch, int64_t len, int32_t out_dtype) {
   const int64_t nblk = (len + kIirBlock - 1) / kIirBlock;
-  return (size_t)batch * (size_t)nblk * kIirMaxCoef * dtype_size(out_dtype);
+  return 16 + iir_flag_bytes(batch, nblk) + 2 * (size_t)batch * (size_t)nblk * kIirMaxCoef * dtype_size(out_dtype);
 }
 
 template <typename T, bool XC, bool OC, bool CC, int CAP>
@@ -418,26 +506,24 @@ static int launch_filter(IirParams &p, cudaStream_t s) {
   }
   using V = IV<T, OC>;
   const size_t xes = sizeof(T) * (XC ? 2 : 1), oes = sizeof(T) * (OC ? 2 : 1);
-  if (p.batch > 65535) GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "filter: at most 65535 rows per call");
-  const size_t csmem = (size_t)p.nblk * kIirMaxCoef * sizeof(V);
   const size_t bsmem = (size_t)kIirThreads * (32 * oes + 16);
-  int rc = ensure_smem((const void *)iir_carries<T, OC, CC, CAP>, csmem, "filter");
-  if (!rc) rc = ensure_smem((const void *)iir_block<T, XC, OC, CC, CAP, false>, bsmem, "filter");
-  if (!rc) rc = ensure_smem((const void *)iir_block<T, XC, OC, CC, CAP, true>, bsmem, "filter");
+  int rc = ensure_smem((const void *)iir_onepass<T, XC, OC, CC, CAP>, bsmem, "filter");
   if (rc) return rc;
   // coalesced 16-byte fills and drains when every row start is 16-byte aligned
   const int vec = (reinterpret_cast<uintptr_t>(p.x) % 16 == 0 && reinterpret_cast<uintptr_t>(p.y) % 16 == 0 &&
                    (p.x_bstride * xes) % 16 == 0 && (p.y_bstride * oes) % 16 == 0)
                       ? 1
                       : 0;
-  const dim3 grid((unsigned)p.nblk, (unsigned)p.batch);
-  iir_block<T, XC, OC, CC, CAP, false><<<grid, kIirThreads, bsmem, s>>>(p, vec);
-  rc = check_launch("filter (IIR block states)");
-  if (rc) return rc;
-  iir_carries<T, OC, CC, CAP><<<(unsigned)p.batch, 128, csmem, s>>>(p);
-  rc = check_launch("filter (IIR carries)");
-  if (rc) return rc;
-  iir_block<T, XC, OC, CC, CAP, true><<<grid, kIirThreads, bsmem, s>>>(p, vec);
+  unsigned char *ws = reinterpret_cast<unsigned char *>(p.ws);
+  const size_t fbytes = iir_flag_bytes(p.batch, p.nblk);
+  auto *ticket = reinterpret_cast<unsigned long long *>(ws);
+  int *flags = reinterpret_cast<int *>(ws + 16);
+  V *agg = reinterpret_cast<V *>(ws + 16 + fbytes);
+  V *incl = agg + (size_t)p.batch * p.nblk * kIirMaxCoef;
+  if (cudaMemsetAsync(ws, 0, 16 + fbytes, s) != cudaSuccess) GBFIR_FAIL(GBFIR_ERR_CUDA, "filter: workspace reset failed");
+  const int64_t grid = p.batch * p.nblk;
+  if (grid > 0x7fffffffLL) GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "filter: too many blocks");
+  iir_onepass<T, XC, OC, CC, CAP><<<(unsigned)grid, kIirThreads, bsmem, s>>>(p, vec, ticket, flags, agg, incl);
   return check_launch("filter (IIR)");
 }
 
@@ -483,7 +569,7 @@ int filter_fp(const gbfir_buf &out, const gbfir_buf &in, const void *a, int na, 
     for (int i = 1; i < cap; i++) A.v[i][i - 1][0] = 1.0;
     CMat M = A;
     for (int i = 0; i < 5; i++) M = cmat_mul(M, M);  // A^32
-    for (int lv = 0; lv < 9; lv++) {
+    for (int lv = 0; lv < kIirPowers; lv++) {
       memcpy(p.mpow[lv], M.v, sizeof(M.v));
       M = cmat_mul(M, M);
     }
@@ -492,7 +578,7 @@ int filter_fp(const gbfir_buf &out, const gbfir_buf &in, const void *a, int na, 
     for (int c = 0; c < 2; c++) {
       p.fa[i][c] = (float)p.a[i][c];
       p.fb[i][c] = (float)p.b[i][c];
-      for (int lv = 0; lv < 9; lv++)
+      for (int lv = 0; lv < kIirPowers; lv++)
         for (int j = 0; j < kIirMaxCoef; j++) p.fmpow[lv][i][j][c] = (float)p.mpow[lv][i][j][c];
     }
   const bool xc = dtype_complex(in.dtype);

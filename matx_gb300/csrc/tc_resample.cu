@@ -605,16 +605,18 @@ namespace gbfir {
 int resample_rowtile_status();
 int adjoint_rowtile_status();
 int tc_wide_status_take();
+int iir_status_take();
 }  // namespace gbfir
 
-// 0 if every bounded wait of the pipelined kernels (tensor-core kernels and the TMA-fed
-// row tile) completed since the last call; 1 if one gave up; -1 if the status could not
-// be read.
+// 0 if every bounded wait of the pipelined kernels (tensor-core kernels, the TMA-fed row
+// tile, the filter's chained carries) completed since the last call; 1 if one gave up; -1 if
+// the status could not be read.
 extern "C" int gbfir_tc_status(void) {
   const int a = gbfir::tc_status_read_and_clear();
   const int b = gbfir::resample_rowtile_status();
   const int c = gbfir::adjoint_rowtile_status();
   const int d = gbfir::tc_wide_status_take();
-  if (a < 0 || b < 0 || c < 0 || d < 0) return -1;
-  return (a | b | c | d) ? 1 : 0;
+  const int e = gbfir::iir_status_take();
+  if (a < 0 || b < 0 || c < 0 || d < 0 || e < 0) return -1;
+  return (a | b | c | d | e) ? 1 : 0;
 }

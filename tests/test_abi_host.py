@@ -134,8 +134,9 @@ def test_filter_validation(lib):
     b = (ctypes.c_float * 4)(2.0, 1.0, 0, 0)
     f = lambda o, i, na=2, nb=2, cdt=0, ws=None, wsb=0: lib.gbfir_filter(o, i, a, na, b, nb, cdt, ws, wsb, None)
     x = buf(1000, batch=3, dtype=0)
-    assert lib.gbfir_filter_workspace_size(3, 1000, 0) == 3 * 1 * 4 * 4
-    assert lib.gbfir_filter_workspace_size(3, 8193, 1) == 3 * 2 * 4 * 8
+    # ticket (16 B) + one flag per (row, block) rounded to 16 B + aggregate and inclusive states
+    assert lib.gbfir_filter_workspace_size(3, 1000, 0) == 16 + 16 + 2 * 3 * 1 * 4 * 4
+    assert lib.gbfir_filter_workspace_size(3, 8193, 1) == 16 + 32 + 2 * 3 * 2 * 4 * 8
     assert f(buf(999, batch=3, dtype=0), x) == 3
     assert f(buf(1000, batch=3, dtype=1), x) == 4           # real in, real taps -> real out
     assert f(buf(1000, batch=3, dtype=0), x, na=5) == 5

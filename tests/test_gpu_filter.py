@@ -69,6 +69,22 @@ def test_iir_long_memory_carries(mx, orc):
     y = mx.filter(torch.from_numpy(x).cuda(), a, [1.0, 0.5]).cpu().numpy()
     r = orc.iir_filter(x.astype(np.float64), a, [1.0, 0.5])
     assert rel_l2(y, r) < 1e-4
+    # every chained-carry wait completed (a wait that gives up is recorded, not hung on)
+    from matx_gb300 import _lib
+    assert _lib.load().gbfir_tc_status() == 0
+
+
+def test_iir_many_rows_and_blocks(mx, orc):
+    # 300 rows x 40 blocks: tickets interleave rows, carries chain within each row only
+    import torch
+    rng = np.random.default_rng(9)
+    x = rng.uniform(-1, 1, (300, 40 * 8192 - 5)).astype(np.float32)
+    y = mx.filter(torch.from_numpy(x).cuda(), [0.9, -0.2], [1.0, -1.0]).cpu().numpy()
+    for row in (0, 1, 150, 299):
+        r = orc.iir_filter(x[row:row + 1].astype(np.float64), [0.9, -0.2], [1.0, -1.0])
+        assert rel_l2(y[row:row + 1], r) < 2e-6, row
+    from matx_gb300 import _lib
+    assert _lib.load().gbfir_tc_status() == 0
 
 
 @pytest.mark.parametrize("nb", [1, 2, 3, 4])
