@@ -11,8 +11,8 @@
 // a transform of NF = 2^n points (1024..8192, at least 2L) in shared memory.  A persistent
 // CTA builds the twiddle table and the filter's spectrum once, then walks blocks of
 // B = NF - L + 1 outputs: it loads the NF-sample window that ends at the block (zero
-// outside the row), transforms it in place (radix-8 decimation-in-frequency stages with a
-// radix-4/2 tail, each lane holding one butterfly's 8 points in registers), multiplies by
+// outside the row), transforms it in place (radix-16 decimation-in-frequency stages with a
+// last stage of radix 4..32, each lane holding one butterfly's points in registers), multiplies by
 // the spectrum (both in the same digit-reversed order, so no reordering pass), runs the
 // mirror-image decimation-in-time inverse back to natural order and writes the B valid
 // outputs.  HBM sees each input about NF/B times (once plus the L-1 overlap) and each
@@ -21,7 +21,7 @@
 
 namespace gbfir {
 
-constexpr int kFftThreads = 1024;
+constexpr int kFftThreads = 512;
 constexpr int kFftMaxLog = 13;  // NF <= 8192
 
 struct FftConvParams {
@@ -90,12 +90,82 @@ __device__ __forceinline__ void dft8(float2 (&v)[8]) {
   }
 }
 
+// cos(2 pi m / 32), m = 0..31 (exact constants of the 32-point circle); a switch, so that
+// unrolled callers with constant m fold it away.
+__host__ __device__ constexpr float cos32(int m) {
+  switch (m & 31) {
+    case 0: return 1.0f;
+    case 1: return 0.98078528040323044913f;
+    case 2: return 0.92387953251128675613f;
+    case 3: return 0.83146961230254523708f;
+    case 4: return 0.70710678118654752440f;
+    case 5: return 0.55557023301960222474f;
+    case 6: return 0.38268343236508977173f;
+    case 7: return 0.19509032201612826785f;
+    case 8: return 0.0f;
+    case 9: return -0.19509032201612826785f;
+    case 10: return -0.38268343236508977173f;
+    case 11: return -0.55557023301960222474f;
+    case 12: return -0.70710678118654752440f;
+    case 13: return -0.83146961230254523708f;
+    case 14: return -0.92387953251128675613f;
+    case 15: return -0.98078528040323044913f;
+    case 16: return -1.0f;
+    case 17: return -0.98078528040323044913f;
+    case 18: return -0.92387953251128675613f;
+    case 19: return -0.83146961230254523708f;
+    case 20: return -0.70710678118654752440f;
+    case 21: return -0.55557023301960222474f;
+    case 22: return -0.38268343236508977173f;
+    case 23: return -0.19509032201612826785f;
+    case 24: return 0.0f;
+    case 25: return 0.19509032201612826785f;
+    case 26: return 0.38268343236508977173f;
+    case 27: return 0.55557023301960222474f;
+    case 28: return 0.70710678118654752440f;
+    case 29: return 0.83146961230254523708f;
+    case 30: return 0.92387953251128675613f;
+    case 31: return 0.98078528040323044913f;
+  }
+  return 0.0f;
+}
+
+// The R-point DFT (R a power of two up to 32) in registers, natural order in and out, by
+// recursive decimation in frequency: a_r = v_r + v_(r+R/2), b_r = (v_r - v_(r+R/2)) W_R^r,
+// X_2k = DFT(a)_k, X_2k+1 = DFT(b)_k.  INV uses the conjugate roots.
+template <int R, bool INV>
+__device__ __forceinline__ void dftp(float2 (&v)[R]) {
+  if constexpr (R == 2) {
+    dft2<INV>(v[0], v[1]);
+  } else if constexpr (R == 4) {
+    dft4<INV>(v);
+  } else {
+    constexpr int Hh = R / 2;
+    float2 a[Hh], b[Hh];
+#pragma unroll
+    for (int r = 0; r < Hh; r++) {
+      a[r] = cadd(v[r], v[r + Hh]);
+      const float2 d = csub(v[r], v[r + Hh]);
+      const int m = r * (32 / R);
+      const float c = cos32(m), sn = cos32(m + 24);  // sin(2 pi m / 32) = cos(2 pi (m - 8) / 32)
+      b[r] = r == 0 ? d : cmul(d, make_float2(c, INV ? sn : -sn));
+    }
+    dftp<Hh, INV>(a);
+    dftp<Hh, INV>(b);
+#pragma unroll
+    for (int k = 0; k < Hh; k++) {
+      v[2 * k] = a[k];
+      v[2 * k + 1] = b[k];
+    }
+  }
+}
+
 // Element p of a transform lives at p + p/16 in shared memory (one pad per 128 bytes): the
 // late stages' butterflies, whose points are 8-128 elements apart, then fall on distinct
 // banks for the lanes of a half-warp.
 __device__ __forceinline__ int fpad(int p) { return p + (p >> 4); }
 
-// The stages of a 2^lognf-point transform: radix-8 with a radix-4 or radix-2 tail; stage s
+// The stages of a 2^lognf-point transform: radix-16, then one of radix 4..32; stage s
 // works on sub-transforms of ls[s] points, and its twiddles W_ls^(r*k), r = 1..R-1, k <
 // ls/R, sit at tw[off[s] + (r-1)*(ls/R) + k] (consecutive lanes read consecutive entries).
 struct FftPlan {
@@ -105,7 +175,7 @@ __host__ __device__ inline FftPlan fft_plan(int lognf) {
   FftPlan f{};
   int rem = lognf, len = 1 << lognf, off = 0;
   while (rem > 0) {
-    const int lr = rem >= 3 ? 3 : rem;
+    const int lr = rem > 5 ? 4 : rem;  // radix-16 stages, the last of up to radix 32
     f.rad[f.ns] = 1 << lr;
     f.ls[f.ns] = len;
     f.off[f.ns] = off;
@@ -116,18 +186,6 @@ __host__ __device__ inline FftPlan fft_plan(int lognf) {
   }
   f.tw_len = off;
   return f;
-}
-
-// The R-point DFT of a butterfly in registers.
-template <int R, bool INV>
-__device__ __forceinline__ void dft_r(float2 (&v)[R]) {
-  if constexpr (R == 8) {
-    dft8<INV>(v);
-  } else if constexpr (R == 4) {
-    dft4<INV>(v);
-  } else {
-    dft2<INV>(v[0], v[1]);
-  }
 }
 
 // One stage in shared memory: butterfly (g, k) on X[g*ls + k + r*ls/R].  Forward
@@ -146,7 +204,7 @@ __device__ __forceinline__ void fft_stage(float2 *X, const float2 *tw, int nf, i
 #pragma unroll
       for (int r = 1; r < R; r++) v[r] = cmul(v[r], cconj(tw[(r - 1) * q + k]));
     }
-    dft_r<R, INV>(v);
+    dftp<R, INV>(v);
     if constexpr (!INV) {
 #pragma unroll
       for (int r = 1; r < R; r++) v[r] = cmul(v[r], tw[(r - 1) * q + k]);
@@ -159,9 +217,13 @@ __device__ __forceinline__ void fft_stage(float2 *X, const float2 *tw, int nf, i
 template <bool INV>
 __device__ __forceinline__ void stage_any(float2 *X, const float2 *tw, const FftPlan &f, int s, int nf) {
   __syncthreads();
-  if (f.rad[s] == 8) fft_stage<8, INV>(X, tw + f.off[s], nf, f.ls[s]);
-  else if (f.rad[s] == 4) fft_stage<4, INV>(X, tw + f.off[s], nf, f.ls[s]);
-  else fft_stage<2, INV>(X, tw + f.off[s], nf, f.ls[s]);
+  switch (f.rad[s]) {
+    case 32: fft_stage<32, INV>(X, tw + f.off[s], nf, f.ls[s]); break;
+    case 16: fft_stage<16, INV>(X, tw + f.off[s], nf, f.ls[s]); break;
+    case 8: fft_stage<8, INV>(X, tw + f.off[s], nf, f.ls[s]); break;
+    case 4: fft_stage<4, INV>(X, tw + f.off[s], nf, f.ls[s]); break;
+    default: fft_stage<2, INV>(X, tw + f.off[s], nf, f.ls[s]); break;
+  }
 }
 
 // The full forward transform in shared memory (for the filter's spectrum); the result is
@@ -182,25 +244,26 @@ __device__ __forceinline__ void fft_middle(float2 *X, const float2 *H, int nf, i
     float2 v[R];
 #pragma unroll
     for (int r = 0; r < R; r++) v[r] = X[fpad(base + r * q)];
-    dft_r<R, false>(v);
+    dftp<R, false>(v);
 #pragma unroll
     for (int r = 0; r < R; r++) v[r] = cmul(v[r], H[fpad(base + r * q)]);
-    dft_r<R, true>(v);
+    dftp<R, true>(v);
 #pragma unroll
     for (int r = 0; r < R; r++) X[fpad(base + r * q)] = v[r];
   }
 }
 
-// The first forward stage (radix 8, ls = nf) straight from the global window: lane k loads
-// window samples k + r*nf/8, coalesced across the warp.
+// The first forward stage (radix 16, ls = nf) straight from the global window: lane k loads
+// window samples k + r*nf/16, coalesced across the warp.
 template <bool SC>
 __device__ __forceinline__ void fft_first(float2 *X, const float2 *tw, const FftConvParams &p, int nf, int64_t b,
                                           int64_t ws) {
-  const int q = nf / 8;
+  constexpr int R = 16;
+  const int q = nf / R;
   for (int k = threadIdx.x; k < q; k += blockDim.x) {
-    float2 v[8];
+    float2 v[R];
 #pragma unroll
-    for (int r = 0; r < 8; r++) {
+    for (int r = 0; r < R; r++) {
       const int64_t n = ws + k + r * q;
       v[r] = make_float2(0.f, 0.f);
       if (n >= 0 && n < p.N) {
@@ -208,29 +271,30 @@ __device__ __forceinline__ void fft_first(float2 *X, const float2 *tw, const Fft
         else v[r].x = reinterpret_cast<const float *>(p.s)[b * p.s_bstride + n];
       }
     }
-    dft8<false>(v);
+    dftp<R, false>(v);
 #pragma unroll
-    for (int r = 1; r < 8; r++) v[r] = cmul(v[r], tw[(r - 1) * q + k]);
+    for (int r = 1; r < R; r++) v[r] = cmul(v[r], tw[(r - 1) * q + k]);
 #pragma unroll
-    for (int r = 0; r < 8; r++) X[fpad(k + r * q)] = v[r];
+    for (int r = 0; r < R; r++) X[fpad(k + r * q)] = v[r];
   }
 }
 
-// The last inverse stage (radix 8, ls = nf) straight to the output: positions k + r*nf/8 in
-// [L-1, L-1+B) are block outputs.
+// The last inverse stage (radix 16, ls = nf) straight to the output: positions k + r*nf/16
+// in [L-1, L-1+B) are block outputs.
 template <bool OC>
 __device__ __forceinline__ void fft_last(const float2 *X, const float2 *tw, const FftConvParams &p, int nf,
                                          int64_t b, int64_t o0) {
-  const int q = nf / 8;
+  constexpr int R = 16;
+  const int q = nf / R;
   for (int k = threadIdx.x; k < q; k += blockDim.x) {
-    float2 v[8];
+    float2 v[R];
 #pragma unroll
-    for (int r = 0; r < 8; r++) v[r] = X[fpad(k + r * q)];
+    for (int r = 0; r < R; r++) v[r] = X[fpad(k + r * q)];
 #pragma unroll
-    for (int r = 1; r < 8; r++) v[r] = cmul(v[r], cconj(tw[(r - 1) * q + k]));
-    dft8<true>(v);
+    for (int r = 1; r < R; r++) v[r] = cmul(v[r], cconj(tw[(r - 1) * q + k]));
+    dftp<R, true>(v);
 #pragma unroll
-    for (int r = 0; r < 8; r++) {
+    for (int r = 0; r < R; r++) {
       const int pos = k + r * q;
       const int64_t o = o0 + pos - (p.L - 1);
       if (pos >= p.L - 1 && pos < p.L - 1 + p.B && o < p.out_len) {
@@ -289,9 +353,12 @@ __global__ void __launch_bounds__(kFftThreads) conv1d_fft(const FftConvParams p)
     fft_first<SC>(X, tw + f.off[0], p, nf, b, ws);
     for (int s = 1; s < last; s++) stage_any<false>(X, tw, f, s, nf);
     __syncthreads();
-    if (f.rad[last] == 8) fft_middle<8>(X, H, nf, f.ls[last]);
-    else if (f.rad[last] == 4) fft_middle<4>(X, H, nf, f.ls[last]);
-    else fft_middle<2>(X, H, nf, f.ls[last]);
+    switch (f.rad[last]) {
+      case 32: fft_middle<32>(X, H, nf, f.ls[last]); break;
+      case 16: fft_middle<16>(X, H, nf, f.ls[last]); break;
+      case 8: fft_middle<8>(X, H, nf, f.ls[last]); break;
+      default: fft_middle<4>(X, H, nf, f.ls[last]); break;
+    }
     for (int s = last - 1; s >= 1; s--) stage_any<true>(X, tw, f, s, nf);
     __syncthreads();
     fft_last<SC || HC>(X, tw + f.off[0], p, nf, b, o0);
