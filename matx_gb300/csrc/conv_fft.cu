@@ -66,29 +66,6 @@ __device__ __forceinline__ void dft4(float2 (&v)[4]) {
   v[1] = cadd(d0, d1);
   v[3] = csub(d0, d1);
 }
-template <bool INV>
-__device__ __forceinline__ void dft8(float2 (&v)[8]) {
-  constexpr float r = 0.70710678118654752440f;
-  float2 a[4], b[4];
-#pragma unroll
-  for (int i = 0; i < 4; i++) {
-    a[i] = cadd(v[i], v[i + 4]);
-    b[i] = csub(v[i], v[i + 4]);
-  }
-  // b_r *= W8^r
-  b[1] = INV ? make_float2(r * (b[1].x - b[1].y), r * (b[1].x + b[1].y))
-             : make_float2(r * (b[1].x + b[1].y), r * (b[1].y - b[1].x));
-  b[2] = mul_mi<INV>(b[2]);
-  b[3] = INV ? make_float2(-r * (b[3].x + b[3].y), r * (b[3].x - b[3].y))
-             : make_float2(r * (b[3].y - b[3].x), -r * (b[3].x + b[3].y));
-  dft4<INV>(a);
-  dft4<INV>(b);
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    v[2 * k] = a[k];
-    v[2 * k + 1] = b[k];
-  }
-}
 
 // cos(2 pi m / 32), m = 0..31 (exact constants of the 32-point circle); a switch, so that
 // unrolled callers with constant m fold it away.
