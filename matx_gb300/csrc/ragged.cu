@@ -7,7 +7,8 @@
 // split over WC warps.  The tile table is ordered most expensive first.  CTAs take
 // tiles from an atomic counter (dynamic scheduling, so a 1e6-sample signal next to a
 // 1e3-sample one costs no idle SMs), rebuild the tap table only when the signal
-// changes, stage the tile's input window with cp.async (zero-filled) and run the same
+// changes, stage the tile's input window with cp.async (zero-filled; even strides in the
+// conflict-free XOR layout of rowtile.cuh for that signal's stride) and run the same
 // per-tile compute as the single-signal kernel.  Taking a tile is one atomicAdd: no
 // CTA ever waits on another, so nothing can spin.  The launch contains no host
 // synchronisation and can be captured in a CUDA graph.
@@ -78,7 +79,7 @@ __host__ __device__ inline RgGeom rg_geometry(int64_t up, int64_t down, int64_t 
 __host__ __device__ inline int64_t rg_window(const RgGeom &g) { return (int64_t)(g.QC - 1) * g.S + (g.kmax - g.kmin) + 1; }
 __host__ __device__ inline int64_t rg_window_alloc(const RgGeom &g) {
   const int64_t w = rg_window(g);
-  return (g.S % 2 == 0) ? w + (w >> 4) + 1 : w;
+  return (g.S % 2 == 0) ? (w + 15) / 16 * 16 : w;  // the XOR layouts permute inside blocks of 16
 }
 
 struct RgParams {
@@ -133,7 +134,10 @@ __global__ void __launch_bounds__(kRgThreads) ragged_rowtile(const RgParams rp) 
       p.scale = (double)g.up;
       s_p = p;
       s_identity = g.identity;
-      s_pad = (g.S % 2) == 0;
+      // even row strides: the conflict-free XOR window layout for t = ctz(S) (rowtile.cuh)
+      int t = 0;
+      while (t < 7 && ((g.S >> t) & 1) == 0) t++;
+      s_pad = t ? 10 + t : 0;
     }
     __syncthreads();
     const RsParams &p = s_p;
@@ -152,22 +156,29 @@ __global__ void __launch_bounds__(kRgThreads) ragged_rowtile(const RgParams rp) 
     }
     const int64_t xs0 = q0 * p.S + p.kmin;
     const XT *row = reinterpret_cast<const XT *>(p.x);
-    const bool pad = s_pad;
-    for (int e = tid; e < p.win; e += kRgThreads) {
-      const int64_t gi = xs0 + e;
-      const bool ok = gi >= 0 && gi < p.N;
-      const int si = pad ? smem_idx<4>(e) : e;
-      cp_async_zfill<8>(&xbuf[si], ok ? (const void *)(row + gi) : (const void *)row, ok);
-    }
-    cp_async_commit();
-    cp_async_wait<0>();
-    __syncthreads();
     const int wr = wid / p.WC, wc = wid - wr * p.WC;
     float2 *orow = reinterpret_cast<float2 *>(p.out);
-    if (pad) {
-      rowtile_compute<float, true, false, 1, 4>(p, xbuf, table, orow, q0, wr, wc, lane, (float)p.scale, 0);
-    } else {
-      rowtile_compute<float, true, false, 1, 0>(p, xbuf, table, orow, q0, wr, wc, lane, (float)p.scale, 0);
+    auto stage_and_compute = [&](auto padc) {
+      constexpr int PAD = decltype(padc)::value;
+      for (int e = tid; e < p.win; e += kRgThreads) {
+        const int64_t gi = xs0 + e;
+        const bool ok = gi >= 0 && gi < p.N;
+        cp_async_zfill<8>(&xbuf[smem_idx<PAD>(e)], ok ? (const void *)(row + gi) : (const void *)row, ok);
+      }
+      cp_async_commit();
+      cp_async_wait<0>();
+      __syncthreads();
+      rowtile_compute<float, true, false, 1, PAD>(p, xbuf, table, orow, q0, wr, wc, lane, (float)p.scale, 0);
+    };
+    switch (s_pad) {
+      case 0: stage_and_compute(std::integral_constant<int, 0>{}); break;
+      case 11: stage_and_compute(std::integral_constant<int, 11>{}); break;
+      case 12: stage_and_compute(std::integral_constant<int, 12>{}); break;
+      case 13: stage_and_compute(std::integral_constant<int, 13>{}); break;
+      case 14: stage_and_compute(std::integral_constant<int, 14>{}); break;
+      case 15: stage_and_compute(std::integral_constant<int, 15>{}); break;
+      case 16: stage_and_compute(std::integral_constant<int, 16>{}); break;
+      default: stage_and_compute(std::integral_constant<int, 17>{}); break;
     }
     __syncthreads();
   }
