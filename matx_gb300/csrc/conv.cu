@@ -16,6 +16,9 @@
 // E*E multiply-adds.  Long filters are processed in chunks of up to 1024 taps,
 // accumulators staying in registers.  Results are staged through shared memory
 // so the global stores are fully coalesced whatever the row alignment.
+// Real rows with one shared real filter of at most 1024 taps take conv1d_real_stream
+// (persistent CTAs, prefetched windows, unrolled tap blocks), which makes the same
+// multiply-adds in the same order.
 #include "common.cuh"
 
 namespace gbfir {
@@ -127,6 +130,184 @@ __global__ void __launch_bounds__(kConvThreads) conv1d_direct(const ConvParams p
   for (int e = tid; e < nvalid; e += kConvThreads) orow[o0 + e] = stage[e];
 }
 
+// ---- real fp32 rows, one shared filter of at most 1024 taps: persistent and pipelined ----
+//
+// The one-tile-per-CTA kernel above waits on its window load before its short compute
+// (8 tap blocks at 63 taps), so it runs latency-bound. Here a persistent CTA walks its
+// tiles (row, 2048 outputs) with the taps loaded once and the next tile's window
+// prefetched by cp.async into the second of two buffers while the current one computes.
+// The multiply-adds are those of conv1d_direct in the same order: results are identical.
+//
+// Window layout: float i sits at i ^ (((i >> 5) & 1) << 2). A thread reads its 8 samples
+// as two 16-byte loads, lanes 32 bytes apart; the swap of 16-byte halves on bit 5 puts the
+// 8 lanes of a quarter warp on 8 distinct bank groups. 16-byte units stay whole, so an
+// aligned window is copied in 16-byte pieces.
+__device__ __forceinline__ int win_swz(int i) { return i ^ (((i >> 5) & 1) << 2); }
+
+__device__ __forceinline__ void stream_issue(const ConvParams &p, int64_t t, float *buf, int LC, int tid) {
+  const int64_t b = t / p.chunks_per_row;
+  const int64_t o0 = (t - b * p.chunks_per_row) * (int64_t)kConvNB;
+  const int64_t wb = o0 + p.start - LC;  // signal index of window float 0
+  const int wlen = kConvNB + LC;         // a multiple of 8
+  const float *srow = reinterpret_cast<const float *>(p.s) + b * p.s_bstride;
+  if (!p.s_rc && (reinterpret_cast<uintptr_t>(srow + wb) & 15) == 0) {
+    for (int u = tid; u < wlen / 4; u += kConvThreads) {
+      const int64_t g = wb + 4 * u;
+      float *dst = buf + win_swz(4 * u);
+      if (g >= 0 && g + 4 <= p.Ns) {
+        cp_async_zfill<16>(dst, srow + g, true);
+      } else {
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+          const bool ok = g + r >= 0 && g + r < p.Ns;
+          cp_async_zfill<4>(dst + r, ok ? srow + g + r : srow, ok);
+        }
+      }
+    }
+  } else {
+    for (int e = tid; e < wlen; e += kConvThreads) {
+      const int64_t gi = wb + e;
+      const bool ok = gi >= 0 && gi < p.Ns;
+      const int64_t si = p.s_rc ? p.Ns - 1 - gi : gi;
+      cp_async_zfill<4>(buf + win_swz(e), ok ? srow + si : srow, ok);
+    }
+  }
+}
+
+// One block of 8 taps: acc[e] += s[n_e - k] * tap[k] over k = kb..kb+7, where the 16 samples
+// below each thread's outputs are `prv` (older) then `cur`: the order of conv1d_direct.
+__device__ __forceinline__ void tap_block(float (&acc)[kConvE], const float (&cur)[kConvE],
+                                          const float (&prv)[kConvE], const float *tap) {
+  const float4 t0 = *reinterpret_cast<const float4 *>(tap);
+  const float4 t1 = *reinterpret_cast<const float4 *>(tap + 4);
+  const float tk[kConvE] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w};
+#pragma unroll
+  for (int kk = 0; kk < kConvE; kk++) {
+#pragma unroll
+    for (int e = 0; e < kConvE; e++)
+      acc[e] = fmaf((e >= kk) ? cur[e - kk] : prv[kConvE + e - kk], tk[kk], acc[e]);
+  }
+}
+
+// The 8 window samples at pos (a multiple of 8): two whole 16-byte units.
+__device__ __forceinline__ void load_block(float (&w)[kConvE], const float *win, int pos) {
+  const int a = win_swz(pos);
+  const float4 v0 = *reinterpret_cast<const float4 *>(win + a);
+  const float4 v1 = *reinterpret_cast<const float4 *>(win + (a ^ 4));
+  w[0] = v0.x; w[1] = v0.y; w[2] = v0.z; w[3] = v0.w;
+  w[4] = v1.x; w[5] = v1.y; w[6] = v1.z; w[7] = v1.w;
+}
+
+// NKB > 0: the filter is NKB blocks of 8 taps, fully unrolled; NKB == 0: any length up to
+// 1024 taps, two blocks per loop trip. Either way the two register windows swap roles from
+// block to block instead of being copied.
+template <int NKB>
+__global__ void __launch_bounds__(kConvThreads) conv1d_real_stream(const ConvParams p, int64_t ntiles) {
+  constexpr int E = kConvE;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int LC = NKB > 0 ? NKB * E : (int)((p.Lf + E - 1) / E * E);
+  const int nkb = LC / E;
+  const int wlen = kConvNB + LC;
+  float *taps = reinterpret_cast<float *>(smem_raw);
+  float *bufs = taps + LC;  // LC is a multiple of 8: 32-byte aligned
+  const float *frow = reinterpret_cast<const float *>(p.f);
+  const int tid = threadIdx.x;
+
+  for (int k = tid; k < LC; k += kConvThreads) taps[k] = k < p.Lf ? (p.f_rc ? frow[p.Lf - 1 - k] : frow[k]) : 0.f;
+
+  int64_t t = blockIdx.x;
+  if (t < ntiles) stream_issue(p, t, bufs, LC, tid);
+  cp_async_commit();
+  for (int it = 0; t < ntiles; it++, t += gridDim.x) {
+    const float *win = bufs + (it & 1) * wlen;
+    if (t + gridDim.x < ntiles) stream_issue(p, t + gridDim.x, bufs + ((it + 1) & 1) * wlen, LC, tid);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+
+    float acc[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) acc[e] = 0.f;
+    float wa[E], wb[E];
+    const int top = tid * E + LC;  // window index of the thread's first output sample
+    load_block(wa, win, top);
+    if constexpr (NKB > 0) {
+#pragma unroll
+      for (int j = 0; j < NKB; j += 2) {
+        load_block(wb, win, top - E * (j + 1));
+        tap_block(acc, wa, wb, taps + E * j);
+        if (j + 1 < NKB) {
+          load_block(wa, win, top - E * (j + 2));
+          tap_block(acc, wb, wa, taps + E * (j + 1));
+        }
+      }
+    } else {
+      int j = 0;
+#pragma unroll 1
+      for (; j + 2 <= nkb; j += 2) {
+        load_block(wb, win, top - E * (j + 1));
+        tap_block(acc, wa, wb, taps + E * j);
+        load_block(wa, win, top - E * (j + 2));
+        tap_block(acc, wb, wa, taps + E * (j + 1));
+      }
+      if (j < nkb) {
+        load_block(wb, win, top - E * (j + 1));
+        tap_block(acc, wa, wb, taps + E * j);
+      }
+    }
+
+    // each thread writes its 8 consecutive outputs (whole 32-byte sectors when aligned)
+    const int64_t b = t / p.chunks_per_row;
+    const int64_t o0 = (t - b * p.chunks_per_row) * (int64_t)kConvNB;
+    float *dst = reinterpret_cast<float *>(p.out) + b * p.out_bstride + o0 + tid * E;
+    const int64_t left = p.out_len - o0 - (int64_t)tid * E;
+    if (left >= E && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+      reinterpret_cast<float4 *>(dst)[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+      reinterpret_cast<float4 *>(dst)[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; e++)
+        if (e < left) dst[e] = acc[e];
+    }
+    __syncthreads();  // the buffer just read is the target of the next prefetch
+  }
+  cp_async_wait<0>();
+}
+
+static int launch_conv_real_stream(const ConvParams &p, int64_t batch, cudaStream_t s) {
+  const int LC = (int)((p.Lf + kConvE - 1) / kConvE * kConvE);
+  const size_t smem = (size_t)(LC + 2 * (kConvNB + LC)) * sizeof(float);
+  const void *fn;
+  switch (LC / kConvE) {
+    case 1: fn = (const void *)conv1d_real_stream<1>; break;
+    case 2: fn = (const void *)conv1d_real_stream<2>; break;
+    case 3: fn = (const void *)conv1d_real_stream<3>; break;
+    case 4: fn = (const void *)conv1d_real_stream<4>; break;
+    case 5: fn = (const void *)conv1d_real_stream<5>; break;
+    case 6: fn = (const void *)conv1d_real_stream<6>; break;
+    case 7: fn = (const void *)conv1d_real_stream<7>; break;
+    case 8: fn = (const void *)conv1d_real_stream<8>; break;
+    default: fn = (const void *)conv1d_real_stream<0>; break;
+  }
+  int rc = ensure_smem(fn, smem, "conv1d");
+  if (rc) return rc;
+  // resident CTAs per SM, per variant (registers bind before shared memory here)
+  static int occ_cache[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  int &occ = occ_cache[LC / kConvE <= 8 ? LC / kConvE : 0];
+  if (occ == 0) {
+    const size_t probe = (size_t)(kConvChunk + 2 * (kConvNB + kConvChunk)) * sizeof(float);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kConvThreads, probe) != cudaSuccess || occ < 1)
+      occ = 1;
+  }
+  const int64_t ntiles = p.chunks_per_row * batch;
+  const int64_t grid = std::min<int64_t>(ntiles, (int64_t)num_sms() * occ);
+  ConvParams pa = p;
+  int64_t nt = ntiles;
+  void *args[] = {(void *)&pa, (void *)&nt};
+  cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kConvThreads), args, smem, s);
+  return check_launch("conv1d");
+}
+
 template <typename T, bool SC, bool FC>
 static int launch_conv(const ConvParams &p, int64_t batch, cudaStream_t s) {
   using ST = typename val_of<T, SC>::type;
@@ -177,6 +358,7 @@ int conv1d_fp(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int
   if (sc && fcx) return launch_conv<float, true, true>(p, out.batch, s);
   if (sc) return launch_conv<float, true, false>(p, out.batch, s);
   if (fcx) return launch_conv<float, false, true>(p, out.batch, s);
+  if (p.f_bstride == 0 && p.Lf <= kConvChunk) return launch_conv_real_stream(p, out.batch, s);
   return launch_conv<float, false, false>(p, out.batch, s);
 }
 

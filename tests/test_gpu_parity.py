@@ -126,6 +126,40 @@ def test_conv_broadcast_signal(mx, orc):
     assert y.shape == r.shape and rel_l2(y, r) < FP32_TOL
 
 
+@pytest.mark.parametrize("B,N,L", [(2, 5000, 63), (5, 3001, 17), (3, 9000, 1024), (4, 40, 300), (7, 1, 1),
+                                   (9, 70000, 64), (2, 4100, 1000), (3, 2047, 8), (2, 3000, 40), (2, 3000, 52)])
+@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("is_corr", [False, True])
+@pytest.mark.parametrize("offset", [0, 1])
+def test_conv_real_stream_matches_tile_kernel(mx, orc, B, N, L, mode, is_corr, offset):
+    """Real rows with one shared filter of at most 1024 taps run on the persistent,
+    prefetching kernel; the same filter given once per row runs on the one-tile-per-CTA
+    kernel. Both make the same multiply-adds in the same order, so they agree bit for
+    bit. offset = 1 takes the rows from a slice one sample in (unaligned windows: the
+    4-byte copy path); odd output lengths give unaligned output rows."""
+    import torch
+    from matx_gb300 import _lib
+    rng = np.random.default_rng(seed_of("stream", B, N, L, mode, is_corr, offset))
+    x = rng.uniform(-1, 1, (B, N + offset)).astype(np.float32)
+    h = rng.standard_normal(L).astype(np.float32)
+    olen = (N + L - 1, max(N, L), max(N, L) - min(N, L) + 1)[mode]
+    xd, hd, hrows = dev(x), dev(h), dev(np.tile(h, (B, 1)))
+    f32 = mx._DT[torch.float32]
+    xb = _lib.Buf(xd.data_ptr() + 4 * offset, B, N, N + offset, f32)  # rows of a slice
+    lib = _lib.load()
+    ys = []
+    for hb in (_lib.Buf(hd.data_ptr(), 1, L, 0, f32), _lib.Buf(hrows.data_ptr(), B, L, L, f32)):
+        y = torch.empty(B, olen, device="cuda")
+        _lib.check(lib.gbfir_conv1d(_lib.Buf(y.data_ptr(), B, olen, olen, f32), xb, hb, mode, int(is_corr), 0,
+                                    mx._stream()))
+        ys.append(y)
+    y = ys[0]
+    assert torch.equal(y, ys[1])
+    r = orc.conv1d(np.ascontiguousarray(x[:, offset:]), h, mode, is_corr)
+    scale = np.linalg.norm(orc.conv1d(np.abs(x[:, offset:]), np.abs(h), mode, is_corr))
+    assert np.linalg.norm(host(y) - r) / max(np.linalg.norm(r), 0.1 * scale) < FP32_TOL
+
+
 def test_conv_config_rows(mx, orc):
     # C1: 8 x 2^20 real, 63-tap Hamming sinc, FULL; every row checked on a sample of rows
     rng = np.random.default_rng(2024)
