@@ -217,3 +217,39 @@ def test_ragged_plan_validation(lib):
     # launch refuses a plan that does not come from the planner (before touching the device)
     bad = RaggedPlanInfo(n, 300 * 1024, 0)
     assert lib.gbfir_ragged_resample(FAKE, 2, FAKE, ctypes.byref(bad), 0, FAKE, 256, None) == 1
+
+
+@pytest.mark.parametrize("updown", [(3, 2), (4, 5), (160, 147), (2, 1), (1, 7), (6, 4)])
+@pytest.mark.parametrize("tma_store", [False, True])
+def test_tuner_candidates_are_valid_tiles(lib, updown, tma_store):
+    """Every tile the autotuner would time is one the library accepts (registration is
+    host-only), the enumeration has no duplicates, and malformed tiles are refused."""
+    from matx_gb300 import autotune
+    up, down = updown
+    cands = list(autotune.candidates(up, down, tma_store))
+    assert cands and len(cands) == len(set(cands))
+    try:
+        for rq, wc, grp, nb in cands:
+            assert lib.gbfir_resample_tile_register(up, down, 61, rq, wc, grp, nb) == 0, (rq, wc, grp, nb)
+            assert (nb & 4 == 0) or tma_store
+        for bad in ((3, 1, 4, 1), (1, 3, 4, 1), (4, 12, 4, 1), (1, 1, 65, 1), (1, 1, 4, 3), (1, 1, 4, 8),
+                    (1, 17, 4, 1), (-1, 1, 4, 1)):
+            assert lib.gbfir_resample_tile_register(up, down, 61, *bad) != 0, bad
+        assert lib.gbfir_resample_tile_register(0, down, 61, 1, 1, 4, 1) != 0
+        assert lib.gbfir_resample_tile_register(up, down, 0, 1, 1, 4, 1) != 0
+    finally:
+        assert lib.gbfir_resample_tile_clear() == 0
+
+
+def test_tuner_cache_round_trip(tmp_path, monkeypatch):
+    from matx_gb300 import autotune
+    path = tmp_path / "sub" / "tiles.json"
+    monkeypatch.setattr(autotune, "CACHE", str(path))
+    assert autotune.load_cache() == {}
+    ent = {"GB300|torch.complex64|torch.float32|3/2|L61|N1048576|B64":
+           {"best": [4, 8, 20, 5], "best_ms": 0.37, "default_ms": 0.41}}
+    autotune._save_cache(ent)
+    assert autotune.load_cache() == ent
+    assert not os.path.exists(str(path) + ".tmp")
+    path.write_text("{not json")
+    assert autotune.load_cache() == {}
