@@ -231,9 +231,50 @@ def _peak():
     return peaks()[0]
 
 
-def run_conv1d(args, rank, world, dev):
+_FP32_PEAK = None
+
+
+def fp32_peak_tflops(dev):
+    """Nominal FP32 FMA peak of this GPU: SMs x 128 FMA/clock x 2 flop x the maximum SM clock
+    (nvidia-smi).  The measured-peaks file holds no FP32 figure, so fractions against it say
+    "of nominal"."""
+    global _FP32_PEAK
+    if _FP32_PEAK is None:
+        import torch
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        mhz = 2070.0
+        try:
+            out = subprocess.run(["nvidia-smi", f"--id={dev.index or 0}", "--query-gpu=clocks.max.sm",
+                                  "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=20)
+            mhz = float(out.stdout.strip().splitlines()[0])
+        except Exception:  # noqa: BLE001
+            pass
+        _FP32_PEAK = sms * 128 * 2 * mhz * 1e6 / 1e12
+    return _FP32_PEAK
+
+
+def tensor_peak_tflops():
+    """Dense bf16 tensor peak: the measured burst figure where the measured-peaks file has it,
+    else the stated fallback."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        for k in ("bf16_tflops", "bf16_tflops_burst"):
+            if k in d:
+                return float(d[k]), "measured"
+    return 1900.0, "fallback"
+
+
+def roofline_frac(ms, nbytes, flops, pipe_tflops):
+    """Fraction of the roofline reached: max(flops at the pipe's peak, bytes at HBM) / time."""
+    t_min = max(flops / (pipe_tflops * 1e12), nbytes / (_peak() * 1e9))
+    return t_min / (ms * 1e-3)
+
+
+def measure_conv1d(args, rank, world, dev, steps=None):
     """conv1d direct FULL, real fp32: 8 rows x 2^20 samples uniform[-1,1], one 63-tap
-    Hamming-windowed sinc low-pass (cut-off 0.25 of Nyquist, unit DC gain)."""
+    Hamming-windowed sinc low-pass (cut-off 0.25 of Nyquist, unit DC gain); FP32 and the
+    tensor-core forms, each with its error against FP64 on row 0."""
     import torch
     from scipy import signal
     import matx_gb300 as mx
@@ -249,12 +290,14 @@ def run_conv1d(args, rank, world, dev):
     for _ in range(args.warmup):
         run()
     l0 = mx.launch_count()
-    steps = max(3, min(args.steps, 100))
+    steps = steps or max(3, min(args.steps, 100))
     ms = _timed(run, steps, lambda: _flush_l2(flushbuf), stream)
     launches = mx.launch_count() - l0
     macs = B * N * L
     nbytes = B * 4 * (N + (N + L - 1)) + 4 * L
-    err = None
+    p32 = fp32_peak_tflops(dev)
+    ptc, ptc_kind = tensor_peak_tflops()
+    r = None
     try:
         import oracle
         oracle.build()
@@ -264,7 +307,8 @@ def run_conv1d(args, rank, world, dev):
         err = {"unavailable": str(e)[:160]}
     forms = {}
     for form in ("bf16x3", "bf16", "fp16"):
-        runf = lambda: mx.conv1d(x, hd, "full", out=y, precision=form)
+        yf = torch.empty_like(y)
+        runf = lambda: mx.conv1d(x, hd, "full", out=yf, precision=form)
         try:
             runf()
         except mx.GbfirError as ge:
@@ -273,20 +317,30 @@ def run_conv1d(args, rank, world, dev):
         for _ in range(args.warmup):
             runf()
         msf = _timed(runf, steps, lambda: _flush_l2(flushbuf), stream)
+        prods = 6 if form == "bf16x3" else 1
         ent = {"ms": msf, "gmacs": macs / (msf * 1e-3) / 1e9, "vs_fp32": ms / msf,
-               "hbm_frac": nbytes / (msf * 1e-3) / 1e9 / _peak()}
-        if isinstance(err, float):
-            ent["rel_l2_vs_fp64_row0"] = float(np.linalg.norm(y[:1].cpu().numpy() - r) / np.linalg.norm(r))
+               "hbm_frac": nbytes / (msf * 1e-3) / 1e9 / _peak(),
+               "roofline_frac": roofline_frac(msf, nbytes, 2 * macs * prods, ptc),
+               "rel_l2_vs_fp32_all_rows": float(((yf - y).double().norm() / y.double().norm()).item())}
+        if r is not None:
+            ent["rel_l2_vs_fp64_row0"] = float(np.linalg.norm(yf[:1].cpu().numpy() - r) / np.linalg.norm(r))
         forms[form] = ent
-    line = {"metric": "FIR GMAC/s (conv1d direct FULL, real fp32)", "value": macs / (ms * 1e-3) / 1e9,
+    return {"metric": "FIR GMAC/s (conv1d direct FULL, real fp32)", "value": macs / (ms * 1e-3) / 1e9,
             "unit": "GMAC/s", "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded uniform[-1,1]; Hamming sinc taps)",
             "config": {"workload": "conv1d FULL 8x2^20 f32, 63-tap Hamming sinc (cut-off 0.25)",
                        "l2": "flushed (256 MB write) before every timed launch"},
             "hbm_gbs": nbytes / (ms * 1e-3) / 1e9, "hbm_frac": nbytes / (ms * 1e-3) / 1e9 / _peak(),
-            "fp32_tflops": 2 * macs / (ms * 1e-3) / 1e12, "rel_l2_vs_fp64_row0": err, "gpu_launches": launches,
-            "forms": forms}
+            "fp32_tflops": 2 * macs / (ms * 1e-3) / 1e12,
+            "fp32_peak_tflops": p32, "fp32_peak_kind": "nominal (SMs x 128 FMA/clock x 2 x max SM clock)",
+            "roofline_frac": roofline_frac(ms, nbytes, 2 * macs, p32),
+            "tensor_peak_tflops": ptc, "tensor_peak_kind": ptc_kind,
+            "rel_l2_vs_fp64_row0": err, "gpu_launches": launches, "forms": forms}
+
+
+def run_conv1d(args, rank, world, dev):
+    line = measure_conv1d(args, rank, world, dev)
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
@@ -516,7 +570,7 @@ def run_conv2d(args, rank, world, dev):
     return 0
 
 
-def run_channelize(args, rank, world, dev):
+def measure_channelize(args, rank, world, dev, steps=None):
     """channelize_poly c64, maximally decimated: 4 rows x 2^24 samples, M = 64 with a
     64x32 Kaiser sinc prototype and M = 256 with 16 taps per channel; FP32 and the
     tensor-core DFT-GEMM forms."""
@@ -529,7 +583,7 @@ def run_channelize(args, rank, world, dev):
     flushbuf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
     res = {}
-    steps = max(3, min(args.steps, 30))
+    steps = steps or max(3, min(args.steps, 30))
     for M, P in ((64, 32), (256, 16)):
         h = torch.from_numpy(signal.firwin(M * P, 1.0 / M, window=("kaiser", 5.0)).astype(np.float32)).to(dev)
         T = (N + M - 1) // M
@@ -560,6 +614,9 @@ def run_channelize(args, rank, world, dev):
             if r64 is not None:
                 yy = y[1, :4096].cpu().numpy()
                 ent["rel_l2_vs_fp64"] = float(np.linalg.norm(yy - r64[0]) / np.linalg.norm(r64[0]))
+            base = res.get(f"M{M}/fp32", {})
+            if form != "fp32" and "ms" in base:
+                ent["vs_fp32"] = base["ms"] / ms
             res[f"M{M}/{form}"] = ent
     best = res["M64/fp32"]
     line = {"metric": "FIR GMAC/s (channelize_poly c64, FIR branch MACs; DFT fused)",
@@ -569,16 +626,36 @@ def run_channelize(args, rank, world, dev):
             "config": {"workload": "channelize_poly c64 4x2^24, D = M, M=64 (P=32) and M=256 (P=16)",
                        "l2": "inputs larger than L2, also flushed before every timed launch"},
             "forms": res}
+    return line
+
+
+def run_channelize(args, rank, world, dev):
+    line = measure_channelize(args, rank, world, dev)
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
 
 
-def run_fwdbwd(args, rank, world, dev):
+def _fwdbwd_errors(x, h, up, down, form, oracle_res):
+    """rel-L2 of y, dL/dx and dL/dh of one form against the FP64 oracle for a fixed upstream
+    gradient (untimed)."""
+    import torch
+    import matx_gb300 as mx
+    from matx_gb300 import autograd as ag
+    xs, hs, gy, y64, dx64, dh64 = oracle_res
+    with torch.no_grad():
+        y = mx.resample_poly(xs, hs, up, down, precision=form)
+        dx, dh = ag.resample_poly_bwd(gy, xs, hs, up, down, precision=form)
+    rel = lambda a, b: float(np.linalg.norm(a.cpu().numpy().astype(np.float64) - b) / np.linalg.norm(b))
+    return {"y": rel(y, y64), "dx": rel(dx, dx64), "dh": rel(dh, dh64)}
+
+
+def measure_fwdbwd(args, rank, world, dev, steps=None):
     """Differentiable FIR fp32: 256 rows x 16384 samples uniform[-1,1], a learnable 127-tap
     filter N(0, 1/127), loss = MSE against the output of a fixed seeded Kaiser filter; one
     step = forward + backward.  (3, 2) runs resample_poly; the (1, 1) case runs conv1d SAME,
-    since resample_poly at up == down is MatX's identity copy with a zero tap gradient."""
+    since resample_poly at up == down is MatX's identity copy with a zero tap gradient.
+    Each form states the rel-L2 of y, dL/dx and dL/dh against the FP64 oracle."""
     import torch
     from scipy import signal
     import matx_gb300 as mx
@@ -589,7 +666,7 @@ def run_fwdbwd(args, rank, world, dev):
     flushbuf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
     res = {}
-    steps = max(3, min(args.steps, 100))
+    steps = steps or max(3, min(args.steps, 100))
     total_macs, total_ms = 0, 0.0
     for up, down in ((3, 2), (1, 1)):
         h = (torch.randn(L, device=dev, generator=g) / L ** 0.5).requires_grad_(True)
@@ -620,6 +697,20 @@ def run_fwdbwd(args, rank, world, dev):
         total_macs += macs
         total_ms += ms
         if (up, down) == (3, 2):
+            oracle_res = None
+            try:
+                import oracle
+                oracle.build()
+                xs, hs = x.detach(), h.detach()
+                gy = torch.randn(B, mx.resample_out_len(N, up, down), device=dev, generator=g)
+                nthr = os.cpu_count() or 1
+                y64 = oracle.resample_poly(xs.cpu().numpy(), hs.cpu().numpy(), up, down, double=True, nthreads=nthr)
+                dx64, dh64 = oracle.resample_poly_bwd(gy.cpu().numpy(), xs.cpu().numpy(), hs.cpu().numpy(), up, down,
+                                                      nthreads=nthr)
+                oracle_res = (xs, hs, gy, y64, dx64, dh64)
+                res[key]["rel_l2_vs_fp64"] = _fwdbwd_errors(x, h, up, down, "fp32", oracle_res)
+            except Exception as e:  # noqa: BLE001
+                res[key]["rel_l2_vs_fp64"] = {"unavailable": str(e)[:160]}
             # tensor-core forms of the forward and dL/dx (dL/dh stays FP32 with FP64 sums)
             forms = {}
             for form in ("bf16x3", "bf16", "fp16"):
@@ -637,8 +728,10 @@ def run_fwdbwd(args, rank, world, dev):
                     step_f()
                 msf = _timed(step_f, steps, lambda: _flush_l2(flushbuf), stream)
                 forms[form] = {"ms": msf, "gmacs": macs / (msf * 1e-3) / 1e9, "vs_fp32": ms / msf}
+                if oracle_res is not None:
+                    forms[form]["rel_l2_vs_fp64"] = _fwdbwd_errors(x, h, up, down, form, oracle_res)
             res["3/2"]["forms"] = forms
-    line = {"metric": "FIR GMAC/s (resample_poly fp32 forward + backward, dL/dx and dL/dh)",
+    return {"metric": "FIR GMAC/s (resample_poly fp32 forward + backward, dL/dx and dL/dh)",
             "value": total_macs / (total_ms * 1e-3) / 1e9, "unit": "GMAC/s", "n_gpus": world, "steps": steps,
             "warmup": args.warmup, "ms_per_step": total_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform[-1,1]; N(0,1/127) taps)",
@@ -646,6 +739,10 @@ def run_fwdbwd(args, rank, world, dev):
                                    "conv1d SAME; MSE loss, torch.autograd through the hand-written adjoints",
                        "l2": "flushed (256 MB write) before every timed step"},
             "per_ratio": res}
+
+
+def run_fwdbwd(args, rank, world, dev):
+    line = measure_fwdbwd(args, rank, world, dev)
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
@@ -654,10 +751,33 @@ def run_fwdbwd(args, rank, world, dev):
 RAGGED_RATIOS = [(1, 2), (2, 3), (3, 4), (5, 4), (160, 147)]
 
 
-def run_ragged(args, rank, world, dev):
+def _graph_ms(fn, steps):
+    """Per-replay time of fn captured in a CUDA graph (stream-ordered, CUDA events)."""
+    import torch
+    sg = torch.cuda.Stream()
+    sg.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(sg):
+        fn()
+    torch.cuda.current_stream().wait_stream(sg)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        fn()
+    graph.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        graph.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def measure_ragged(args, rank, world, dev, steps=None):
     """4096 complex64 signals, log-uniform lengths in [1e3, 1e6], odd taps uniform in
     [15, 511], (up, down) drawn from RAGGED_RATIOS, Kaiser sinc filters: one persistent
-    launch vs one plain launch per signal."""
+    launch (graph-captured) vs one plain launch per signal, in FP32 and the tensor-core
+    forms the ragged launch takes."""
     import torch
     from scipy import signal
     import matx_gb300 as mx
@@ -683,7 +803,7 @@ def run_ragged(args, rank, world, dev):
     for _ in range(args.warmup):
         plan.run()
     torch.cuda.synchronize()
-    steps = max(3, min(args.steps, 50))
+    steps = steps or max(3, min(args.steps, 50))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = mx.launch_count()
     e0.record()
@@ -693,37 +813,37 @@ def run_ragged(args, rank, world, dev):
     torch.cuda.synchronize()
     launches = mx.launch_count() - l0
     ms_ragged = e0.elapsed_time(e1) / steps
-    # CUDA graph of the same launch
-    sg = torch.cuda.Stream()
-    sg.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(sg):
-        plan.run()
-    torch.cuda.current_stream().wait_stream(sg)
-    graph = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(graph):
-        plan.run()
-    graph.replay()
-    torch.cuda.synchronize()
-    e0.record()
-    for _ in range(steps):
-        graph.replay()
-    e1.record()
-    torch.cuda.synchronize()
-    ms_graph = e0.elapsed_time(e1) / steps
+    ms_graph = _graph_ms(plan.run, steps)
     # one plain launch per signal
     outs = plan.outputs
     for (x, h, up, down), y in zip(sigs, outs):
         mx.resample_poly(x, h, up, down, out=y)
     torch.cuda.synchronize()
+    reps = max(1, steps // 10)
     e0.record()
-    for _ in range(max(1, steps // 10)):
+    for _ in range(reps):
         for (x, h, up, down), y in zip(sigs, outs):
             mx.resample_poly(x, h, up, down, out=y)
     e1.record()
     torch.cuda.synchronize()
-    ms_single = e0.elapsed_time(e1) / max(1, steps // 10)
+    ms_single = e0.elapsed_time(e1) / reps
     in_bytes = int(lens.sum()) * 8
-    line = {
+    nbytes = in_bytes + outs_total * 8
+    forms = {}
+    ref = [y.clone() for y in outs[:64]]
+    for form in ("bf16x3", "bf16", "fp16"):
+        try:
+            plan.run(precision=form)
+        except mx.GbfirError as ge:
+            forms[form] = {"unavailable": str(ge)[:160]}
+            continue
+        msf = _graph_ms(lambda: plan.run(precision=form), steps)
+        num = sum(float((a - b).abs().pow(2).sum()) for a, b in zip(plan.outputs[:64], ref))
+        den = sum(float(b.abs().pow(2).sum()) for b in ref)
+        forms[form] = {"graph_ms": msf, "gmacs": macs / (msf * 1e-3) / 1e9, "vs_fp32": ms_graph / msf,
+                       "hbm_frac": nbytes / (msf * 1e-3) / 1e9 / _peak(),
+                       "rel_l2_vs_fp32_first64": (num / den) ** 0.5}
+    return {
         "metric": "FIR GMAC/s (ragged resample_poly c64, one persistent launch)",
         "value": macs / (ms_graph * 1e-3) / 1e9, "unit": "GMAC/s", "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": ms_graph, "higher_is_better": True, "scaling": "weak",
@@ -734,12 +854,44 @@ def run_ragged(args, rank, world, dev):
         "ragged_ms": ms_ragged, "ragged_graph_ms": ms_graph, "per_signal_launches_ms": ms_single,
         "speedup_vs_per_signal": ms_single / ms_graph,
         "output_samples_per_s": outs_total / (ms_graph * 1e-3),
-        "hbm_gbs": (in_bytes + outs_total * 8) / (ms_graph * 1e-3) / 1e9,
-        "gpu_launches": launches,
+        "hbm_gbs": nbytes / (ms_graph * 1e-3) / 1e9, "hbm_frac": nbytes / (ms_graph * 1e-3) / 1e9 / _peak(),
+        "gpu_launches": launches, "forms": forms,
     }
+
+
+def run_ragged(args, rank, world, dev):
+    line = measure_ragged(args, rank, world, dev)
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def _summary(line, keys):
+    return {k: line[k] for k in keys if k in line}
+
+
+def measure_configs(args, rank, world, dev):
+    """The other configurations of the headline metric, measured after the C2 step: C1 conv1d,
+    C3 channelize_poly, C4 forward + backward, C5 ragged, each in FP32 and the tensor-core
+    forms with their error against FP64 (short runs: a few timed launches each)."""
+    out = {}
+    steps = max(3, min(args.steps, 10))
+    plan = (("C1_conv1d", measure_conv1d, ("ms_per_step", "value", "unit", "hbm_frac", "fp32_tflops",
+                                           "fp32_peak_tflops", "fp32_peak_kind", "roofline_frac",
+                                           "tensor_peak_tflops", "tensor_peak_kind", "rel_l2_vs_fp64_row0",
+                                           "forms", "config")),
+            ("C3_channelize", measure_channelize, ("forms", "config")),
+            ("C4_fwdbwd", measure_fwdbwd, ("ms_per_step", "value", "unit", "per_ratio", "config")),
+            ("C5_ragged", measure_ragged, ("ms_per_step", "value", "unit", "hbm_frac", "per_signal_launches_ms",
+                                           "speedup_vs_per_signal", "forms", "config")))
+    for name, fn, keys in plan:
+        try:
+            t0 = time.perf_counter()
+            out[name] = _summary(fn(args, rank, world, dev, steps), keys)
+            out[name]["wall_s"] = time.perf_counter() - t0
+        except Exception as e:  # noqa: BLE001 - one config failing leaves the others standing
+            out[name] = {"unavailable": f"{type(e).__name__}: {str(e)[:200]}"}
+    return out
 
 
 def main():
@@ -752,6 +904,8 @@ def main():
     ap.add_argument("--precision", default="fp32")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the C1/C3/C4/C5 configurations appended to the headline line")
     ap.add_argument("--batch", type=int, default=BATCH, help="rows per GPU (profiling cases)")
     ap.add_argument("--no-tune", action="store_true", help="use the built-in tile heuristic")
     ap.add_argument("--tiles", default="",
@@ -980,6 +1134,11 @@ def main():
                "kind": "reference" if use_ref else "port",
                "sample": "the full step (64 rows x 2^20 at the three ratios), one timed pass after a 4-row warm-up"}
 
+    # ---- the headline metric's other configurations (N = 1 only, after the timed region) ----
+    configs = None
+    if rank == 0 and world == 1 and not args.no_configs and not args.no_e2e and prec == "fp32":
+        configs = measure_configs(args, rank, world, dev)
+
     if rank == 0:
         line = {
             "metric": "FIR GMAC/s (resample_poly c64, algorithmic complex x real MACs)",
@@ -1002,6 +1161,7 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": launches,
+            "configs": configs,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

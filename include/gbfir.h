@@ -269,9 +269,11 @@ GBFIR_API int gbfir_resample_poly_bwd_prec(gbfir_buf dx, gbfir_buf dh, gbfir_buf
  * GBFIR_ERR_INVALID_SIZE before any device work.  Nothing here calls cudaMalloc or
  * cudaFree.  The first call on each device looks the array's device address up
  * (cudaGetSymbolAddress) with that device current; make that first call before any
- * stream capture.  All calls share the one array: calls whose work overlaps on the
- * GPU (different streams without ordering, or different host threads) race on it and
- * must be serialised by the caller. */
+ * stream capture.  The address is kept for the life of the process, so a
+ * cudaDeviceReset() of a device (which unloads the library's device code there) ends
+ * this entry point's use on that device.  All calls share the one array: calls whose
+ * work overlaps on the GPU (different streams without ordering, or different host
+ * threads) race on it and must be serialised by the caller. */
 #define GBFIR_NOALLOC_SCRATCH_BYTES (4u << 20)
 GBFIR_API int gbfir_resample_poly_bwd_noalloc(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy,
                                               gbfir_buf x, gbfir_buf h, int64_t up,
@@ -345,16 +347,6 @@ GBFIR_API int gbfir_resample_tile_register(int64_t up, int64_t down, int64_t h_l
                                  int32_t rows_per_thread, int32_t col_warps,
                                  int32_t group, int32_t buffers);
 GBFIR_API int gbfir_resample_tile_clear(void);
-
-/* Diagnostic: C[M][N] = A[M][K] * B[N][K]^T on the tcgen05 tensor cores (no MatX
- * counterpart).  FP32 in/out; operands rounded to bf16 (terms = 1) or split into three
- * bf16 terms with the six products of order <= 2 accumulated in FP32 (terms = 3).
- * M % 128 == 0, N in [16, 256] step 16, K in {16, 32, 48, 64}.  swap_offsets exchanges
- * the two shared-memory descriptor offsets (layout check).  *status (device int) is set
- * to 1 if a bounded wait in the kernel gave up. */
-GBFIR_API int gbfir_tc_gemm_selftest(const float *A, const float *B, float *C, int32_t M,
-                           int32_t N, int32_t K, int32_t terms, int32_t swap_offsets,
-                           int32_t *status, gbfir_stream_t stream);
 
 /* Status of the bounded waits inside the pipelined kernels of the current device (the
  * tensor-core kernels and the TMA-fed row tile) since the last call: 0 = none gave up,

@@ -78,7 +78,6 @@ SIGNATURES = [
     ("gbfir_set_resample_tile", ctypes.c_int, [_i32, _i32, _i32, _i32]),
     ("gbfir_resample_tile_register", ctypes.c_int, [_i64, _i64, _i64, _i32, _i32, _i32, _i32]),
     ("gbfir_resample_tile_clear", ctypes.c_int, []),
-    ("gbfir_tc_gemm_selftest", ctypes.c_int, [_p, _p, _p, _i32, _i32, _i32, _i32, _i32, _p, _p]),
     ("gbfir_tc_status", ctypes.c_int, []),
     ("gbfir_launch_count", ctypes.c_uint64, []),
     ("gbfir_status_string", ctypes.c_char_p, [ctypes.c_int]),

@@ -19,6 +19,10 @@
 // Real rows with one shared real filter of at most 1024 taps take conv1d_real_stream
 // (persistent CTAs, prefetched windows, unrolled tap blocks), which makes the same
 // multiply-adds in the same order.
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "common.cuh"
 
 namespace gbfir {
@@ -291,20 +295,31 @@ static int launch_conv_real_stream(const ConvParams &p, int64_t batch, cudaStrea
   }
   int rc = ensure_smem(fn, smem, "conv1d");
   if (rc) return rc;
-  // resident CTAs per SM, per variant (registers bind before shared memory here)
-  static int occ_cache[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  int &occ = occ_cache[LC / kConvE <= 8 ? LC / kConvE : 0];
-  if (occ == 0) {
-    const size_t probe = (size_t)(kConvChunk + 2 * (kConvNB + kConvChunk)) * sizeof(float);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kConvThreads, probe) != cudaSuccess || occ < 1)
-      occ = 1;
+  // resident CTAs per SM of this variant at this shared-memory size, per device
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+  int occ = 0;
+  {
+    static std::mutex mu;
+    static std::map<std::tuple<int, const void *, size_t>, int> occ_cache;
+    std::lock_guard<std::mutex> lk(mu);
+    const auto key = std::make_tuple(dev, fn, smem);
+    auto it = occ_cache.find(key);
+    if (it != occ_cache.end()) {
+      occ = it->second;
+    } else {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kConvThreads, smem) != cudaSuccess || occ < 1)
+        occ = 1;
+      occ_cache[key] = occ;
+    }
   }
   const int64_t ntiles = p.chunks_per_row * batch;
   const int64_t grid = std::min<int64_t>(ntiles, (int64_t)num_sms() * occ);
   ConvParams pa = p;
   int64_t nt = ntiles;
   void *args[] = {(void *)&pa, (void *)&nt};
-  cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kConvThreads), args, smem, s);
+  const cudaError_t e = cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kConvThreads), args, smem, s);
+  if (e != cudaSuccess) GBFIR_FAIL(GBFIR_ERR_CUDA, "conv1d: %s", cudaGetErrorString(e));
   return check_launch("conv1d");
 }
 

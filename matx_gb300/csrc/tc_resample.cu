@@ -2,31 +2,41 @@
 // (bf16, fp16 and bf16x3 split precision, FP32 accumulate in TMEM).  No MatX counterpart.
 //
 // Math.  With gcd-reduced rates, y[n] = up * sum_i x[i] * he[c + n*down - i*up].
-// The kernel groups outputs into rows whose inputs advance by exactly 8 samples of a
-// linear array xs, so that the Hankel operand A[q][k] = xs[8q + k] is a plain
-// K-major shared-memory matrix with overlapping rows: its 8-row x 16-byte core
-// matrices are 16 bytes apart along K (LBO = 16) and 128 bytes apart along rows
-// (SBO = 128), and no Hankel matrix is ever materialised.
-//   path A (down divides 8): xs[u] = x[u + k0]; a row holds Nt = 8*up/down outputs and
-//     D[q][j] = sum_k xs[8q + k] * W[j][k],  W[j][k] = up*he[c + j*down - (k + k0)*up].
+// The kernel groups outputs into rows whose inputs advance by exactly R samples (the row
+// pitch, 8 or 64) of a linear array xs, so that the Hankel operand A[q][k] = xs[R*q + k]
+// is a K-major shared-memory matrix with overlapping rows and no Hankel matrix is ever
+// materialised:
+//   R = 8:  no-swizzle layout; the 8-row x 16-byte core matrices are 16 bytes apart along
+//           K (LBO = 16) and 128 bytes apart along rows (SBO = 128).
+//   R = 64: 128-byte-swizzled layout; an operand row is 64 bf16 = 128 bytes, so xs stored
+//           linearly with the swizzle applied at its (1024-aligned) addresses is exactly
+//           A with rows 128 bytes apart (SBO = 1024 per 8-row group), K-step s starting
+//           32*s bytes in.  Rows of 64 inputs give N = 64*up/down MMA columns instead of
+//           8*up/down, so each MMA does eight times the work for the same issue cost.
+//   path A (down divides R): xs[u] = x[u + k0]; a row holds Nt = R*up/down outputs and
+//     D[q][j] = sum_k xs[R*q + k] * W[j][k],  W[j][k] = up*he[c + j*down - (k + k0)*up].
 //   path B (other down): x is split into its `down` polyphase components
 //     xs_b[a] = x[down*a + b]; each is an interpolator (rate up) and a row holds
-//     Nt = 8*up outputs:  D[q][j] = sum_b sum_k xs_b[8q + k + k0] * W_b[j][k],
+//     Nt = R*up outputs:  D[q][j] = sum_b sum_k xs_b[R*q + k + k0] * W_b[j][k],
 //     W_b[j][k] = up*he[c + down*j - up*(b + down*(k + k0))].
 // The tap matrices W (N = Nt rounded up to 16 columns, Kp = band rounded to 16) are
 // built once per CTA.  Complex x runs as two M = 128 MMAs (real, imaginary rows) on the
 // same W.  bf16x3 splits both operands into three bf16 terms and accumulates the six
 // products of order <= 2 (smallest first) — 24 significant bits, FP32-class accuracy.
 //
-// bf16x3 concatenates the three tap terms along N (W_cat = [b0 | b1 | b2]) so one K-step
-// is three MMAs — a0*[b0|b1|b2] into D[0:3N), a1*[b0|b1] into D[N:3N), a2*b0 into
-// D[2N:3N) — and the epilogue sums the three column blocks: exactly the six products of
-// order <= 2, with the small terms accumulated apart from a0*b0.
+// bf16x3 with 3*N <= 256 concatenates the three tap terms along N (W_cat = [b0 | b1 | b2])
+// so one K-step is three MMAs — a0*[b0|b1|b2] into D[0:3N), a1*[b0|b1] into D[N:3N), a2*b0
+// into D[2N:3N) — and the epilogue sums the three column blocks: exactly the six products
+// of order <= 2, with the small terms accumulated apart from a0*b0.  Wider rows issue the
+// six products as six MMAs of N columns into one accumulator.
 //
 // Pipeline (persistent, warp-specialised CTA; roles below).  A stage covers MT M-tiles
 // of 128 rows; raw input is staged two stages ahead with cp.async, converted into a
 // two-slot operand ring, multiplied into one of two TMEM accumulator sets and drained
 // by the epilogue warps while the next stage's MMAs run.
+#include <cstdlib>
+#include <cstring>
+
 #include "rowtile.cuh"
 #include "tc.cuh"
 
@@ -48,7 +58,7 @@ struct TcParams {
   int32_t Kp;       // K band (multiple of 16)
   int64_t k0;       // aligned band start (multiple of 8)
   int32_t MT;       // M-tiles (128 rows) per iteration
-  int32_t LA;       // elements per xs array per buffer = 8*128*MT + Kp
+  int32_t LA;       // elements per xs array per buffer = rp*128*MT + Kp
   int32_t terms;    // 1 or 3
   int32_t fp16;     // 1: fp16 operands (single term), 0: bf16
   int64_t rows;     // rows per signal row = ceil(out_len / Nt)
@@ -58,17 +68,22 @@ struct TcParams {
   int32_t nbuf;     // operand ring slots (1 or 2)
   int32_t nsets;    // TMEM accumulator sets (1 or 2)
   int32_t nraw;     // raw staging slots: 2 = stage two iterations ahead, 1 = one ahead
+  int32_t rp;       // Hankel row pitch in samples: 8 (no swizzle) or 64 (128-byte swizzle)
+  int32_t concat;   // bf16x3: 1 = tap terms concatenated along N, 0 = six MMAs into one
+  int32_t acols;    // TMEM accumulator columns per (M-tile, part): 3*Nmma (concat) or Nmma
 };
 
 // Bounded-wait status of the tensor-core kernels (1 = a wait gave up); read and
 // cleared by gbfir_tc_status().
 __device__ int32_t g_tc_status;
 
-__device__ __forceinline__ float tap_value(const TcParams &p, int64_t tp) {
+// Tap he(tp) of the logical filter (reversed when rev, 0 outside), read from hs: the filter's
+// taps staged in shared memory, or the global row.
+__device__ __forceinline__ float tap_value(const TcParams &p, const float *hs, int64_t tp) {
   if (tp < 0 || tp >= p.Lo) return 0.f;
   const int64_t te = p.rev ? p.Lo - 1 - tp : tp;
   if (p.even && te == 0) return 0.f;
-  return p.h[te - p.even];
+  return hs[te - p.even];
 }
 
 // Warp roles (12 warps): warp 0 lane 0 issues the MMAs; warps 1-7 stage raw input with
@@ -91,19 +106,22 @@ template <bool XC>
 __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcParams p) {
   using XT = typename val_of<float, XC>::type;
   constexpr int NPARTS = XC ? 2 : 1;  // real / imaginary operand rows
-  extern __shared__ __align__(128) unsigned char smem[];
+  extern __shared__ __align__(1024) unsigned char smem_dyn[];
   __shared__ uint64_t op_full[2], op_empty[2], tm_full[2], tm_empty[2];
   __shared__ uint32_t tmem_slot;
   __shared__ int s_fail, s_pok, s_eok;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-  // shared layout: W_cat [P][terms*Nmma rows][Kp] ; operand ring [nbuf][NPARTS][terms][P][LA] ;
-  // raw ring [nraw][P*LA]
+  // shared layout (1024-aligned; the 128-byte swizzle pattern follows address bits 4-9):
+  // W_cat [P][terms*Nmma rows][Kp] ; operand ring [nbuf][NPARTS][terms][P][LA] ; raw ring
+  // [nraw][P*LA]
+  unsigned char *smem = smem_dyn + ((1024u - (tc::smem_u32(smem_dyn) & 1023u)) & 1023u);
   const int wrows = p.terms * p.Nmma;
   const uint32_t wbytes = (uint32_t)wrows * p.Kp * 2u;
   unsigned char *wbase = smem;
-  unsigned char *xbase = smem + ((size_t)p.P * wbytes + 127) / 128 * 128;
-  const size_t xarr = ((size_t)p.LA * 2 + 127) / 128 * 128;
+  unsigned char *xbase = smem + ((size_t)p.P * wbytes + 1023) / 1024 * 1024;
+  const size_t xalign = p.rp == 64 ? 1024 : 128;
+  const size_t xarr = ((size_t)p.LA * 2 + xalign - 1) / xalign * xalign;
   auto warr = [&](int pp) { return wbase + (size_t)pp * wbytes; };
   auto xarrp = [&](int slot, int part, int t, int pp) {
     return xbase + ((((size_t)slot * NPARTS + part) * p.terms + t) * p.P + pp) * xarr;
@@ -123,6 +141,15 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
     s_fail = 0;
     tc::mbar_fence_init();
   }
+  // The filter's taps, staged once into the raw ring (not in use yet) so that the W build
+  // reads shared memory instead of making one dependent global load per element.
+  const int64_t Lh = p.Lo - p.even;
+  const bool h_staged = (size_t)Lh * sizeof(float) <= (size_t)p.nraw * raw_elems * sizeof(XT);
+  float *hs_stage = reinterpret_cast<float *>(raw0);
+  if (h_staged)
+    for (int64_t e = tid; e < Lh; e += kWsThreads) hs_stage[e] = p.h[e];
+  __syncthreads();
+  const float *hsrc = h_staged ? hs_stage : p.h;
   // ---- W_cat[pp][t*Nmma + j][k] = term t of up*he[tap(j, k)] (K-major core layout) ----
   const int wel = wrows * p.Kp;
   for (int e = tid; e < p.P * wel; e += kWsThreads) {
@@ -134,7 +161,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
       const int64_t kk = k + p.k0;
       const int64_t tp = p.path == 0 ? p.c + (int64_t)j * p.down - kk * p.up
                                      : p.c + p.down * (int64_t)j - p.up * (pp + p.down * kk);
-      v = tap_value(p, tp) * (float)p.scale;
+      v = tap_value(p, hsrc, tp) * (float)p.scale;
     }
     const uint32_t off = tc::kmajor_offset(row, k, p.Kp);
     if (p.fp16) {
@@ -150,7 +177,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = tmem_slot;
-  const uint32_t set_cols = (uint32_t)(p.MT * NPARTS * wrows);
+  const uint32_t set_cols = (uint32_t)(p.MT * NPARTS * p.acols);
   const XT *xp = reinterpret_cast<const XT *>(p.x);
   (void)xp;
 
@@ -161,12 +188,22 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
       const int64_t b = itx / p.iters_per_row;
       const int64_t q0 = (itx - b * p.iters_per_row) * (int64_t)(128 * p.MT);
       const XT *row = xp + b * p.x_bstride;
-      const int64_t base = p.path == 0 ? 8 * q0 + p.k0 : p.down * (8 * q0 + p.k0);
+      const int64_t base = p.path == 0 ? p.rp * q0 + p.k0 : p.down * (p.rp * q0 + p.k0);
       XT *dst = rawp(slot);
-      for (int v = ptid; v < (int)raw_elems; v += kNProd) {
-        const int64_t gi = base + v;
-        const bool okk = gi >= 0 && gi < p.N;
-        cp_async_zfill<sizeof(XT)>(dst + v, okk ? (const void *)(row + gi) : (const void *)row, okk);
+      constexpr int G = 16 / (int)sizeof(XT);
+      // windows inside the signal with a 16-byte aligned start come in 16-byte pieces; the
+      // others element by element, zero-filled outside the signal
+      const bool vec = ((reinterpret_cast<uintptr_t>(row + base) | (uintptr_t)tc::smem_u32(dst)) & 15) == 0 &&
+                       base >= 0 && base + (int64_t)raw_elems <= p.N && raw_elems % G == 0;
+      if (vec) {
+        for (int v = ptid; v < (int)(raw_elems / G); v += kNProd)
+          cp_async_zfill<16>(dst + (size_t)v * G, row + base + (int64_t)v * G, true);
+      } else {
+        for (int v = ptid; v < (int)raw_elems; v += kNProd) {
+          const int64_t gi = base + v;
+          const bool okk = gi >= 0 && gi < p.N;
+          cp_async_zfill<sizeof(XT)>(dst + v, okk ? (const void *)(row + gi) : (const void *)row, okk);
+        }
       }
     };
     const int nraw = p.nraw;
@@ -193,8 +230,11 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
         break;
       }
       // convert raw slot -> operand slot: two consecutive samples of one component per item
+      // (with 64-sample rows the 4-byte pair at byte o goes to the 128-byte-swizzled slot
+      // o ^ ((o >> 7) & 7) << 4; a warp writes one 128-byte row, conflict-free)
       const XT *src = rawp(rslot);
       const int half = p.LA / 2;
+      const uint32_t swz = p.rp == 64 ? 7u : 0u;
       for (int pp = 0; pp < p.P; pp++) {
         unsigned char *dst[NPARTS][3];
 #pragma unroll
@@ -203,6 +243,8 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
           for (int t = 0; t < 3; t++) dst[part][t] = xarrp(slot, part, t < p.terms ? t : 0, pp);
         for (int v = ptid; v < half; v += kNProd) {
           const int u = 2 * v;
+          const uint32_t o = 4u * (uint32_t)v;
+          const uint32_t po = o ^ (((o >> 7) & swz) << 4);
           XT v0, v1;
           if (p.P == 1) {
             if constexpr (XC) {
@@ -222,14 +264,14 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
           for (int part = 0; part < NPARTS; part++) {
             const float2 f = part == 0 ? make_float2(re_of(v0), re_of(v1)) : make_float2(im_of(v0), im_of(v1));
             if (p.fp16) {
-              reinterpret_cast<__half2 *>(dst[part][0])[v] = __float22half2_rn(f);
+              *reinterpret_cast<__half2 *>(dst[part][0] + po) = __float22half2_rn(f);
             } else {
               __nv_bfloat162 t0, t1, t2;
               tc::split3_bf16x2(f, t0, t1, t2);
-              reinterpret_cast<__nv_bfloat162 *>(dst[part][0])[v] = t0;
+              *reinterpret_cast<__nv_bfloat162 *>(dst[part][0] + po) = t0;
               if (p.terms == 3) {
-                reinterpret_cast<__nv_bfloat162 *>(dst[part][1])[v] = t1;
-                reinterpret_cast<__nv_bfloat162 *>(dst[part][2])[v] = t2;
+                *reinterpret_cast<__nv_bfloat162 *>(dst[part][1] + po) = t1;
+                *reinterpret_cast<__nv_bfloat162 *>(dst[part][2] + po) = t2;
               }
             }
           }
@@ -246,15 +288,26 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
     cp_async_wait<0>();
   } else if (warp == 0) {
     // ================= MMA issuer =================
-    if (lane == 0) {
+    // every TMEM column the MMAs touch lies inside the allocation (checked once)
+    const bool geom_ok = (p.rp == 8 || p.rp == 64) && p.Nmma % 16 == 0 && p.Nmma <= 256 &&
+                         (!p.concat || 3 * p.Nmma <= 256) && p.Kp % 16 == 0 &&
+                         (uint32_t)p.nsets * set_cols <= (uint32_t)p.tmem_cols;
+    if (lane == 0 && !geom_ok) s_fail = 1;
+    if (lane == 0 && geom_ok) {
       const uint32_t idesc3 = tc::idesc_f16(128, (uint32_t)(3 * p.Nmma), 1u);
       const uint32_t idesc2 = tc::idesc_f16(128, (uint32_t)(2 * p.Nmma), 1u);
       const uint32_t idesc1 = tc::idesc_f16(128, (uint32_t)p.Nmma, p.fp16 ? 0u : 1u);
       const uint32_t wsbo = (uint32_t)(p.Kp / 8) * 128u;
       const int nks = p.Kp / 16;
-      // descriptor fields that never change; only the 14-bit start address (bytes >> 4) moves
-      const uint64_t afix = tc::smem_desc(0u, 16u, 128u), bfix = tc::smem_desc(0u, 128u, wsbo);
+      // descriptor fields that never change; only the 14-bit start address (bytes >> 4) moves.
+      // 64-sample rows: 128-byte swizzle (layout type 2), 8-row groups 1024 bytes apart, base
+      // offset 0 (the swizzle follows the absolute address, so starts inside a row are exact)
+      const uint64_t afix = p.rp == 64 ? (tc::smem_desc(0u, 16u, 1024u) | ((uint64_t)2 << 61))
+                                       : tc::smem_desc(0u, 16u, 128u);
+      const uint64_t bfix = tc::smem_desc(0u, 128u, wsbo);
       const uint32_t xs0 = tc::smem_u32(xbase), w0 = tc::smem_u32(wbase);
+      const uint32_t mtile_bytes = (uint32_t)p.rp * 128u * 2u;    // one M-tile of 128 rows
+      const uint64_t term_step = (uint64_t)p.Nmma * p.Kp / 8;      // W term block, in 16-byte units
       int64_t it = blockIdx.x;
       for (int k = 0; it < p.niters; it += gridDim.x, ++k) {
         const int slot = k % p.nbuf, tset = k % p.nsets;
@@ -269,12 +322,12 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
         auto a_desc = [&](int a, int t, int pp, int ks) -> uint64_t {
           const int m = a / NPARTS, part = a - m * NPARTS;
           const uint32_t aaddr = xs0 + (uint32_t)((((slot * NPARTS + part) * p.terms + t) * p.P + pp) * xarr) +
-                                 (uint32_t)(8 * 128 * m) * 2u;
+                                 mtile_bytes * (uint32_t)m;
           return (afix | (uint64_t)(aaddr >> 4)) + (uint64_t)(2 * ks);
         };
-        if (p.terms == 3) {
+        if (p.terms == 3 && p.concat) {
           for (int a = 0; a < nacc; a++) {
-            const uint32_t d = dset + (uint32_t)(a * wrows);
+            const uint32_t d = dset + (uint32_t)(a * p.acols);
             for (int pp = 0; pp < p.P; pp++) {
               const uint64_t bd0 = bfix | (uint64_t)((w0 + (uint32_t)pp * wbytes) >> 4);
               for (int ks = 0; ks < nks; ks++) {
@@ -286,13 +339,30 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
               }
             }
           }
+        } else if (p.terms == 3) {
+          // six MMAs of N columns into one accumulator per K-step, products of order <= 2
+          // (signal term tx, tap term tw), smallest first: (1,1) (2,0) (0,2) (1,0) (0,1) (0,0)
+          constexpr uint32_t kTx = 0x001021u, kTw = 0x010201u;
+          for (int a = 0; a < nacc; a++) {
+            const uint32_t d = dset + (uint32_t)(a * p.acols);
+            for (int pp = 0; pp < p.P; pp++) {
+              const uint64_t bd0 = bfix | (uint64_t)((w0 + (uint32_t)pp * wbytes) >> 4);
+              for (int ks = 0; ks < nks; ks++) {
+                for (int pr = 0; pr < 6; pr++) {
+                  const int tx = (int)((kTx >> (4 * pr)) & 15u), tw = (int)((kTw >> (4 * pr)) & 15u);
+                  const uint64_t bd = bd0 + (uint64_t)tw * term_step + (uint64_t)(16 * ks);
+                  tc::mma_f16(d, a_desc(a, tx, pp, ks), bd, idesc1, (pp > 0 || ks > 0 || pr > 0) ? 1u : 0u);
+                }
+              }
+            }
+          }
         } else {
           for (int pp = 0; pp < p.P; pp++) {
             const uint64_t bd0 = bfix | (uint64_t)((w0 + (uint32_t)pp * wbytes) >> 4);
             for (int ks = 0; ks < nks; ks++) {
               const uint64_t bd = bd0 + (uint64_t)(16 * ks);
               for (int a = 0; a < nacc; a++)
-                tc::mma_f16(dset + (uint32_t)(a * wrows), a_desc(a, 0, pp, ks), bd, idesc1,
+                tc::mma_f16(dset + (uint32_t)(a * p.acols), a_desc(a, 0, pp, ks), bd, idesc1,
                             (pp > 0 || ks > 0) ? 1u : 0u);
             }
           }
@@ -325,20 +395,21 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
         const int64_t left64 = p.out_len - n0;
         const int nv = left64 < p.Nt ? (left64 > 0 ? (int)left64 : 0) : p.Nt;  // valid outputs of this row
         XT *dst = orow + n0;
-        const bool vec = XC && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0);
+        const bool vec = (reinterpret_cast<uintptr_t>(dst) & 15) == 0;
+        const bool blocks3 = p.terms == 3 && p.concat;
         for (int col = 0; col < p.Nmma; col += 16) {
           float acc[NPARTS][16];
 #pragma unroll
           for (int part = 0; part < NPARTS; part++) {
-            const uint32_t base = dset + lane_base + (uint32_t)((m * NPARTS + part) * wrows + col);
+            const uint32_t base = dset + lane_base + (uint32_t)((m * NPARTS + part) * p.acols + col);
             uint32_t r0[16], r1[16], r2[16];
             tc::tmem_ld16(base, r0);
-            if (p.terms == 3) {
+            if (blocks3) {
               tc::tmem_ld16(base + (uint32_t)p.Nmma, r1);
               tc::tmem_ld16(base + (uint32_t)(2 * p.Nmma), r2);
             }
             tc::tmem_ld_wait();
-            if (p.terms == 3) {
+            if (blocks3) {
 #pragma unroll
               for (int i = 0; i < 16; i++)
                 acc[part][i] = (__uint_as_float(r0[i]) + __uint_as_float(r1[i])) + __uint_as_float(r2[i]);
@@ -360,9 +431,18 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
               }
             }
           } else {
+            // groups of four outputs as one 16-byte store where the row start is aligned
 #pragma unroll
-            for (int i = 0; i < 16; i++)
-              if (col + i < nv) dst[col + i] = acc[0][i];
+            for (int i = 0; i < 16; i += 4) {
+              if (vec && col + i + 3 < nv) {
+                *reinterpret_cast<float4 *>(dst + col + i) =
+                    make_float4(acc[0][i], acc[0][i + 1], acc[0][i + 2], acc[0][i + 3]);
+              } else {
+#pragma unroll
+                for (int e = 0; e < 4; e++)
+                  if (col + i + e < nv) dst[col + i + e] = acc[0][i + e];
+              }
+            }
           }
         }
       }
@@ -412,8 +492,9 @@ static TcTaps resample_taps(int64_t L, int64_t up) {
   return t;
 }
 
+// rp: Hankel row pitch, 8 or 64 samples.
 static TcPlan plan_tc(int64_t up, int64_t down, const TcTaps &taps, int64_t N_in, int64_t out_len, int64_t batch,
-                      int xc, int precision) {
+                      int xc, int precision, int rp) {
   TcPlan pl{};
   TcParams &p = pl.p;
   p.even = taps.even;
@@ -427,15 +508,21 @@ static TcPlan plan_tc(int64_t up, int64_t down, const TcTaps &taps, int64_t N_in
   p.scale = taps.scale;
   p.fp16 = precision == GBFIR_PREC_FP16;
   p.terms = precision == GBFIR_PREC_BF16X3 ? 3 : 1;
-  p.path = (8 % down == 0) ? 0 : 1;
+  p.rp = rp;
+  p.path = (rp % down == 0) ? 0 : 1;
   p.P = p.path == 0 ? 1 : (int32_t)down;
+  if (up > 256 || (p.path == 0 ? up * (rp / down) : rp * up) > 256) {
+    snprintf(pl.why, sizeof(pl.why), "a row of %lld outputs exceeds the MMA N limit of 256",
+             (long long)(p.path == 0 ? up * (rp / down) : rp * up));
+    return pl;
+  }
   int64_t kmin, kmax;
   if (p.path == 0) {
-    p.Nt = (int32_t)(up * (8 / down));
+    p.Nt = (int32_t)(up * (rp / down));
     kmin = ceil_div(p.c - p.Lo + 1, up);
     kmax = floor_div(p.c + (int64_t)(p.Nt - 1) * down, up);
   } else {
-    p.Nt = (int32_t)(8 * up);
+    p.Nt = (int32_t)(rp * up);
     kmin = INT64_MAX;
     kmax = INT64_MIN;
     for (int64_t b = 0; b < down; b++) {
@@ -455,24 +542,25 @@ static TcPlan plan_tc(int64_t up, int64_t down, const TcTaps &taps, int64_t N_in
     return pl;
   }
   const int nparts = xc ? 2 : 1;
-  if (p.terms == 3 && 3 * p.Nmma > 256) {
-    snprintf(pl.why, sizeof(pl.why), "bf16x3 needs 3*%d MMA columns (> 256)", p.Nmma);
-    return pl;
-  }
+  // bf16x3: concatenate the tap terms along N where 3*N fits one MMA, else six MMAs of N
+  p.concat = (p.terms == 3 && 3 * p.Nmma <= 256) ? 1 : 0;
+  p.acols = p.concat ? 3 * p.Nmma : p.Nmma;
   const int wrows = p.terms * p.Nmma;
+  const size_t xalign = rp == 64 ? 1024 : 128;
   auto smem_for = [&](int MT, int nraw, int nslots) -> size_t {
     const size_t w = (size_t)p.P * wrows * p.Kp * 2;
-    const size_t la = (size_t)8 * 128 * MT + p.Kp;
-    const size_t xa = (la * 2 + 127) / 128 * 128;
+    const size_t la = (size_t)rp * 128 * MT + p.Kp;
+    const size_t xa = (la * 2 + xalign - 1) / xalign * xalign;
     const size_t raw = (size_t)nraw * p.P * la * (xc ? 8 : 4);
-    return (w + 127) / 128 * 128 + (size_t)nslots * nparts * p.terms * p.P * xa + raw;
+    // 1024 bytes of slack to align the dynamic shared memory base
+    return 1024 + (w + 1023) / 1024 * 1024 + (size_t)nslots * nparts * p.terms * p.P * xa + raw;
   };
   // A stage holds MT M-tiles of 128 rows.  Shrink, in this order, until it fits: MT, the raw
   // staging depth, the number of TMEM accumulator sets (512 columns), the operand ring depth.
   const size_t kMaxSmem = 225 * 1024;
-  int MT = 4, nraw = 2, nsets = 2, nslots = 2;
+  int MT = rp == 64 ? 1 : 4, nraw = 2, nsets = 2, nslots = 2;
   auto smem_ok = [&]() { return smem_for(MT, nraw, nslots) <= kMaxSmem; };
-  auto tmem_ok = [&]() { return nsets * MT * nparts * wrows <= 512; };
+  auto tmem_ok = [&]() { return nsets * MT * nparts * p.acols <= 512; };
   while (MT > 1 && !(smem_ok() && tmem_ok())) MT /= 2;
   if (!smem_ok()) nraw = 1;
   if (!tmem_ok()) nsets = 1;
@@ -485,9 +573,9 @@ static TcPlan plan_tc(int64_t up, int64_t down, const TcTaps &taps, int64_t N_in
   p.nbuf = nslots;
   p.nraw = nraw;
   p.nsets = nsets;
-  p.LA = 8 * 128 * MT + p.Kp;
+  p.LA = rp * 128 * MT + p.Kp;
   uint32_t cols = 32;
-  while (cols < (uint32_t)(nsets * MT * nparts * wrows)) cols <<= 1;
+  while (cols < (uint32_t)(nsets * MT * nparts * p.acols)) cols <<= 1;
   p.tmem_cols = (int32_t)cols;
   p.rows = (out_len + p.Nt - 1) / p.Nt;
   p.iters_per_row = (p.rows + 128 * MT - 1) / (128 * MT);
@@ -525,6 +613,31 @@ static int launch_tc(TcPlan &pl, const gbfir_buf &out, const gbfir_buf &in, cons
   return GBFIR_SUCCESS;
 }
 
+// Which tensor-core kernel a pass prefers: 0 = the built-in order, 8 / 64 = the Toeplitz kernel
+// with that row pitch only, 1 = the 64-sample-row kernel with the taps in TMEM (tc_wide.cu)
+// first.  GBFIR_TC_ROWS ("8", "64", "wide") pins one for measurements.
+static int tc_rows_pref() {
+  const char *e = getenv("GBFIR_TC_ROWS");
+  if (e == nullptr) return 0;
+  if (strcmp(e, "8") == 0) return 8;
+  if (strcmp(e, "64") == 0) return 64;
+  if (strcmp(e, "wide") == 0) return 1;
+  return 0;
+}
+
+// The Toeplitz plan to run, or the one the preference pins: 64-sample rows where they keep
+// the whole pipeline (two operand slots, two accumulator sets), else 8-sample rows, else
+// 64-sample rows with whatever pipeline fits.
+static TcPlan plan_tc_rows(int64_t up, int64_t down, const TcTaps &taps, int64_t N_in, int64_t out_len,
+                           int64_t batch, int xc, int precision, int pref) {
+  if (pref == 8 || pref == 64) return plan_tc(up, down, taps, N_in, out_len, batch, xc, precision, pref);
+  TcPlan wide = plan_tc(up, down, taps, N_in, out_len, batch, xc, precision, 64);
+  if (wide.ok && wide.p.nbuf == 2 && wide.p.nsets == 2) return wide;
+  TcPlan narrow = plan_tc(up, down, taps, N_in, out_len, batch, xc, precision, 8);
+  if (narrow.ok || !wide.ok) return narrow;
+  return wide;
+}
+
 int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t up, int64_t down,
                      int precision, cudaStream_t s) {
   if (dtype_double(in.dtype) || dtype_complex(h.dtype))
@@ -532,14 +645,15 @@ int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf 
                                         "float32 taps");
   const bool xc = dtype_complex(in.dtype);
   const TcTaps taps = resample_taps(h.len, up);
-  // 64-sample rows where they fill at least half of the 128 MMA lanes with output phases
-  // (measured faster there); the 8-sample-row kernel otherwise
-  if (64 % down == 0 && 64 * up / down >= 64) {
+  const int pref = tc_rows_pref();
+  // 64-sample rows with the taps in TMEM where they fill at least half of the 128 MMA lanes
+  // with output phases (measured faster there); the Toeplitz kernel otherwise
+  if ((pref == 0 || pref == 1) && 64 % down == 0 && 64 * up / down >= 64) {
     TwPlan wp = plan_tc_wide(up, down, taps.Lo, taps.c, taps.even, taps.rev, taps.scale, in.len, out.len, out.batch,
                              xc, precision);
     if (wp.ok) return launch_tc_wide(wp, out, in, h, xc, "resample_poly (tensor cores)", s);
   }
-  TcPlan pl = plan_tc(up, down, taps, in.len, out.len, out.batch, xc, precision);
+  TcPlan pl = plan_tc_rows(up, down, taps, in.len, out.len, out.batch, xc, precision, pref);
   if (!pl.ok)
     GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly: tensor-core form unavailable for up=%lld down=%lld: %s",
                (long long)up, (long long)down, pl.why);
@@ -550,7 +664,8 @@ int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf 
 // extension, gain 1 and the mode's start offset as the centre (conv.h:155-168 semantics:
 // out[o] = full[o + start], start = 0 FULL, (L-1)/2 or L/2-1 SAME, L-1 VALID); corr reads
 // the (real) taps reversed.  Covers a real float32 filter row shared by every signal row,
-// with the signal at least as long as the filter (no operand swap).
+// with the signal at least as long as the filter (no operand swap).  Rows of 64 outputs
+// (64-sample Hankel rows) where the tile fits, 8 otherwise.
 int conv1d_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int mode, int is_corr, int precision,
               cudaStream_t s) {
   if (dtype_double(in.dtype) || dtype_complex(h.dtype))
@@ -569,7 +684,7 @@ int conv1d_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int
   t.scale = 1.0;
   t.c = mode == GBFIR_MODE_SAME ? ((L & 1) ? (L - 1) / 2 : L / 2 - 1) : mode == GBFIR_MODE_VALID ? L - 1 : 0;
   const bool xc = dtype_complex(in.dtype);
-  TcPlan pl = plan_tc(1, 1, t, in.len, out.len, out.batch, xc, precision);
+  TcPlan pl = plan_tc_rows(1, 1, t, in.len, out.len, out.batch, xc, precision, tc_rows_pref());
   if (!pl.ok) GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "conv1d: tensor-core form unavailable: %s", pl.why);
   return launch_tc(pl, out, in, h, xc, "conv1d (tensor cores)", s);
 }
@@ -582,10 +697,13 @@ int resample_poly_bwd_dx_tc(const gbfir_buf &dx, const gbfir_buf &gy, const gbfi
                             int precision, cudaStream_t s) {
   TcTaps taps = resample_taps(h.len, up);
   taps.rev = 1;
-  TwPlan wp = plan_tc_wide(down, up, taps.Lo, taps.c, taps.even, taps.rev, taps.scale, gy.len, dx.len, dx.batch, 0,
-                           precision);
-  if (wp.ok) return launch_tc_wide(wp, dx, gy, h, false, "resample_poly_bwd dx (tensor cores)", s);
-  TcPlan pl = plan_tc(down, up, taps, gy.len, dx.len, dx.batch, 0, precision);
+  const int pref = tc_rows_pref();
+  if (pref == 0 || pref == 1) {
+    TwPlan wp = plan_tc_wide(down, up, taps.Lo, taps.c, taps.even, taps.rev, taps.scale, gy.len, dx.len, dx.batch, 0,
+                             precision);
+    if (wp.ok) return launch_tc_wide(wp, dx, gy, h, false, "resample_poly_bwd dx (tensor cores)", s);
+  }
+  TcPlan pl = plan_tc_rows(down, up, taps, gy.len, dx.len, dx.batch, 0, precision, pref);
   if (!pl.ok)
     GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly_bwd: tensor-core dx unavailable for up=%lld down=%lld: %s",
                (long long)up, (long long)down, pl.why);

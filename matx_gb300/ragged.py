@@ -17,7 +17,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from . import resample_out_len, _stream
+from . import resample_out_len, _prec, _stream
 
 
 class RaggedPlan:
@@ -64,10 +64,12 @@ class RaggedPlan:
         self.workspace = torch.zeros(ws, dtype=torch.uint8, device=dev)
         self.num_tiles = int(cnt)
 
-    def run(self):
+    def run(self, precision="fp32"):
+        """One persistent launch over every signal; ``precision`` selects the arithmetic of
+        the tap contraction as for resample_poly."""
         lib = _lib.load()
         _lib.check(lib.gbfir_ragged_resample(
             ctypes.c_void_p(self.d_descs.data_ptr()), self.count, ctypes.c_void_p(self.d_tiles.data_ptr()),
-            ctypes.byref(self.info), 0, ctypes.c_void_p(self.workspace.data_ptr()), self.workspace.numel(),
-            _stream()))
+            ctypes.byref(self.info), _prec(precision), ctypes.c_void_p(self.workspace.data_ptr()),
+            self.workspace.numel(), _stream()))
         return self.outputs

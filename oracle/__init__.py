@@ -29,11 +29,31 @@ _int = ctypes.c_int
 _p = ctypes.c_void_p
 
 
+def matx_root():
+    """Root of the MatX source tree the reference build reads: ``$MATX_REF`` if set, else
+    the default named by this directory's Makefile recipe (``MATX ?= ...``); None where no
+    MatX headers are present (the GPU machine, any machine without the tree)."""
+    root = os.environ.get("MATX_REF")
+    if not root:
+        try:
+            for line in open(os.path.join(_HERE, "Makefile")):
+                if line.replace(" ", "").startswith("MATX?="):
+                    root = line.split("=", 1)[1].strip()
+                    break
+        except OSError:
+            root = None
+    if root and os.path.isdir(os.path.join(root, "include", "matx")):
+        return root
+    return None
+
+
 def build(ref: bool = False) -> None:
-    """Compile the C oracle (and MatX's host reference when ``ref``)."""
+    """Compile the C oracle (and MatX's host reference when ``ref`` and the MatX tree is
+    present)."""
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
-    if ref:
-        subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True)
+    root = matx_root() if ref else None
+    if root:
+        subprocess.run(["make", "-s", "-C", _HERE, "ref", f"MATX={root}"], check=True)
 
 
 def lib():

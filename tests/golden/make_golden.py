@@ -1,8 +1,8 @@
 #!/usr/bin/env python3
 """Regenerate the golden fixtures in tests/golden/ from the MatX reference.
 
-Run once in a container where the MatX source tree is mounted (default
-/root/reference, override with MATX_REF=...):
+Run once in a container where the MatX source tree is mounted (the tree the oracle's
+Makefile recipe names, or MATX_REF=...):
 
     python tests/golden/make_golden.py
 
@@ -34,9 +34,14 @@ import sys
 
 import numpy as np
 
-REF = os.environ.get("MATX_REF", "/root/reference")
-GEN = os.path.join(REF, "test", "test_vectors", "generators")
 HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+import oracle  # noqa: E402
+
+REF = oracle.matx_root()
+if REF is None:
+    raise SystemExit("make_golden.py: no MatX source tree found (set MATX_REF)")
+GEN = os.path.join(REF, "test", "test_vectors", "generators")
 
 
 def _gen():

@@ -1,22 +1,22 @@
-// tc_gemm.cu — self-test GEMM of the tcgen05 building blocks (diagnostic entry point,
-// no MatX counterpart).
+// tc_gemm_selftest.cu — test-only self-test GEMM of the library's tcgen05 building blocks
+// (matx_gb300/csrc/tc.cuh).  Built by tests/tc_selftest/build.py into a library of its own;
+// nothing in the product links or loads it.
 //
 //   C[M][N] = A[M][K] * B[N][K]^T   (FP32 in and out)
 // with the operands rounded to bf16 (terms = 1) or split into three bf16 terms
 // (terms = 3; the six products of order <= 2, smallest first, accumulated in FP32 TMEM).
 // One CTA of 128 threads per 128-row block: pack operands into the K-major core-matrix
 // layout, one thread issues the MMAs and a commit to an mbarrier, all four warps wait
-// (bounded) and read their 32 TMEM lanes back.  `swap_offsets` exchanges the roles of the
-// two descriptor byte offsets (a layout diagnostic; both settings stay inside the operand
-// buffers).  A timed-out wait sets *status = 1.
-#include "common.cuh"
+// (bounded) and read their 32 TMEM lanes back.  A timed-out wait sets *status = 1.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
 #include "tc.cuh"
 
 namespace gbfir {
 
 __global__ void __launch_bounds__(128) tc_gemm_selftest_kernel(const float *A, const float *B, float *C, int M,
-                                                               int N, int K, int terms, int swap_offsets,
-                                                               int *status) {
+                                                               int N, int K, int terms, int *status) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_slot;
@@ -68,8 +68,7 @@ __global__ void __launch_bounds__(128) tc_gemm_selftest_kernel(const float *A, c
 
   if (tid == 0) {
     const uint32_t kstride = 128, rstride = (uint32_t)(K / 8) * 128;  // layout of kmajor_offset
-    const uint32_t lbo = swap_offsets ? rstride : kstride;
-    const uint32_t sbo = swap_offsets ? kstride : rstride;
+    const uint32_t lbo = kstride, sbo = rstride;
     const uint32_t idesc = tc::idesc_f16(128, (uint32_t)N, 1);
     const int pa3[6] = {2, 1, 0, 1, 0, 0}, pb3[6] = {0, 1, 2, 0, 1, 0};
     const int npairs = terms == 3 ? 6 : 1;
@@ -112,20 +111,19 @@ __global__ void __launch_bounds__(128) tc_gemm_selftest_kernel(const float *A, c
 
 using namespace gbfir;
 
-extern "C" {
-
-int gbfir_tc_gemm_selftest(const float *A, const float *B, float *C, int32_t M, int32_t N, int32_t K, int32_t terms,
-                           int32_t swap_offsets, int32_t *status, gbfir_stream_t stream) {
-  if (!A || !B || !C || !status) GBFIR_FAIL(GBFIR_ERR_NULL_POINTER, "tc_gemm_selftest: null pointer");
+// 0 on success; 1 = null pointer, 2 = unsupported size, 3 = CUDA error.
+extern "C" __attribute__((visibility("default"))) int tc_gemm_selftest(const float *A, const float *B, float *C,
+                                                                        int32_t M, int32_t N, int32_t K,
+                                                                        int32_t terms, int32_t *status,
+                                                                        void *stream) {
+  if (!A || !B || !C || !status) return 1;
   if (M <= 0 || M % 128 || N < 16 || N > 256 || N % 16 || K < 16 || K > 64 || K % 16 || (terms != 1 && terms != 3))
-    GBFIR_FAIL(GBFIR_ERR_INVALID_SIZE, "tc_gemm_selftest: need M%%128==0, N in [16,256] step 16, K in {16,32,48,64}, "
-                                       "terms 1 or 3");
+    return 2;
   const size_t smem = 3 * (128u * K * 2u) + 3 * ((size_t)N * K * 2u);
-  int rc = ensure_smem((const void *)tc_gemm_selftest_kernel, smem, "tc_gemm_selftest");
-  if (rc) return rc;
+  if (cudaFuncSetAttribute(tc_gemm_selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return 3;
   tc_gemm_selftest_kernel<<<M / 128, 128, smem, reinterpret_cast<cudaStream_t>(stream)>>>(A, B, C, M, N, K, terms,
-                                                                                           swap_offsets, status);
-  return check_launch("tc_gemm_selftest");
+                                                                                           status);
+  return cudaGetLastError() == cudaSuccess ? 0 : 3;
 }
-
-}  // extern "C"

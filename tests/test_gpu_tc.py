@@ -1,4 +1,5 @@
-"""tcgen05 building blocks: the self-test GEMM against an FP64 torch reference.
+"""tcgen05 building blocks (matx_gb300/csrc/tc.cuh): a test-only self-test GEMM
+(tests/tc_selftest/) against an FP64 torch reference.
 
 bf16 (one term) must match the FP64 product of the bf16-rounded operands closely
 and the FP32 product to bf16 accuracy; bf16x3 (three terms, six products) must
@@ -16,22 +17,23 @@ def lib():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
-    from matx_gb300 import build, _lib
-    build.build()
-    return _lib.load()
+    from tc_selftest.build import build
+    so = ctypes.CDLL(build())
+    so.tc_gemm_selftest.restype = ctypes.c_int
+    so.tc_gemm_selftest.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int32] * 4 + [ctypes.c_void_p] * 2
+    return so
 
 
-def run(lib, A, B, terms, swap=0):
+def run(lib, A, B, terms):
     import torch
     M, K = A.shape
     N = B.shape[0]
     C = torch.zeros(M, N, dtype=torch.float32, device="cuda")
     st = torch.zeros(1, dtype=torch.int32, device="cuda")
     s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    rc = lib.gbfir_tc_gemm_selftest(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr()),
-                                    ctypes.c_void_p(C.data_ptr()), M, N, K, terms, swap,
-                                    ctypes.c_void_p(st.data_ptr()), s)
-    assert rc == 0, lib.gbfir_last_error()
+    rc = lib.tc_gemm_selftest(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr()),
+                              ctypes.c_void_p(C.data_ptr()), M, N, K, terms, ctypes.c_void_p(st.data_ptr()), s)
+    assert rc == 0, rc
     torch.cuda.synchronize()
     assert int(st.item()) == 0, "bounded wait gave up"
     return C

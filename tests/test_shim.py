@@ -8,12 +8,13 @@ import subprocess
 
 import pytest
 
+import oracle
 from conftest import ROOT
 
-MATX = os.environ.get("MATX_REF", "/root/reference")
+MATX = oracle.matx_root()
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(MATX, "include", "matx")), reason="MatX headers not present")
+@pytest.mark.skipif(MATX is None, reason="MatX headers not present")
 def test_shim_routes_matx_operators(tmp_path):
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     obj = tmp_path / "shim.o"
