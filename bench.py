@@ -799,6 +799,10 @@ def measure_ragged(args, rank, world, dev, steps=None):
         sigs.append((x, h, up, down))
         macs += mac_count(int(lens[i]), int(taps[i]), up, down)
         outs_total += out_len(int(lens[i]), up, down)
+    tiles = {}
+    if not args.no_tune:
+        from matx_gb300 import autotune
+        tiles = autotune.tune_ragged(sigs)
     plan = RaggedPlan(sigs)
     for _ in range(args.warmup):
         plan.run()
@@ -855,7 +859,7 @@ def measure_ragged(args, rank, world, dev, steps=None):
         "speedup_vs_per_signal": ms_single / ms_graph,
         "output_samples_per_s": outs_total / (ms_graph * 1e-3),
         "hbm_gbs": nbytes / (ms_graph * 1e-3) / 1e9, "hbm_frac": nbytes / (ms_graph * 1e-3) / 1e9 / _peak(),
-        "gpu_launches": launches, "forms": forms,
+        "gpu_launches": launches, "forms": forms, "tiles": tiles,
     }
 
 
@@ -883,7 +887,7 @@ def measure_configs(args, rank, world, dev):
             ("C3_channelize", measure_channelize, ("forms", "config")),
             ("C4_fwdbwd", measure_fwdbwd, ("ms_per_step", "value", "unit", "per_ratio", "config")),
             ("C5_ragged", measure_ragged, ("ms_per_step", "value", "unit", "hbm_frac", "per_signal_launches_ms",
-                                           "speedup_vs_per_signal", "forms", "config")))
+                                           "speedup_vs_per_signal", "forms", "tiles", "config")))
     for name, fn, keys in plan:
         try:
             t0 = time.perf_counter()

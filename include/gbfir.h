@@ -301,23 +301,37 @@ GBFIR_API size_t gbfir_ragged_workspace_size(int64_t count, int64_t num_tiles);
 
 /* Launch geometry produced by the planner (host memory). */
 typedef struct gbfir_ragged_plan_info {
-  int64_t num_tiles;     /* entries in the tile table                         */
-  int64_t shared_bytes;  /* dynamic shared memory per CTA                     */
-  int64_t table_bytes;   /* of which the tap table (the window follows it)    */
+  int64_t num_tiles;     /* entries (work items) in the tile table             */
+  int64_t shared_bytes;  /* dynamic shared memory per CTA                      */
+  int64_t table_bytes;   /* of which the tap table (the window buffers follow) */
+  int64_t window_elems;  /* complex samples per window buffer                  */
+  int64_t buffers;       /* window buffers per CTA (2: the next tile prefetched) */
 } gbfir_ragged_plan_info;
 
+/* Tile shape the ragged planner uses for signals of one reduced (up, down) whose tap
+ * count falls in h_len's bucket (the smallest power of two >= h_len): rows_per_thread
+ * 1 or 2, col_warps 1, 2, 4 or 8, group 1..64 (outputs per row = up * group).  Filled
+ * by the autotuner (no MatX counterpart); signals without an entry take the built-in
+ * heuristic, and rows_per_thread = col_warps = group = 0 removes the entry.  Applies to
+ * plans made after the call. */
+GBFIR_API int gbfir_ragged_tile_register(int64_t up, int64_t down, int64_t h_len,
+                                         int32_t rows_per_thread, int32_t col_warps,
+                                         int32_t group);
+GBFIR_API int gbfir_ragged_tile_clear(void);
+
 /* Host-side planner.  Validates the descriptors (host copies), cuts every signal
- * into row tiles of its own geometry and writes `tile_table` (host memory, two
- * int64 per tile: signal index, first tile row), most expensive tiles first.
- * Returns the number of tiles (with tile_table == NULL it only counts) or a
+ * into row tiles of its own geometry and groups consecutive tiles of one signal into
+ * work items of similar cost; writes `tile_table` (host memory, four int64 per item:
+ * signal index, first row, number of rows, packed tile shape), most expensive items
+ * first.  Returns the number of items (with tile_table == NULL it only counts) or a
  * negative gbfir_status, and fills *info.  Each signal's up/down are reduced by
  * their gcd. */
 GBFIR_API int64_t gbfir_ragged_plan(const gbfir_ragged_desc *host_descs, int64_t count,
                           int64_t *tile_table, gbfir_ragged_plan_info *info);
 
-/* One persistent launch over all tiles.  device_descs / device_tile_table are
+/* One persistent launch over all work items.  device_descs / device_tile_table are
  * device copies of the descriptors and of the planner's table; info is the
- * planner's host struct.  CTAs take tiles from an atomic counter in `workspace`
+ * planner's host struct.  CTAs take items from an atomic counter in `workspace`
  * (zeroed on the stream first), so the launch balances arbitrary length skew and
  * contains no host synchronisation: it can be captured in a CUDA graph. */
 GBFIR_API int gbfir_ragged_resample(const gbfir_ragged_desc *device_descs, int64_t count,

@@ -18,6 +18,12 @@ The winner is registered in the library (gbfir_resample_tile_register), so every
 later call with the same reduced (up, down) and filter length uses it, and it is
 stored in a JSON cache keyed by device name, dtype, rates, filter length and the
 row-length bucket, so a later process can register it without re-timing.
+
+``tune_ragged`` does the same for the ragged launch: per reduced (up, down) and
+tap-length bucket (the smallest power of two >= the tap count) it times the ragged
+launch of that group's signals under every candidate shape (rows per thread 1 or 2,
+column warps 1/2/4/8, row groups of 1, 2 or 4 times the smallest) and registers the
+winner with gbfir_ragged_tile_register, which later ragged plans read.
 """
 from __future__ import annotations
 
@@ -149,3 +155,61 @@ def tune_resample(x: torch.Tensor, h: torch.Tensor, up: int, down: int, *, reps:
         cache[key] = {"best": list(best), "best_ms": best_ms, "default_ms": default_ms}
         _save_cache(cache)
     return TuneResult(key, best, best_ms, default_ms, table)
+
+
+def _bucket(n: int) -> int:
+    b = 1
+    while b < n:
+        b <<= 1
+    return b
+
+
+def ragged_candidates(up: int, down: int):
+    g = math.gcd(up, down)
+    u = up // g
+    g0 = 4 // math.gcd(u, 4)
+    for rq in (1, 2):
+        for wc in (1, 2, 4, 8):
+            for m in (1, 2, 4):
+                if g0 * m <= 64:
+                    yield (rq, wc, g0 * m)
+
+
+def tune_ragged(signals, *, reps: int = 3, max_per_group: int = 64) -> dict:
+    """Tune the ragged launch's tile shape per (reduced up/down, tap-length bucket) group of
+    ``signals`` ((x, h, up, down) tuples as for RaggedPlan): each group's longest signals are
+    planned and launched alone under every candidate shape; the fastest shape (or the
+    built-in heuristic, if nothing beats it) is registered for later plans."""
+    from .ragged import RaggedPlan
+    lib = _lib.load()
+    groups = {}
+    for x, h, up, down in signals:
+        g = math.gcd(int(up), int(down))
+        u, d = int(up) // g, int(down) // g
+        if u == d:
+            continue
+        groups.setdefault((u, d, _bucket(h.shape[-1])), []).append((x, h, up, down))
+    results = {}
+    for (u, d, b), sigs in sorted(groups.items()):
+        sigs = sorted(sigs, key=lambda s: -s[0].shape[-1])[:max_per_group]
+        _lib.check(lib.gbfir_ragged_tile_register(u, d, b, 0, 0, 0))
+        base = RaggedPlan(sigs)
+        outs = base.outputs
+        base_ms = _time(base.run, reps)
+        best, best_ms = None, base_ms
+        for cand in ragged_candidates(u, d):
+            _lib.check(lib.gbfir_ragged_tile_register(u, d, b, *cand))
+            try:
+                plan = RaggedPlan(sigs, outputs=outs)
+                ms = _time(plan.run, reps)
+            except _lib.GbfirError:
+                continue
+            if ms < best_ms:
+                best, best_ms = cand, ms
+        if best is None:
+            _lib.check(lib.gbfir_ragged_tile_register(u, d, b, 0, 0, 0))
+        else:
+            _lib.check(lib.gbfir_ragged_tile_register(u, d, b, *best))
+        results[f"{u}/{d}|L<={b}"] = {"tile": list(best) if best else "heuristic", "ms": best_ms,
+                                      "heuristic_ms": base_ms, "signals": len(sigs)}
+    return results

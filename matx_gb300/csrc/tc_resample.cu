@@ -77,14 +77,19 @@ struct TcParams {
 // cleared by gbfir_tc_status().
 __device__ int32_t g_tc_status;
 
-// Tap he(tp) of the logical filter (reversed when rev, 0 outside), read from hs: the filter's
-// taps staged in shared memory, or the global row.
-__device__ __forceinline__ float tap_value(const TcParams &p, const float *hs, int64_t tp) {
-  if (tp < 0 || tp >= p.Lo) return 0.f;
-  const int64_t te = p.rev ? p.Lo - 1 - tp : tp;
-  if (p.even && te == 0) return 0.f;
-  return hs[te - p.even];
+// Two floats as an fp16 pair (round to nearest), low half first.
+__device__ __forceinline__ uint32_t tw_pack_h2(float a, float b) {
+  const __half2 h = __floats2half2_rn(a, b);
+  return *reinterpret_cast<const uint32_t *>(&h);
 }
+
+// Timing hooks of the pipeline roles (role, stage, event); they compile to nothing unless a
+// tracing build defines them.
+#ifndef GBFIR_TC_TRACE
+#define GBFIR_TC_TRACE(role, stage, event) \
+  do {                                     \
+  } while (0)
+#endif
 
 // Warp roles (12 warps): warp 0 lane 0 issues the MMAs; warps 1-7 stage raw input with
 // cp.async and convert it into the operand ring; warps 8-11 (one per TMEM lane quarter)
@@ -102,15 +107,127 @@ __device__ __forceinline__ void named_sync(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
+// Epilogue of one 16-lane half of a warp's TMEM lane quarter (tb: its TMEM address, columns of
+// one M-tile).  16x256b loads: for TMEM lanes l0 + L/4 and l0 + L/4 + 8, lane L holds columns
+// c and c + 1 of each 8-column group, c = 2 * (L % 4); so four lanes hold 8 consecutive outputs
+// of one row and each store instruction writes 32 (real) or 64 (complex) contiguous bytes of
+// 8 rows: whole sectors.  GCH 32-column chunks (16x256b.x4 loads of every part and of the BLK
+// concatenated term blocks) go per TMEM wait, up to 64 registers; 8-column groups for a
+// remainder.  qa: the signal row of lane L's first TMEM lane.
+template <bool XC, int BLK>
+__device__ __forceinline__ void tcr_drain_half(const TcParams &p, uint32_t tb,
+                                               typename val_of<float, XC>::type *orow, int64_t qa, int lane) {
+  using XT = typename val_of<float, XC>::type;
+  constexpr int NPARTS = XC ? 2 : 1;
+  constexpr int GCH = (64 / (16 * NPARTS * BLK)) > 0 ? 64 / (16 * NPARTS * BLK) : 1;
+  auto valid = [&](int64_t n0) -> int {
+    const int64_t left = p.out_len - n0;
+    return left < p.Nt ? (left > 0 ? (int)left : 0) : p.Nt;
+  };
+  const int64_t na = qa * p.Nt, nb = (qa + 8) * p.Nt;
+  const int nva = valid(na), nvb = valid(nb);
+  XT *da = orow + na, *db = orow + nb;
+  // c is even, so a pair of outputs is one vector store wherever the row start is aligned to
+  // the pair (8 bytes real, 16 bytes complex)
+  constexpr uintptr_t kPairAlign = XC ? 15 : 7;
+  const bool ala = (reinterpret_cast<uintptr_t>(da) & kPairAlign) == 0;
+  const bool alb = (reinterpret_cast<uintptr_t>(db) & kPairAlign) == 0;
+  auto put = [&](XT *d, int nv, bool al, int c, const float (&w)[NPARTS][2]) {
+    if (al && c + 1 < nv) {
+      if constexpr (XC) *reinterpret_cast<float4 *>(d + c) = make_float4(w[0][0], w[1][0], w[0][1], w[1][1]);
+      else *reinterpret_cast<float2 *>(d + c) = make_float2(w[0][0], w[0][1]);
+    } else {
+      if constexpr (XC) {
+        if (c < nv) d[c] = make_float2(w[0][0], w[1][0]);
+        if (c + 1 < nv) d[c + 1] = make_float2(w[0][1], w[1][1]);
+      } else {
+        if (c < nv) d[c] = w[0][0];
+        if (c + 1 < nv) d[c + 1] = w[0][1];
+      }
+    }
+  };
+  const int nfull = p.Nmma / 32;
+  for (int c0 = 0; c0 < nfull; c0 += GCH) {
+    uint32_t rb[GCH][NPARTS][BLK][16];
+#pragma unroll
+    for (int g = 0; g < GCH; g++) {
+      if (c0 + g >= nfull) break;
+#pragma unroll
+      for (int part = 0; part < NPARTS; part++)
+#pragma unroll
+        for (int bk = 0; bk < BLK; bk++)
+          tc::tmem_ld_16x256b_x4(tb + (uint32_t)(part * p.acols + bk * p.Nmma + 32 * (c0 + g)), rb[g][part][bk]);
+    }
+    tc::tmem_ld_wait();
+#pragma unroll
+    for (int g = 0; g < GCH; g++) {
+      if (c0 + g >= nfull) break;
+#pragma unroll
+      for (int grp = 0; grp < 4; grp++) {
+        float va[NPARTS][2], vb[NPARTS][2];
+#pragma unroll
+        for (int part = 0; part < NPARTS; part++) {
+          float v[4];
+#pragma unroll
+          for (int i = 0; i < 4; i++) {
+            const int r = 4 * grp + i;
+            if constexpr (BLK == 3)
+              v[i] = (__uint_as_float(rb[g][part][0][r]) + __uint_as_float(rb[g][part][1][r])) +
+                     __uint_as_float(rb[g][part][2][r]);
+            else
+              v[i] = __uint_as_float(rb[g][part][0][r]);
+          }
+          va[part][0] = v[0];
+          va[part][1] = v[1];
+          vb[part][0] = v[2];
+          vb[part][1] = v[3];
+        }
+        const int c = 32 * (c0 + g) + 8 * grp + 2 * (lane & 3);
+        put(da, nva, ala, c, va);
+        put(db, nvb, alb, c, vb);
+      }
+    }
+  }
+  for (int cg = 32 * nfull; cg < p.Nmma; cg += 8) {
+    float va[NPARTS][2], vb[NPARTS][2];
+    uint32_t r[NPARTS][BLK][4];
+#pragma unroll
+    for (int part = 0; part < NPARTS; part++)
+#pragma unroll
+      for (int bk = 0; bk < BLK; bk++)
+        tc::tmem_ld_16x256b(tb + (uint32_t)(part * p.acols + bk * p.Nmma + cg), r[part][bk]);
+    tc::tmem_ld_wait();
+#pragma unroll
+    for (int part = 0; part < NPARTS; part++) {
+      float v[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        if constexpr (BLK == 3)
+          v[i] = (__uint_as_float(r[part][0][i]) + __uint_as_float(r[part][1][i])) + __uint_as_float(r[part][2][i]);
+        else
+          v[i] = __uint_as_float(r[part][0][i]);
+      }
+      va[part][0] = v[0];
+      va[part][1] = v[1];
+      vb[part][0] = v[2];
+      vb[part][1] = v[3];
+    }
+    const int c = cg + 2 * (lane & 3);
+    put(da, nva, ala, c, va);
+    put(db, nvb, alb, c, vb);
+  }
+}
+
 template <bool XC>
 __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcParams p) {
   using XT = typename val_of<float, XC>::type;
   constexpr int NPARTS = XC ? 2 : 1;  // real / imaginary operand rows
   extern __shared__ __align__(1024) unsigned char smem_dyn[];
-  __shared__ uint64_t op_full[2], op_empty[2], tm_full[2], tm_empty[2];
+  __shared__ uint64_t op_full[2], op_empty[2], tm_full[2], tm_empty[2], raw_full[2];
   __shared__ uint32_t tmem_slot;
   __shared__ int s_fail, s_pok, s_eok;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) GBFIR_TC_TRACE(3, 0, 1);
 
   // shared layout (1024-aligned; the 128-byte swizzle pattern follows address bits 4-9):
   // W_cat [P][terms*Nmma rows][Kp] ; operand ring [nbuf][NPARTS][terms][P][LA] ; raw ring
@@ -137,52 +254,107 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
       tc::mbar_init(&op_empty[i], 1);
       tc::mbar_init(&tm_full[i], 1);
       tc::mbar_init(&tm_empty[i], 1);
+      tc::mbar_init(&raw_full[i], 1);
     }
     s_fail = 0;
     tc::mbar_fence_init();
   }
-  // The filter's taps, staged once into the raw ring (not in use yet) so that the W build
-  // reads shared memory instead of making one dependent global load per element.
+  // The filter's taps, scaled and split into the operand terms once (hterm[t][e] = term t
+  // of scale * h[e], 16-bit), staged in the raw ring (not in use yet), so that the W build
+  // gathers 8 taps per 16-byte store instead of splitting every element.
   const int64_t Lh = p.Lo - p.even;
-  const bool h_staged = (size_t)Lh * sizeof(float) <= (size_t)p.nraw * raw_elems * sizeof(XT);
-  float *hs_stage = reinterpret_cast<float *>(raw0);
-  if (h_staged)
-    for (int64_t e = tid; e < Lh; e += kWsThreads) hs_stage[e] = p.h[e];
-  __syncthreads();
-  const float *hsrc = h_staged ? hs_stage : p.h;
-  // ---- W_cat[pp][t*Nmma + j][k] = term t of up*he[tap(j, k)] (K-major core layout) ----
-  const int wel = wrows * p.Kp;
-  for (int e = tid; e < p.P * wel; e += kWsThreads) {
-    const int pp = e / wel, r = e - pp * wel;
-    const int row = r / p.Kp, k = r - row * p.Kp;
-    const int t = row / p.Nmma, j = row - t * p.Nmma;
-    float v = 0.f;
-    if (j < p.Nt) {
-      const int64_t kk = k + p.k0;
-      const int64_t tp = p.path == 0 ? p.c + (int64_t)j * p.down - kk * p.up
-                                     : p.c + p.down * (int64_t)j - p.up * (pp + p.down * kk);
-      v = tap_value(p, hsrc, tp) * (float)p.scale;
-    }
-    const uint32_t off = tc::kmajor_offset(row, k, p.Kp);
+  const bool h_staged = (size_t)Lh * 2 * p.terms <= (size_t)p.nraw * raw_elems * sizeof(XT);
+  uint16_t *hterm = reinterpret_cast<uint16_t *>(raw0);
+  auto split_terms = [&](float v, uint16_t (&o)[3]) {
     if (p.fp16) {
-      *reinterpret_cast<__half *>(warr(pp) + off) = __float2half_rn(v);
+      o[0] = __half_as_ushort(__float2half_rn(v));
+      o[1] = o[2] = 0;
     } else {
       __nv_bfloat16 t0, t1, t2;
       tc::split3_bf16(v, t0, t1, t2);
-      *reinterpret_cast<__nv_bfloat16 *>(warr(pp) + off) = t == 0 ? t0 : (t == 1 ? t1 : t2);
+      o[0] = __bfloat16_as_ushort(t0);
+      o[1] = __bfloat16_as_ushort(t1);
+      o[2] = __bfloat16_as_ushort(t2);
     }
+  };
+  if (h_staged) {
+    for (int64_t e = tid; e < Lh; e += kWsThreads) {
+      uint16_t o[3];
+      split_terms(p.h[e] * (float)p.scale, o);
+      for (int t = 0; t < p.terms; t++) hterm[t * Lh + e] = o[t];
+    }
+  }
+  __syncthreads();
+  // term t of W at tap position tp (he read reversed when rev, 0 outside the filter)
+  auto w_term = [&](int t, int64_t tp) -> uint32_t {
+    if (tp < 0 || tp >= p.Lo) return 0u;
+    const int64_t te = p.rev ? p.Lo - 1 - tp : tp;
+    if (p.even && te == 0) return 0u;
+    const int64_t e = te - p.even;
+    if (h_staged) return hterm[t * Lh + e];
+    uint16_t o[3];
+    split_terms(p.h[e] * (float)p.scale, o);
+    return o[t];
+  };
+  // ---- W_cat[pp][t*Nmma + j][k] = term t of up*he[tap(j, k)] (K-major core layout) ----
+  // Every tap position a W element reads lies in [tp_lo, tp_hi]; zline[t][tp - tp_lo] holds
+  // its term t (0 outside the filter), so each element is one branch-free shared load.  An
+  // item is one 8-wide K chunk of one row (one 16-byte store); along a chunk the tap position
+  // steps by -up (path A) or -up*down (path B).
+  if (tid == 0) GBFIR_TC_TRACE(3, 1, 0);
+  const int kch = p.Kp / 8;
+  const int64_t dtp = p.path == 0 ? -p.up : -p.up * p.down;
+  const int64_t kk_hi = p.k0 + p.Kp - 1;
+  const int64_t tp_lo = p.path == 0 ? p.c - kk_hi * p.up : p.c - p.up * ((p.P - 1) + p.down * kk_hi);
+  const int64_t tp_hi = p.path == 0 ? p.c + (int64_t)(p.Nt - 1) * p.down - p.k0 * p.up
+                                    : p.c + p.down * (int64_t)(p.Nt - 1) - p.up * p.down * p.k0;
+  const int64_t zlen = tp_hi - tp_lo + 1;
+  uint16_t *zline = hterm + (h_staged ? (size_t)p.terms * Lh : 0);
+  const bool z_staged = h_staged && zlen > 0 &&
+                        ((size_t)p.terms * Lh + (size_t)p.terms * zlen) * 2 <= (size_t)p.nraw * raw_elems * sizeof(XT);
+  if (z_staged) {
+    for (int64_t i = tid; i < p.terms * zlen; i += kWsThreads) {
+      const int t = (int)(i / zlen);
+      zline[i] = (uint16_t)w_term(t, tp_lo + (i - (int64_t)t * zlen));
+    }
+  }
+  __syncthreads();
+  for (int it = tid; it < p.P * wrows * kch; it += kWsThreads) {
+    const int rr = it / kch, kc = it - rr * kch;
+    const int pp = rr / wrows, row = rr - pp * wrows;
+    const int t = row / p.Nmma, j = row - t * p.Nmma;
+    uint32_t w[4] = {0u, 0u, 0u, 0u};
+    if (j < p.Nt) {
+      const int64_t kk = 8 * kc + p.k0;
+      const int64_t tp0 = p.path == 0 ? p.c + (int64_t)j * p.down - kk * p.up
+                                      : p.c + p.down * (int64_t)j - p.up * (pp + p.down * kk);
+      if (z_staged) {
+        const uint16_t *zt = zline + (size_t)t * zlen + (tp0 - tp_lo);
+#pragma unroll
+        for (int e = 0; e < 8; e++) w[e >> 1] |= (uint32_t)zt[e * dtp] << (16 * (e & 1));
+      } else {
+#pragma unroll
+        for (int e = 0; e < 8; e++) w[e >> 1] |= w_term(t, tp0 + e * dtp) << (16 * (e & 1));
+      }
+    }
+    *reinterpret_cast<uint4 *>(warr(pp) + tc::kmajor_offset(row, 8 * kc, p.Kp)) = make_uint4(w[0], w[1], w[2], w[3]);
   }
   tc::fence_async_smem();
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = tmem_slot;
+  if (tid == 0) GBFIR_TC_TRACE(3, 0, 0);
   const uint32_t set_cols = (uint32_t)(p.MT * NPARTS * p.acols);
   const XT *xp = reinterpret_cast<const XT *>(p.x);
   (void)xp;
 
   if (warp >= kProdWarp0 && warp < kProdWarp0 + kProdWarps) {
     // ================= producers =================
+    // An iteration's raw window (one contiguous run of P*LA samples of the signal from base)
+    // comes in with one TMA bulk copy completing on raw_full[slot] when it lies inside the
+    // signal with a 16-byte aligned start; other windows (at the row ends) are staged with
+    // plain loads, zeros outside the signal.  Windows are staged nraw iterations ahead.
     const int ptid = tid - kProdWarp0 * 32;
     auto fetch = [&](int64_t itx, int slot) {
       const int64_t b = itx / p.iters_per_row;
@@ -190,88 +362,149 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
       const XT *row = xp + b * p.x_bstride;
       const int64_t base = p.path == 0 ? p.rp * q0 + p.k0 : p.down * (p.rp * q0 + p.k0);
       XT *dst = rawp(slot);
-      constexpr int G = 16 / (int)sizeof(XT);
-      // windows inside the signal with a 16-byte aligned start come in 16-byte pieces; the
-      // others element by element, zero-filled outside the signal
-      const bool vec = ((reinterpret_cast<uintptr_t>(row + base) | (uintptr_t)tc::smem_u32(dst)) & 15) == 0 &&
-                       base >= 0 && base + (int64_t)raw_elems <= p.N && raw_elems % G == 0;
-      if (vec) {
-        for (int v = ptid; v < (int)(raw_elems / G); v += kNProd)
-          cp_async_zfill<16>(dst + (size_t)v * G, row + base + (int64_t)v * G, true);
+      const size_t bytes = raw_elems * sizeof(XT);
+      const bool bulk = ((reinterpret_cast<uintptr_t>(row + base) | (uintptr_t)tc::smem_u32(dst)) & 15) == 0 &&
+                        base >= 0 && base + (int64_t)raw_elems <= p.N && bytes % 16 == 0 && bytes < (1u << 20);
+      if (bulk) {
+        // four bulk copies (16-byte multiples) from four lanes, so the pieces are in flight
+        // together; the transaction count is set before any of them is issued
+        if (ptid < 32) {
+          if (ptid == 0) {
+            tc::fence_async_smem();
+            tc::mbar_arrive_expect_tx(&raw_full[slot], (uint32_t)bytes);
+          }
+          __syncwarp();
+          const uint32_t piece = (uint32_t)(((bytes / 4) + 15) & ~(size_t)15);
+          const uint32_t off = (uint32_t)ptid * piece;
+          if (ptid < 4 && off < bytes) {
+            const uint32_t nb = (uint32_t)std::min<size_t>(piece, bytes - off);
+            tc::bulk_copy_g2s(reinterpret_cast<unsigned char *>(dst) + off,
+                              reinterpret_cast<const unsigned char *>(row + base) + off, nb, &raw_full[slot]);
+          }
+        }
       } else {
         for (int v = ptid; v < (int)raw_elems; v += kNProd) {
           const int64_t gi = base + v;
-          const bool okk = gi >= 0 && gi < p.N;
-          cp_async_zfill<sizeof(XT)>(dst + v, okk ? (const void *)(row + gi) : (const void *)row, okk);
+          dst[v] = (gi >= 0 && gi < p.N) ? row[gi] : zero_val<XT>();
         }
+        named_sync(1, kNProd);
+        if (ptid == 0) tc::mbar_arrive_plain(&raw_full[slot]);
       }
     };
     const int nraw = p.nraw;
-    int64_t it = blockIdx.x;
-    if (it < p.niters) fetch(it, 0);
-    cp_async_commit();
-    if (nraw == 2 && it + gridDim.x < p.niters) fetch(it + gridDim.x, 1);
-    cp_async_commit();
+    const int64_t my_iters = p.niters > blockIdx.x ? (p.niters - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    if (my_iters > 0) fetch(blockIdx.x, 0);
+    if (nraw == 2 && my_iters > 1) fetch(blockIdx.x + gridDim.x, 1);
     const int nslots = p.nbuf;
-    for (int k = 0; it < p.niters; it += gridDim.x, ++k) {
-      const int slot = k % nslots;
-      const int rslot = nraw == 2 ? (k & 1) : 0;
-      // with two raw slots this iteration's group is the older of two outstanding ones;
-      // with one slot it is the most recent group
-      if (nraw == 2) cp_async_wait<1>();
-      else cp_async_wait<0>();
-      // one thread waits for the slot; the named barrier publishes its verdict (and every
-      // producer's landed copies) to all producers, so the role leaves the loop together
-      if (ptid == 0)
-        s_pok = (k < nslots) ? 1 : (tc::mbar_wait(&op_empty[slot], ((k - nslots) / nslots) & 1) ? 1 : 0);
+    const uint32_t swz = p.rp == 64 ? 7u : 0u;
+    const int half = p.LA / 2;
+    for (int64_t k = 0; k < my_iters; ++k) {
+      const int slot = (int)(k % nslots);
+      if (ptid == 0) GBFIR_TC_TRACE(0, (int)k, 0);
+      const int rslot = nraw == 2 ? (int)(k & 1) : 0;
+      // one thread waits for the raw window and the operand slot; the named barrier publishes
+      // its verdict to all producers, so the role leaves the loop together
+      if (ptid == 0) {
+        bool ok = tc::mbar_wait(&raw_full[rslot], (uint32_t)((k / nraw) & 1));
+        if (ok && k >= nslots) ok = tc::mbar_wait(&op_empty[slot], (uint32_t)(((k - nslots) / nslots) & 1));
+        s_pok = ok ? 1 : 0;
+      }
       named_sync(1, kNProd);
+      if (ptid == 0) GBFIR_TC_TRACE(0, (int)k, 1);
       if (!s_pok) {
         s_fail = 1;
+        // windows still in flight land before the CTA's shared memory goes away
+        if (ptid == 0)
+          for (int64_t j = k; j < my_iters && j < k + nraw; j++)
+            (void)tc::mbar_wait(&raw_full[nraw == 2 ? (int)(j & 1) : 0], (uint32_t)((j / nraw) & 1));
         break;
       }
-      // convert raw slot -> operand slot: two consecutive samples of one component per item
-      // (with 64-sample rows the 4-byte pair at byte o goes to the 128-byte-swizzled slot
-      // o ^ ((o >> 7) & 7) << 4; a warp writes one 128-byte row, conflict-free)
+      // convert raw slot -> operand slot.  One component (P == 1): eight consecutive samples
+      // per item, 16-byte shared loads and one 16-byte store per term and part (with 64-sample
+      // rows the 16-byte chunk at byte o goes to o ^ ((o >> 7) & 7) << 4 of the 128-byte
+      // swizzle; a quarter warp writes one 128-byte row, conflict-free).  Polyphase
+      // components (P > 1): pairs of samples of one component per item.
       const XT *src = rawp(rslot);
-      const int half = p.LA / 2;
-      const uint32_t swz = p.rp == 64 ? 7u : 0u;
-      for (int pp = 0; pp < p.P; pp++) {
+      if (p.P == 1) {
         unsigned char *dst[NPARTS][3];
 #pragma unroll
         for (int part = 0; part < NPARTS; part++)
 #pragma unroll
-          for (int t = 0; t < 3; t++) dst[part][t] = xarrp(slot, part, t < p.terms ? t : 0, pp);
-        for (int v = ptid; v < half; v += kNProd) {
-          const int u = 2 * v;
-          const uint32_t o = 4u * (uint32_t)v;
-          const uint32_t po = o ^ (((o >> 7) & swz) << 4);
-          XT v0, v1;
-          if (p.P == 1) {
-            if constexpr (XC) {
-              const float4 w = *reinterpret_cast<const float4 *>(src + u);
-              v0 = make_float2(w.x, w.y);
-              v1 = make_float2(w.z, w.w);
-            } else {
-              const float2 w = *reinterpret_cast<const float2 *>(src + u);
-              v0 = w.x;
-              v1 = w.y;
+          for (int t = 0; t < 3; t++) dst[part][t] = xarrp(slot, part, t < p.terms ? t : 0, 0);
+        const int n8 = p.LA / 8;
+        for (int u = ptid; u < n8; u += kNProd) {
+          float vr[8], vi[8];
+          if constexpr (XC) {
+            const float4 *s4 = reinterpret_cast<const float4 *>(src + 8 * u);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              const float4 w = s4[q];
+              vr[2 * q] = w.x;
+              vi[2 * q] = w.y;
+              vr[2 * q + 1] = w.z;
+              vi[2 * q + 1] = w.w;
             }
           } else {
-            v0 = src[(size_t)u * p.P + pp];
-            v1 = src[(size_t)(u + 1) * p.P + pp];
+            const float4 *s4 = reinterpret_cast<const float4 *>(src + 8 * u);
+            const float4 w0 = s4[0], w1 = s4[1];
+            vr[0] = w0.x; vr[1] = w0.y; vr[2] = w0.z; vr[3] = w0.w;
+            vr[4] = w1.x; vr[5] = w1.y; vr[6] = w1.z; vr[7] = w1.w;
           }
+          const uint32_t o = 16u * (uint32_t)u;
+          const uint32_t po = o ^ (((o >> 7) & swz) << 4);
 #pragma unroll
           for (int part = 0; part < NPARTS; part++) {
-            const float2 f = part == 0 ? make_float2(re_of(v0), re_of(v1)) : make_float2(im_of(v0), im_of(v1));
+            const float *v = part == 0 ? vr : vi;
             if (p.fp16) {
-              *reinterpret_cast<__half2 *>(dst[part][0] + po) = __float22half2_rn(f);
+              uint4 h4;
+              h4.x = tw_pack_h2(v[0], v[1]);
+              h4.y = tw_pack_h2(v[2], v[3]);
+              h4.z = tw_pack_h2(v[4], v[5]);
+              h4.w = tw_pack_h2(v[6], v[7]);
+              *reinterpret_cast<uint4 *>(dst[part][0] + po) = h4;
             } else {
-              __nv_bfloat162 t0, t1, t2;
-              tc::split3_bf16x2(f, t0, t1, t2);
-              *reinterpret_cast<__nv_bfloat162 *>(dst[part][0] + po) = t0;
+              uint32_t w0[4], w1[4], w2[4];
+#pragma unroll
+              for (int q = 0; q < 4; q++) {
+                __nv_bfloat162 t0, t1, t2;
+                tc::split3_bf16x2(make_float2(v[2 * q], v[2 * q + 1]), t0, t1, t2);
+                w0[q] = *reinterpret_cast<uint32_t *>(&t0);
+                w1[q] = *reinterpret_cast<uint32_t *>(&t1);
+                w2[q] = *reinterpret_cast<uint32_t *>(&t2);
+              }
+              *reinterpret_cast<uint4 *>(dst[part][0] + po) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
               if (p.terms == 3) {
-                *reinterpret_cast<__nv_bfloat162 *>(dst[part][1] + po) = t1;
-                *reinterpret_cast<__nv_bfloat162 *>(dst[part][2] + po) = t2;
+                *reinterpret_cast<uint4 *>(dst[part][1] + po) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+                *reinterpret_cast<uint4 *>(dst[part][2] + po) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+              }
+            }
+          }
+        }
+      } else {
+        for (int pp = 0; pp < p.P; pp++) {
+          unsigned char *dst[NPARTS][3];
+#pragma unroll
+          for (int part = 0; part < NPARTS; part++)
+#pragma unroll
+            for (int t = 0; t < 3; t++) dst[part][t] = xarrp(slot, part, t < p.terms ? t : 0, pp);
+          for (int v = ptid; v < half; v += kNProd) {
+            const int u = 2 * v;
+            const XT a0 = src[(size_t)u * p.P + pp], a1 = src[(size_t)(u + 1) * p.P + pp];
+            const uint32_t o = 4u * (uint32_t)v;
+            const uint32_t po = o ^ (((o >> 7) & swz) << 4);
+#pragma unroll
+            for (int part = 0; part < NPARTS; part++) {
+              const float2 f = part == 0 ? make_float2(re_of(a0), re_of(a1)) : make_float2(im_of(a0), im_of(a1));
+              if (p.fp16) {
+                *reinterpret_cast<uint32_t *>(dst[part][0] + po) = tw_pack_h2(f.x, f.y);
+              } else {
+                __nv_bfloat162 t0, t1, t2;
+                tc::split3_bf16x2(f, t0, t1, t2);
+                *reinterpret_cast<__nv_bfloat162 *>(dst[part][0] + po) = t0;
+                if (p.terms == 3) {
+                  *reinterpret_cast<__nv_bfloat162 *>(dst[part][1] + po) = t1;
+                  *reinterpret_cast<__nv_bfloat162 *>(dst[part][2] + po) = t2;
+                }
               }
             }
           }
@@ -280,12 +513,11 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
       tc::fence_async_smem();
       named_sync(1, kNProd);
       if (ptid == 0) mbar_arrive(&op_full[slot]);
-      // the raw slot is consumed: stage iteration k + nraw into it
-      const int64_t it2 = it + (int64_t)nraw * gridDim.x;
-      if (it2 < p.niters) fetch(it2, rslot);
-      cp_async_commit();
+      if (ptid == 0) GBFIR_TC_TRACE(0, (int)k, 2);
+      // the raw slot is consumed (every producer passed the barrier): stage iteration
+      // k + nraw into it
+      if (k + nraw < my_iters) fetch(blockIdx.x + (k + nraw) * (int64_t)gridDim.x, rslot);
     }
-    cp_async_wait<0>();
   } else if (warp == 0) {
     // ================= MMA issuer =================
     // every TMEM column the MMAs touch lies inside the allocation (checked once)
@@ -311,8 +543,10 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
       int64_t it = blockIdx.x;
       for (int k = 0; it < p.niters; it += gridDim.x, ++k) {
         const int slot = k % p.nbuf, tset = k % p.nsets;
+        GBFIR_TC_TRACE(1, k, 0);
         if (!tc::mbar_wait(&op_full[slot], (k / p.nbuf) & 1)) { s_fail = 1; break; }
         if (k >= p.nsets && !tc::mbar_wait(&tm_empty[tset], ((k - p.nsets) / p.nsets) & 1)) { s_fail = 1; break; }
+        GBFIR_TC_TRACE(1, k, 1);
         tc::tc_fence_after();
         const uint32_t dset = tmem + (uint32_t)tset * set_cols;
         // Issue order (measured): with three terms, accumulator-major — per (M-tile, part)
@@ -368,18 +602,20 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
           }
         }
         tc::mma_commit(&op_empty[slot]);
+        GBFIR_TC_TRACE(1, k, 2);
         tc::mma_commit(&tm_full[tset]);
       }
     }
   } else {
     // ================= epilogue (warps 8-11: TMEM lane quarters 0-3) =================
     const int quarter = warp - kEpiWarp0;
-    const uint32_t lane_base = (uint32_t)(32 * quarter) << 16;
     int64_t it = blockIdx.x;
     for (int k = 0; it < p.niters; it += gridDim.x, ++k) {
       const int slot = k % p.nsets;
+      if (quarter == 0 && lane == 0) GBFIR_TC_TRACE(2, k, 0);
       if (quarter == 0 && lane == 0) s_eok = tc::mbar_wait(&tm_full[slot], (k / p.nsets) & 1) ? 1 : 0;
       named_sync(2, 128);
+      if (quarter == 0 && lane == 0) GBFIR_TC_TRACE(2, k, 1);
       if (!s_eok) {
         s_fail = 1;
         break;
@@ -389,66 +625,19 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
       const int64_t b = it / p.iters_per_row;
       const int64_t q0 = (it - b * p.iters_per_row) * (int64_t)(128 * p.MT);
       XT *orow = reinterpret_cast<XT *>(p.out) + b * p.out_bstride;
+      const bool blocks3 = p.terms == 3 && p.concat;
       for (int m = 0; m < p.MT; m++) {
-        const int64_t q = q0 + 128 * m + 32 * quarter + lane;
-        const int64_t n0 = q * p.Nt;
-        const int64_t left64 = p.out_len - n0;
-        const int nv = left64 < p.Nt ? (left64 > 0 ? (int)left64 : 0) : p.Nt;  // valid outputs of this row
-        XT *dst = orow + n0;
-        const bool vec = (reinterpret_cast<uintptr_t>(dst) & 15) == 0;
-        const bool blocks3 = p.terms == 3 && p.concat;
-        for (int col = 0; col < p.Nmma; col += 16) {
-          float acc[NPARTS][16];
-#pragma unroll
-          for (int part = 0; part < NPARTS; part++) {
-            const uint32_t base = dset + lane_base + (uint32_t)((m * NPARTS + part) * p.acols + col);
-            uint32_t r0[16], r1[16], r2[16];
-            tc::tmem_ld16(base, r0);
-            if (blocks3) {
-              tc::tmem_ld16(base + (uint32_t)p.Nmma, r1);
-              tc::tmem_ld16(base + (uint32_t)(2 * p.Nmma), r2);
-            }
-            tc::tmem_ld_wait();
-            if (blocks3) {
-#pragma unroll
-              for (int i = 0; i < 16; i++)
-                acc[part][i] = (__uint_as_float(r0[i]) + __uint_as_float(r1[i])) + __uint_as_float(r2[i]);
-            } else {
-#pragma unroll
-              for (int i = 0; i < 16; i++) acc[part][i] = __uint_as_float(r0[i]);
-            }
-          }
-          if constexpr (XC) {
-            // pairs of outputs as one 16-byte store where the row start is 16-byte aligned
-#pragma unroll
-            for (int i = 0; i < 16; i += 2) {
-              if (vec && col + i + 1 < nv) {
-                *reinterpret_cast<float4 *>(dst + col + i) =
-                    make_float4(acc[0][i], acc[1][i], acc[0][i + 1], acc[1][i + 1]);
-              } else {
-                if (col + i < nv) dst[col + i] = make_float2(acc[0][i], acc[1][i]);
-                if (col + i + 1 < nv) dst[col + i + 1] = make_float2(acc[0][i + 1], acc[1][i + 1]);
-              }
-            }
-          } else {
-            // groups of four outputs as one 16-byte store where the row start is aligned
-#pragma unroll
-            for (int i = 0; i < 16; i += 4) {
-              if (vec && col + i + 3 < nv) {
-                *reinterpret_cast<float4 *>(dst + col + i) =
-                    make_float4(acc[0][i], acc[0][i + 1], acc[0][i + 2], acc[0][i + 3]);
-              } else {
-#pragma unroll
-                for (int e = 0; e < 4; e++)
-                  if (col + i + e < nv) dst[col + i + e] = acc[0][i + e];
-              }
-            }
-          }
+        for (int half = 0; half < 2; half++) {
+          const int64_t qa = q0 + 128 * m + 32 * quarter + 16 * half + (lane >> 2);
+          const uint32_t tb = dset + ((uint32_t)(32 * quarter + 16 * half) << 16) + (uint32_t)(m * NPARTS * p.acols);
+          if (blocks3) tcr_drain_half<XC, 3>(p, tb, orow, qa, lane);
+          else tcr_drain_half<XC, 1>(p, tb, orow, qa, lane);
         }
       }
       tc::tc_fence_before();
       named_sync(2, 128);
       if (quarter == 0 && lane == 0) mbar_arrive(&tm_empty[slot]);
+      if (quarter == 0 && lane == 0) GBFIR_TC_TRACE(2, k, 2);
     }
   }
   __syncthreads();
@@ -542,8 +731,10 @@ static TcPlan plan_tc(int64_t up, int64_t down, const TcTaps &taps, int64_t N_in
     return pl;
   }
   const int nparts = xc ? 2 : 1;
-  // bf16x3: concatenate the tap terms along N where 3*N fits one MMA, else six MMAs of N
-  p.concat = (p.terms == 3 && 3 * p.Nmma <= 256) ? 1 : 0;
+  // bf16x3: rows of fewer than 64 columns concatenate the tap terms along N (3*N fits one
+  // MMA); wider rows issue six MMAs of N into one accumulator, so the epilogue reads one
+  // column block instead of three
+  p.concat = (p.terms == 3 && 3 * p.Nmma <= 256 && p.Nmma < 64) ? 1 : 0;
   p.acols = p.concat ? 3 * p.Nmma : p.Nmma;
   const int wrows = p.terms * p.Nmma;
   const size_t xalign = rp == 64 ? 1024 : 128;
@@ -589,6 +780,10 @@ static TcPlan plan_tc(int64_t up, int64_t down, const TcTaps &taps, int64_t N_in
 #include "tc_wide.h"
 namespace gbfir {
 
+int launch_tc_blocks(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t up, int64_t down,
+                     int64_t Lo, int64_t c, int even, int rev, double scale, int precision, const char *what,
+                     cudaStream_t s);
+
 static int launch_tc(TcPlan &pl, const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, bool xc,
                      const char *what, cudaStream_t s) {
   TcParams &p = pl.p;
@@ -625,17 +820,14 @@ static int tc_rows_pref() {
   return 0;
 }
 
-// The Toeplitz plan to run, or the one the preference pins: 64-sample rows where they keep
-// the whole pipeline (two operand slots, two accumulator sets), else 8-sample rows, else
-// 64-sample rows with whatever pipeline fits.
+// The Toeplitz plan to run, or the one the preference pins: 64-sample rows where the tile
+// fits (measured faster even with one operand slot), else 8-sample rows.
 static TcPlan plan_tc_rows(int64_t up, int64_t down, const TcTaps &taps, int64_t N_in, int64_t out_len,
                            int64_t batch, int xc, int precision, int pref) {
   if (pref == 8 || pref == 64) return plan_tc(up, down, taps, N_in, out_len, batch, xc, precision, pref);
   TcPlan wide = plan_tc(up, down, taps, N_in, out_len, batch, xc, precision, 64);
-  if (wide.ok && wide.p.nbuf == 2 && wide.p.nsets == 2) return wide;
-  TcPlan narrow = plan_tc(up, down, taps, N_in, out_len, batch, xc, precision, 8);
-  if (narrow.ok || !wide.ok) return narrow;
-  return wide;
+  if (wide.ok) return wide;
+  return plan_tc(up, down, taps, N_in, out_len, batch, xc, precision, 8);
 }
 
 int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int64_t up, int64_t down,
@@ -646,18 +838,24 @@ int resample_poly_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf 
   const bool xc = dtype_complex(in.dtype);
   const TcTaps taps = resample_taps(h.len, up);
   const int pref = tc_rows_pref();
+  // The Toeplitz kernel with 64-sample rows where its tile fits (measured fastest); else
   // 64-sample rows with the taps in TMEM where they fill at least half of the 128 MMA lanes
-  // with output phases (measured faster there); the Toeplitz kernel otherwise
+  // with output phases; else the Toeplitz kernel with 8-sample rows.
+  if (pref == 0) {
+    TcPlan wide = plan_tc(up, down, taps, in.len, out.len, out.batch, xc, precision, 64);
+    if (wide.ok) return launch_tc(wide, out, in, h, xc, "resample_poly (tensor cores)", s);
+  }
   if ((pref == 0 || pref == 1) && 64 % down == 0 && 64 * up / down >= 64) {
     TwPlan wp = plan_tc_wide(up, down, taps.Lo, taps.c, taps.even, taps.rev, taps.scale, in.len, out.len, out.batch,
                              xc, precision);
     if (wp.ok) return launch_tc_wide(wp, out, in, h, xc, "resample_poly (tensor cores)", s);
   }
   TcPlan pl = plan_tc_rows(up, down, taps, in.len, out.len, out.batch, xc, precision, pref);
-  if (!pl.ok)
-    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly: tensor-core form unavailable for up=%lld down=%lld: %s",
-               (long long)up, (long long)down, pl.why);
-  return launch_tc(pl, out, in, h, xc, "resample_poly (tensor cores)", s);
+  if (pl.ok) return launch_tc(pl, out, in, h, xc, "resample_poly (tensor cores)", s);
+  // rows that advance a number of samples no aliased layout expresses (e.g. 160/147):
+  // materialised Hankel rows in column blocks
+  return launch_tc_blocks(out, in, h, up, down, taps.Lo, taps.c, taps.even, taps.rev, taps.scale, precision,
+                          "resample_poly (tensor cores)", s);
 }
 
 // conv1d / corr on the tensor cores: the Toeplitz pass with up = down = 1, no even-length
@@ -698,16 +896,19 @@ int resample_poly_bwd_dx_tc(const gbfir_buf &dx, const gbfir_buf &gy, const gbfi
   TcTaps taps = resample_taps(h.len, up);
   taps.rev = 1;
   const int pref = tc_rows_pref();
+  if (pref == 0) {
+    TcPlan wide = plan_tc(down, up, taps, gy.len, dx.len, dx.batch, 0, precision, 64);
+    if (wide.ok) return launch_tc(wide, dx, gy, h, false, "resample_poly_bwd dx (tensor cores)", s);
+  }
   if (pref == 0 || pref == 1) {
     TwPlan wp = plan_tc_wide(down, up, taps.Lo, taps.c, taps.even, taps.rev, taps.scale, gy.len, dx.len, dx.batch, 0,
                              precision);
     if (wp.ok) return launch_tc_wide(wp, dx, gy, h, false, "resample_poly_bwd dx (tensor cores)", s);
   }
   TcPlan pl = plan_tc_rows(down, up, taps, gy.len, dx.len, dx.batch, 0, precision, pref);
-  if (!pl.ok)
-    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly_bwd: tensor-core dx unavailable for up=%lld down=%lld: %s",
-               (long long)up, (long long)down, pl.why);
-  return launch_tc(pl, dx, gy, h, false, "resample_poly_bwd dx (tensor cores)", s);
+  if (pl.ok) return launch_tc(pl, dx, gy, h, false, "resample_poly_bwd dx (tensor cores)", s);
+  return launch_tc_blocks(dx, gy, h, down, up, taps.Lo, taps.c, taps.even, taps.rev, taps.scale, precision,
+                          "resample_poly_bwd dx (tensor cores)", s);
 }
 
 int tc_status_read_and_clear() {
@@ -723,6 +924,8 @@ namespace gbfir {
 int resample_rowtile_status();
 int adjoint_rowtile_status();
 int tc_wide_status_take();
+int tc_channelize_status_take();
+int tc_blocks_status_take();
 int iir_status_take();
 }  // namespace gbfir
 
@@ -735,6 +938,8 @@ extern "C" int gbfir_tc_status(void) {
   const int c = gbfir::adjoint_rowtile_status();
   const int d = gbfir::tc_wide_status_take();
   const int e = gbfir::iir_status_take();
-  if (a < 0 || b < 0 || c < 0 || d < 0 || e < 0) return -1;
-  return (a | b | c | d | e) ? 1 : 0;
+  const int f = gbfir::tc_channelize_status_take();
+  const int g = gbfir::tc_blocks_status_take();
+  if (a < 0 || b < 0 || c < 0 || d < 0 || e < 0 || f < 0 || g < 0) return -1;
+  return (a | b | c | d | e | f | g) ? 1 : 0;
 }

@@ -73,13 +73,6 @@ __device__ __forceinline__ uint64_t tw_desc_sw128(uint32_t saddr) {
   return tc::smem_desc(saddr, 16u, 1024u) | ((uint64_t)2 << 61);
 }
 
-__device__ __forceinline__ float tw_tap(const TwParams &p, int64_t tp) {
-  if (tp < 0 || tp >= p.Lo) return 0.f;
-  const int64_t te = p.rev ? p.Lo - 1 - tp : tp;
-  if (p.even && te == 0) return 0.f;
-  return p.h[te - p.even];
-}
-
 __device__ __forceinline__ uint32_t tw_pack_fp16(float a, float b) {
   return (uint32_t)__half_as_ushort(__float2half_rn(a)) | ((uint32_t)__half_as_ushort(__float2half_rn(b)) << 16);
 }
@@ -118,6 +111,42 @@ __global__ void __launch_bounds__(kTwThreads, 1) tc_wide_kernel(const TwParams p
   tc::tc_fence_after();
   const uint32_t tmem = tmem_slot;
 
+  // ---- the taps, scaled and split into the operand terms once (hterm[t][e] = term t of
+  // scale * h[e], 16-bit), staged in the raw ring (not in use yet) ----
+  const int64_t Lh = p.Lo - p.even;
+  const bool h_staged = (size_t)Lh * 2 * p.terms <= (size_t)p.nraw * p.raw_elems * sizeof(XT);
+  uint16_t *hterm = reinterpret_cast<uint16_t *>(raw0);
+  auto split_terms = [&](float v, uint16_t (&o)[3]) {
+    if (p.fp16) {
+      o[0] = __half_as_ushort(__float2half_rn(v));
+      o[1] = o[2] = 0;
+    } else {
+      __nv_bfloat16 t0, t1, t2;
+      tc::split3_bf16(v, t0, t1, t2);
+      o[0] = __bfloat16_as_ushort(t0);
+      o[1] = __bfloat16_as_ushort(t1);
+      o[2] = __bfloat16_as_ushort(t2);
+    }
+  };
+  if (h_staged) {
+    for (int64_t e = tid; e < Lh; e += kTwThreads) {
+      uint16_t o[3];
+      split_terms(p.h[e] * (float)p.scale, o);
+      for (int t = 0; t < p.terms; t++) hterm[t * Lh + e] = o[t];
+    }
+  }
+  __syncthreads();
+  // term t of W at tap position tp (he read reversed when rev, 0 outside the filter)
+  auto w_term = [&](int t, int64_t tp) -> uint32_t {
+    if (tp < 0 || tp >= p.Lo) return 0u;
+    const int64_t te = p.rev ? p.Lo - 1 - tp : tp;
+    if (p.even && te == 0) return 0u;
+    const int64_t e = te - p.even;
+    if (h_staged) return hterm[t * Lh + e];
+    uint16_t o[3];
+    split_terms(p.h[e] * (float)p.scale, o);
+    return o[t];
+  };
   // ---- W into TMEM: lane j = output phase, columns = K packed two per column ----
   if (warp >= kTwEpi0) {
     const int quarter = warp - kTwEpi0;
@@ -130,20 +159,10 @@ __global__ void __launch_bounds__(kTwThreads, 1) tc_wide_kernel(const TwParams p
 #pragma unroll
         for (int i = 0; i < 16; i++) {
           const int k = 2 * (kc + i);
-          float v0 = 0.f, v1 = 0.f;
+          r[i] = 0u;
           if (j < p.Nt) {
             const int64_t tb = p.c + (int64_t)j * p.down - (p.k0 + k) * p.up;
-            v0 = tw_tap(p, tb) * (float)p.scale;
-            v1 = tw_tap(p, tb - p.up) * (float)p.scale;
-          }
-          if (p.fp16) {
-            r[i] = tw_pack_fp16(v0, v1);
-          } else {
-            __nv_bfloat16 a0, a1, a2, b0, b1, b2;
-            tc::split3_bf16(v0, a0, a1, a2);
-            tc::split3_bf16(v1, b0, b1, b2);
-            const __nv_bfloat16 lo = t == 0 ? a0 : (t == 1 ? a1 : a2), hi = t == 0 ? b0 : (t == 1 ? b1 : b2);
-            r[i] = (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+            r[i] = w_term(t, tb) | (w_term(t, tb - p.up) << 16);
           }
         }
         tw_tmem_st16(tmem + lane_base + (uint32_t)(p.wcol0 + t * half + kc), r);

@@ -50,7 +50,7 @@ class RaggedPlan:
         cnt = lib.gbfir_ragged_plan(descs, n, None, ctypes.byref(info))
         if cnt < 0:
             _lib.check(-cnt)
-        table = np.empty((cnt, 2), dtype=np.int64)
+        table = np.empty((cnt, 4), dtype=np.int64)
         cnt2 = lib.gbfir_ragged_plan(descs, n, table.ctypes.data_as(ctypes.c_void_p), ctypes.byref(info))
         if cnt2 != cnt:
             _lib.check(5 if cnt2 >= 0 else -cnt2)

@@ -24,14 +24,18 @@ import torch
 
 
 class RowPipeline:
-    def __init__(self, device: torch.device, rows_per_chunk: int = 8):
+    def __init__(self, device: torch.device, rows_per_chunk: int = 8, copy_streams: int = 2):
+        """``copy_streams`` device->host streams share each chunk's copies back (row slices
+        of every output), so several copy engines drain the results at once."""
         if rows_per_chunk < 1:
             raise ValueError("rows_per_chunk must be >= 1")
+        if copy_streams < 1:
+            raise ValueError("copy_streams must be >= 1")
         self.device = torch.device(device)
         self.rows = int(rows_per_chunk)
         self.s_in = torch.cuda.Stream(self.device)
         self.s_cmp = torch.cuda.Stream(self.device)
-        self.s_out = torch.cuda.Stream(self.device)
+        self.s_outs = [torch.cuda.Stream(self.device) for _ in range(int(copy_streams))]
         self._bufs = None
 
     def _buffers(self, x: torch.Tensor, outs: Sequence[torch.Tensor]):
@@ -54,13 +58,14 @@ class RowPipeline:
         if any(o.shape[0] != B for o in outs):
             raise ValueError("every output needs the same number of rows as the input")
         xb, ob = self._buffers(x, outs)
+        ns = len(self.s_outs)
         h2d = [torch.cuda.Event() for _ in range(2)]
         cmp = [torch.cuda.Event() for _ in range(2)]
-        d2h = [torch.cuda.Event() for _ in range(2)]
+        d2h = [[torch.cuda.Event() for _ in range(ns)] for _ in range(2)]
         used = [False, False]
         caller = torch.cuda.current_stream(self.device)
         # the pipeline's work is ordered after what the caller already queued
-        for s in (self.s_in, self.s_cmp, self.s_out):
+        for s in (self.s_in, self.s_cmp, *self.s_outs):
             s.wait_stream(caller)
         for c, r0 in enumerate(range(0, B, self.rows)):
             r1 = min(B, r0 + self.rows)
@@ -73,15 +78,22 @@ class RowPipeline:
                 h2d[k].record(self.s_in)
             self.s_cmp.wait_event(h2d[k])
             if used[k]:
-                self.s_cmp.wait_event(d2h[k])     # chunk c-2's outputs have left ob[k]
+                for e in d2h[k]:
+                    self.s_cmp.wait_event(e)      # chunk c-2's outputs have left ob[k]
             with torch.cuda.stream(self.s_cmp):
                 fn(xb[k][:n], [b[:n] for b in ob[k]])
                 cmp[k].record(self.s_cmp)
-            self.s_out.wait_event(cmp[k])
-            with torch.cuda.stream(self.s_out):
-                for o, b in zip(outs, ob[k]):
-                    o[r0:r1].copy_(b[:n], non_blocking=True)
-                d2h[k].record(self.s_out)
+            # copy stream j takes the j-th contiguous slice of the chunk's rows
+            bounds = [n * j // ns for j in range(ns + 1)]
+            for j, so in enumerate(self.s_outs):
+                so.wait_event(cmp[k])
+                a, b_ = bounds[j], bounds[j + 1]
+                with torch.cuda.stream(so):
+                    if b_ > a:
+                        for o, b in zip(outs, ob[k]):
+                            o[r0 + a:r0 + b_].copy_(b[a:b_], non_blocking=True)
+                    d2h[k][j].record(so)
             used[k] = True
         # the caller's stream sees every copy back
-        caller.wait_stream(self.s_out)
+        for so in self.s_outs:
+            caller.wait_stream(so)

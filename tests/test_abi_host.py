@@ -207,15 +207,30 @@ def test_ragged_plan_validation(lib):
     assert lib.gbfir_ragged_plan(d, 2, None, ctypes.byref(info)) == -7
     d[1] = RaggedDesc(FAKE + 4, FAKE, FAKE, 1000, 800, 101, 4, 5, 0)  # misaligned complex input
     assert lib.gbfir_ragged_plan(d, 2, None, ctypes.byref(info)) == -8
-    # tiles are ordered most expensive first and cover every row tile
+    # work items cover every row of every signal exactly once, in runs of consecutive rows
     d[1] = RaggedDesc(FAKE, FAKE, FAKE, 100000, 80000, 101, 4, 5, 0)
     n = lib.gbfir_ragged_plan(d, 2, None, ctypes.byref(info))
     import numpy as np
-    t = np.empty((n, 2), dtype=np.int64)
+    t = np.empty((n, 4), dtype=np.int64)
     assert lib.gbfir_ragged_plan(d, 2, t.ctypes.data_as(ctypes.c_void_p), ctypes.byref(info)) == n
     assert set(t[:, 0].tolist()) == {0, 1}
+    for sig in (0, 1):
+        runs = sorted((int(r0), int(nr)) for s_, r0, nr, _ in t if s_ == sig)
+        assert runs[0][0] == 0 and all(nr > 0 for _, nr in runs)
+        assert all(a[0] + a[1] == b[0] for a, b in zip(runs, runs[1:]))
+    assert info.buffers in (1, 2) and info.window_elems > 0
+    assert info.table_bytes + info.buffers * info.window_elems * 8 <= info.shared_bytes
+    # a registered tile shape reaches the items of its rate and tap-length bucket
+    assert lib.gbfir_ragged_tile_register(8, 10, 100, 2, 4, 2) == 0   # (4,5), taps 65..128
+    n2 = lib.gbfir_ragged_plan(d, 2, None, ctypes.byref(info))
+    t2 = np.empty((n2, 4), dtype=np.int64)
+    lib.gbfir_ragged_plan(d, 2, t2.ctypes.data_as(ctypes.c_void_p), ctypes.byref(info))
+    assert set(t2[t2[:, 0] == 1, 3].tolist()) == {2 | (4 << 4) | (2 << 8)}
+    assert set(t2[t2[:, 0] == 0, 3].tolist()) == {0}
+    assert lib.gbfir_ragged_tile_register(4, 5, 100, 3, 4, 2) == 1     # rows per thread 1 or 2
+    assert lib.gbfir_ragged_tile_clear() == 0
     # launch refuses a plan that does not come from the planner (before touching the device)
-    bad = RaggedPlanInfo(n, 300 * 1024, 0)
+    bad = RaggedPlanInfo(n, 300 * 1024, 0, 1, 2)
     assert lib.gbfir_ragged_resample(FAKE, 2, FAKE, ctypes.byref(bad), 0, FAKE, 256, None) == 1
 
 

@@ -1,7 +1,10 @@
 """Tensor-core forms of resample_poly (tcgen05 Toeplitz MMAs) against the FP64
 oracle.  Stated error bars (rel-L2 vs FP64): bf16 <= 1e-2, fp16 <= 2e-3,
-bf16x3 <= 1e-6.  Rates whose row needs more than 256 MMA columns (e.g. 160/147,
-a row of 8*160 outputs) are rejected with GBFIR_ERR_NOT_SUPPORTED."""
+bf16x3 <= 1e-6.  Rates whose rows alias an 8- or 64-sample operand pitch run the
+Hankel kernels; the others (160/147, 40/3, 7/19) the column-blocked kernel over
+materialised rows.  Double-precision signals, complex taps and decimators whose Hankel
+slab does not fit shared memory (1/17 with a 341-tap filter) are rejected with
+GBFIR_ERR_NOT_SUPPORTED."""
 import numpy as np
 import pytest
 
@@ -36,7 +39,7 @@ def kaiser(up, down):
 
 
 @pytest.mark.parametrize("updown", [(3, 2), (4, 5), (1, 2), (2, 3), (3, 4), (5, 4), (2, 1), (7, 1), (1, 7),
-                                    (6, 4), (3, 8), (5, 3)])
+                                    (6, 4), (3, 8), (5, 3), (160, 147), (40, 3), (7, 19)])
 @pytest.mark.parametrize("form", ["bf16x3", "bf16", "fp16"])
 @pytest.mark.parametrize("cplx", [True, False])
 def test_tc_resample_vs_fp64(mx, orc, updown, form, cplx):
@@ -72,10 +75,15 @@ def test_tc_resample_filter_lengths(mx, orc, L):
 
 
 def test_tc_config_rows(mx, orc):
+    """The 64 x 2^20 c64 workload at its three rates in bf16x3: sampled rows against FP64,
+    and linearity over the whole batch (resample(a*x1 + x2) = a*resample(x1) +
+    resample(x2)), which a wrong row, tile or column-block offset anywhere would break."""
     import torch
     g = torch.Generator(device="cuda").manual_seed(7)
     x = torch.randn(64, 1 << 20, dtype=torch.complex64, device="cuda", generator=g)
-    for up, down in ((3, 2), (4, 5)):
+    x2 = torch.randn(64, 1 << 20, dtype=torch.complex64, device="cuda", generator=g)
+    a = 0.625
+    for up, down in ((3, 2), (4, 5), (160, 147)):
         h = torch.from_numpy(kaiser(up, down).astype(np.float32)).cuda()
         y = mx.resample_poly(x, h, up, down, precision="bf16x3")
         assert mx._lib.load().gbfir_tc_status() == 0
@@ -83,12 +91,23 @@ def test_tc_config_rows(mx, orc):
         r = orc.resample_poly(x[rows].cpu().numpy().astype(np.complex128), h.cpu().numpy().astype(np.float64),
                               up, down, nthreads=3)
         assert rel_l2(y[rows].cpu().numpy(), r) < 1e-6
+        y2 = mx.resample_poly(x2, h, up, down, precision="bf16x3")
+        y12 = mx.resample_poly(a * x + x2, h, up, down, precision="bf16x3")
+        lin = float(((y12 - (a * y + y2)).abs().pow(2).sum() / y12.abs().pow(2).sum()).sqrt())
+        assert lin < 2e-6, (up, down, lin)
+        del y, y2, y12
 
 
-def test_tc_unsupported_rate_is_rejected(mx):
+def test_tc_unsupported_operands_are_rejected(mx):
     import torch
     x = torch.zeros(1, 1000, dtype=torch.complex64, device="cuda")
-    h = torch.ones(3201, device="cuda")
-    with pytest.raises(mx.GbfirError) as e:
-        mx.resample_poly(x, h, 160, 147, precision="bf16x3")
+    with pytest.raises(mx.GbfirError) as e:   # complex taps
+        mx.resample_poly(x, torch.ones(31, dtype=torch.complex64, device="cuda"), 3, 2, precision="bf16x3")
+    assert e.value.code == 5
+    with pytest.raises(mx.GbfirError) as e:   # double-precision signal
+        mx.resample_poly(x.to(torch.complex128), torch.ones(31, dtype=torch.float64, device="cuda"), 3, 2,
+                         precision="bf16")
+    assert e.value.code == 5
+    with pytest.raises(mx.GbfirError) as e:   # 1/17 with 341 taps: the Hankel slab needs > 225 KB
+        mx.resample_poly(x, torch.ones(341, device="cuda"), 1, 17, precision="bf16x3")
     assert e.value.code == 5
