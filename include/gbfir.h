@@ -304,8 +304,10 @@ typedef struct gbfir_ragged_plan_info {
   int64_t num_tiles;     /* entries (work items) in the tile table             */
   int64_t shared_bytes;  /* dynamic shared memory per CTA                      */
   int64_t table_bytes;   /* of which the tap table (the window buffers follow) */
-  int64_t window_elems;  /* complex samples per window buffer                  */
+  int64_t window_elems;  /* complex samples per window buffer (FP32 plans); the K
+                            chunk of the tensor-core plans                     */
   int64_t buffers;       /* window buffers per CTA (2: the next tile prefetched) */
+  int64_t precision;     /* the gbfir_precision the plan was made for          */
 } gbfir_ragged_plan_info;
 
 /* Tile shape the ragged planner uses for signals of one reduced (up, down) whose tap
@@ -329,11 +331,22 @@ GBFIR_API int gbfir_ragged_tile_clear(void);
 GBFIR_API int64_t gbfir_ragged_plan(const gbfir_ragged_desc *host_descs, int64_t count,
                           int64_t *tile_table, gbfir_ragged_plan_info *info);
 
+/* The planner for one arithmetic form (no MatX counterpart): FP32 is gbfir_ragged_plan; the
+ * tensor-core forms (BF16, FP16, BF16X3) plan the column-blocked Toeplitz-MMA pass, each
+ * signal with its own block geometry packed into its items (four int64 per item: signal,
+ * first row, rows, packed geometry), rows in tiles of 64.  A signal whose tap matrix does not
+ * fit shared memory fails the plan with GBFIR_ERR_NOT_SUPPORTED.  Pass the same precision to
+ * gbfir_ragged_resample. */
+GBFIR_API int64_t gbfir_ragged_plan_prec(const gbfir_ragged_desc *host_descs, int64_t count,
+                                         int32_t precision, int64_t *tile_table,
+                                         gbfir_ragged_plan_info *info);
+
 /* One persistent launch over all work items.  device_descs / device_tile_table are
  * device copies of the descriptors and of the planner's table; info is the
- * planner's host struct.  CTAs take items from an atomic counter in `workspace`
- * (zeroed on the stream first), so the launch balances arbitrary length skew and
- * contains no host synchronisation: it can be captured in a CUDA graph. */
+ * planner's host struct, made for `precision` (GBFIR_ERR_INVALID_PARAMETER otherwise).
+ * CTAs take items from an atomic counter in `workspace` (zeroed on the stream first), so
+ * the launch balances arbitrary length skew and contains no host synchronisation: it can
+ * be captured in a CUDA graph. */
 GBFIR_API int gbfir_ragged_resample(const gbfir_ragged_desc *device_descs, int64_t count,
                           const int64_t *device_tile_table,
                           const gbfir_ragged_plan_info *info, int32_t precision,

@@ -16,11 +16,12 @@
 // dimension is strided (conv1d with an axis, or a permuted view as in the radar
 // three-pulse canceller) run in place of the view's layout (gbfir_conv1d_axis).
 // This header adds, in namespace matx, overloads with the same parameter lists and
-// stronger constraints — a CUDA executor and MatX tensor operands of float, double,
-// complex<float> or complex<double> — so C++20 overload resolution selects them (the
-// executor argument brings namespace matx into argument-dependent lookup).  Host
-// executors, operator expressions as inputs, FFT convolutions outside the overlap-save
-// kernel's range and other value types keep MatX's own implementation.
+// stronger constraints — a CUDA executor, a MatX tensor output and tensor or operator
+// expression inputs of float, double, complex<float> or complex<double> — so C++20 overload
+// resolution selects them (the executor argument brings namespace matx into argument-
+// dependent lookup).  An expression input is evaluated once into a contiguous temporary.
+// Host executors, FFT convolutions outside the overlap-save kernel's range and other value
+// types keep MatX's own implementation.
 //
 // Each overload keeps the MatX transform's asserts and error classes: a gbfir_status
 // is rethrown as matxException with the matching matxError_t.  Tensors whose batch
@@ -51,6 +52,16 @@ constexpr int32_t dtype_of() {
 template <typename Op>
 concept routable_tensor = is_tensor_view_v<remove_cvref_t<Op>> && (remove_cvref_t<Op>::Rank() >= 1) &&
                           (dtype_of<typename remove_cvref_t<Op>::value_type>() >= 0);
+
+// An input operand: a tensor view, or an operator expression (x * 2.f, conj(x), a generator
+// ...) of a routable value type.  MatX's kernels read an expression element by element
+// (transforms/resample_poly.h:142-146 chooses between the tensor and operator paths); here
+// Staged evaluates it once into a contiguous temporary with MatX's elementwise executor,
+// after which the C-ABI sees plain rows.
+template <typename Op>
+concept routable_operand = (is_tensor_view_v<remove_cvref_t<Op>> || is_matx_op_c<Op>) &&
+                           (remove_cvref_t<Op>::Rank() >= 1) &&
+                           (dtype_of<typename remove_cvref_t<Op>::value_type>() >= 0);
 
 inline matxError_t to_matx_error(int rc) {
   switch (rc) {
@@ -110,7 +121,9 @@ struct Staged {
   decltype(make_tensor<value_type>(cuda::std::array<index_t, R>{}, MATX_ASYNC_DEVICE_MEMORY,
                                    cudaStream_t{})) tmp;
   Staged(const Op &t, const Executor &exec) {
-    if (!describe(t, buf)) {
+    bool direct = false;
+    if constexpr (is_tensor_view_v<remove_cvref_t<Op>>) direct = describe(t, buf);
+    if (!direct) {
       cuda::std::array<index_t, R> shape;
       for (int i = 0; i < R; i++) shape[i] = t.Size(i);
       (void)(tmp = make_tensor<value_type>(shape, MATX_ASYNC_DEVICE_MEMORY, exec.getStream()));
@@ -176,7 +189,7 @@ bool describe_axis(const Op &t, AxisLayout &l) {
 template <typename OutputType, typename In1Type, typename In2Type, typename Executor>
 bool conv_axis(OutputType &o, const In1Type &i1, const In2Type &i2, matxConvCorrMode_t mode, int is_corr,
                const Executor &exec) {
-  if constexpr (remove_cvref_t<In2Type>::Rank() != 1 ||
+  if constexpr (remove_cvref_t<In2Type>::Rank() != 1 || !is_tensor_view_v<remove_cvref_t<In1Type>> ||
                 remove_cvref_t<In1Type>::Rank() != remove_cvref_t<OutputType>::Rank()) {
     return false;
   } else {
@@ -198,7 +211,7 @@ bool conv_axis(OutputType &o, const In1Type &i1, const In2Type &i2, matxConvCorr
 // Replaces transforms/resample_poly.h:299-354 for CUDA executors.
 template <typename OutType, typename InType, typename FilterType, typename Executor>
   requires is_executor<Executor> && is_cuda_executor_v<Executor> && gbfir_shim::routable_tensor<OutType> &&
-           gbfir_shim::routable_tensor<InType> && gbfir_shim::routable_tensor<FilterType>
+           gbfir_shim::routable_operand<InType> && gbfir_shim::routable_operand<FilterType>
 inline void resample_poly_impl(OutType &out, const InType &in, const FilterType &f, index_t up, index_t down,
                                Executor &&exec) {
   MATX_NVTX_START("gbfir resample_poly", matx::MATX_NVTX_LOG_API)
@@ -216,7 +229,7 @@ inline void resample_poly_impl(OutType &out, const InType &in, const FilterType 
 // Replaces transforms/conv.h:467-532 for CUDA executors and the direct method.
 template <typename OutputType, typename In1Type, typename In2Type, typename Executor>
   requires is_cuda_executor_v<Executor> && gbfir_shim::routable_tensor<OutputType> &&
-           gbfir_shim::routable_tensor<In1Type> && gbfir_shim::routable_tensor<In2Type>
+           gbfir_shim::routable_operand<In1Type> && gbfir_shim::routable_operand<In2Type>
 inline void conv1d_impl(OutputType o, const In1Type &i1, const In2Type &i2, matxConvCorrMode_t mode,
                         matxConvCorrMethod_t method, const Executor &exec) {
   MATX_NVTX_START("gbfir conv1d", matx::MATX_NVTX_LOG_API)
@@ -268,7 +281,7 @@ inline void conv1d_impl(OutputType o, const In1Type &i1, const In2Type &i2, matx
 // Replaces transforms/corr.h:60-69: corr(a, b) = conv1d(a, reverse(conj(b))), applied in-kernel.
 template <typename OutputTensor, typename In1Type, typename In2Type, typename Executor>
   requires is_cuda_executor_v<Executor> && gbfir_shim::routable_tensor<OutputTensor> &&
-           gbfir_shim::routable_tensor<In1Type> && gbfir_shim::routable_tensor<In2Type>
+           gbfir_shim::routable_operand<In1Type> && gbfir_shim::routable_operand<In2Type>
 __MATX_INLINE__ void corr_impl(OutputTensor o, const In1Type i1, const In2Type i2, matxConvCorrMode_t mode,
                                [[maybe_unused]] matxConvCorrMethod_t method, const Executor &exec) {
   MATX_NVTX_START("gbfir corr", matx::MATX_NVTX_LOG_API)
@@ -329,7 +342,9 @@ struct Staged2d {
   decltype(make_tensor<value_type>(cuda::std::array<index_t, R>{}, MATX_ASYNC_DEVICE_MEMORY,
                                    cudaStream_t{})) tmp;
   Staged2d(const Op &t, const Executor &exec) {
-    if (!describe2d(t, buf)) {
+    bool direct = false;
+    if constexpr (is_tensor_view_v<remove_cvref_t<Op>>) direct = describe2d(t, buf);
+    if (!direct) {
       cuda::std::array<index_t, R> shape;
       for (int i = 0; i < R; i++) shape[i] = t.Size(i);
       (void)(tmp = make_tensor<value_type>(shape, MATX_ASYNC_DEVICE_MEMORY, exec.getStream()));
@@ -342,7 +357,7 @@ struct Staged2d {
 
 template <typename OutputType, typename In1Type, typename In2Type, typename Executor>
   requires is_cuda_executor_v<Executor> && gbfir_shim::routable_tensor<OutputType> &&
-           gbfir_shim::routable_tensor<In1Type> && gbfir_shim::routable_tensor<In2Type> &&
+           gbfir_shim::routable_operand<In1Type> && gbfir_shim::routable_operand<In2Type> &&
            (remove_cvref_t<In1Type>::Rank() >= 2) && (remove_cvref_t<In2Type>::Rank() >= 2)
 inline void conv2d_impl(OutputType o, const In1Type in1, const In2Type in2, matxConvCorrMode_t mode,
                         const Executor &exec) {
@@ -371,7 +386,7 @@ inline void conv2d_impl(OutputType o, const In1Type in1, const In2Type in2, matx
 // Replaces transforms/filter.h:456-495: without recursive coefficients conv1d SAME
 // (filter.h:185), else the recursive filter, with a workspace from MatX's allocator.
 template <size_t NR, size_t NNR, typename OutType, typename InType, typename FilterType>
-  requires gbfir_shim::routable_tensor<OutType> && gbfir_shim::routable_tensor<InType> &&
+  requires gbfir_shim::routable_tensor<OutType> && gbfir_shim::routable_operand<InType> &&
            (gbfir_shim::dtype_of<FilterType>() >= 0) && (NR <= 4) && (NNR >= 1) && (NNR <= 4)
 void filter_impl(OutType &o, const InType &i, const cuda::std::array<FilterType, NR> h_rec,
                  const cuda::std::array<FilterType, NNR> h_nonrec, const cudaExecutor &exec) {
@@ -397,8 +412,8 @@ void filter_impl(OutType &o, const InType &i, const cuda::std::array<FilterType,
 // Replaces transforms/channelize_poly.h:724-849 (FIR + in-place cuFFT) with the fused kernel,
 // for the default accumulator (the output's inner type).
 template <typename OutType, typename InType, typename FilterType, typename AccumType>
-  requires gbfir_shim::routable_tensor<OutType> && gbfir_shim::routable_tensor<InType> &&
-           gbfir_shim::routable_tensor<FilterType> &&
+  requires gbfir_shim::routable_tensor<OutType> && gbfir_shim::routable_operand<InType> &&
+           gbfir_shim::routable_operand<FilterType> &&
            std::is_same_v<AccumType, typename inner_op_type_t<typename remove_cvref_t<OutType>::value_type>::type>
 inline void channelize_poly_impl(OutType out, const InType &in, const FilterType &f, index_t num_channels,
                                  index_t decimation_factor, cudaStream_t stream) {

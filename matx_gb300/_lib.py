@@ -49,7 +49,7 @@ class RaggedDesc(ctypes.Structure):
 
 class RaggedPlanInfo(ctypes.Structure):
     _fields_ = [("num_tiles", ctypes.c_int64), ("shared_bytes", ctypes.c_int64), ("table_bytes", ctypes.c_int64),
-                ("window_elems", ctypes.c_int64), ("buffers", ctypes.c_int64)]
+                ("window_elems", ctypes.c_int64), ("buffers", ctypes.c_int64), ("precision", ctypes.c_int64)]
 
 
 # (name, restype, argtypes) of every symbol include/gbfir.h declares
@@ -75,6 +75,7 @@ SIGNATURES = [
     ("gbfir_conv1d_bwd", ctypes.c_int, [_B, _B, _B, _B, _B, _i32, _p, _sz, _p]),
     ("gbfir_ragged_workspace_size", _sz, [_i64, _i64]),
     ("gbfir_ragged_plan", _i64, [_p, _i64, _p, _p]),
+    ("gbfir_ragged_plan_prec", _i64, [_p, _i64, _i32, _p, _p]),
     ("gbfir_ragged_tile_register", ctypes.c_int, [_i64, _i64, _i64, _i32, _i32, _i32]),
     ("gbfir_ragged_tile_clear", ctypes.c_int, []),
     ("gbfir_ragged_resample", ctypes.c_int, [_p, _i64, _p, _p, _i32, _p, _sz, _p]),

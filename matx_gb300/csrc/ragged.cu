@@ -275,6 +275,45 @@ static int64_t rg_shape_for(int64_t up, int64_t down, int64_t L) {
   return it == g_rg_tiles.end() ? 0 : it->second;
 }
 
+// Descriptor checks shared by the planners (host copies): 0 or a negative status.
+static int64_t rg_validate(const gbfir_ragged_desc *descs, int64_t count) {
+  for (int64_t s = 0; s < count; s++) {
+    const gbfir_ragged_desc &d = descs[s];
+    char buf[256];
+    if (!d.in || !d.out || !d.h) {
+      snprintf(buf, sizeof(buf), "ragged_plan: signal %lld has a null pointer", (long long)s);
+      set_error(buf);
+      return -GBFIR_ERR_NULL_POINTER;
+    }
+    if (d.in_len < 1 || d.h_len < 1 || d.up < 1 || d.down < 1) {
+      snprintf(buf, sizeof(buf), "ragged_plan: signal %lld has a non-positive length or rate", (long long)s);
+      set_error(buf);
+      return -GBFIR_ERR_INVALID_PARAMETER;
+    }
+    const int64_t up_size = d.in_len * d.up;
+    const int64_t olen = up_size / d.down + ((up_size % d.down) ? 1 : 0);
+    if (d.out_len != olen) {
+      snprintf(buf, sizeof(buf), "ragged_plan: signal %lld out_len %lld, expected %lld", (long long)s,
+               (long long)d.out_len, (long long)olen);
+      set_error(buf);
+      return -GBFIR_ERR_INVALID_DIM;
+    }
+    if ((reinterpret_cast<uintptr_t>(d.in) | reinterpret_cast<uintptr_t>(d.out)) % 8 ||
+        reinterpret_cast<uintptr_t>(d.h) % 4) {
+      snprintf(buf, sizeof(buf), "ragged_plan: signal %lld has a misaligned pointer", (long long)s);
+      set_error(buf);
+      return -GBFIR_ERR_ALIGNMENT;
+    }
+  }
+  return 0;
+}
+
+// tensor-core form (tc_blocks.cu)
+int64_t ragged_plan_tc(const gbfir_ragged_desc *descs, int64_t count, int precision, int64_t *table,
+                       int64_t *shared_bytes, int64_t *kchunk);
+int ragged_resample_tc(const gbfir_ragged_desc *device_descs, const int64_t *device_items, int64_t nitems,
+                       int64_t shared_bytes, int64_t kchunk, int precision, void *workspace, cudaStream_t s);
+
 }  // namespace gbfir
 
 using namespace gbfir;
@@ -317,6 +356,10 @@ int64_t gbfir_ragged_plan(const gbfir_ragged_desc *descs, int64_t count, int64_t
     set_error("ragged_plan: no descriptors");
     return -GBFIR_ERR_INVALID_PARAMETER;
   }
+  {
+    const int64_t rc = rg_validate(descs, count);
+    if (rc) return rc;
+  }
   struct Sig {
     RgGeom g;
     int64_t shape, ntiles;
@@ -327,31 +370,6 @@ int64_t gbfir_ragged_plan(const gbfir_ragged_desc *descs, int64_t count, int64_t
   double total = 0;
   for (int64_t s = 0; s < count; s++) {
     const gbfir_ragged_desc &d = descs[s];
-    char buf[256];
-    if (!d.in || !d.out || !d.h) {
-      snprintf(buf, sizeof(buf), "ragged_plan: signal %lld has a null pointer", (long long)s);
-      set_error(buf);
-      return -GBFIR_ERR_NULL_POINTER;
-    }
-    if (d.in_len < 1 || d.h_len < 1 || d.up < 1 || d.down < 1) {
-      snprintf(buf, sizeof(buf), "ragged_plan: signal %lld has a non-positive length or rate", (long long)s);
-      set_error(buf);
-      return -GBFIR_ERR_INVALID_PARAMETER;
-    }
-    const int64_t up_size = d.in_len * d.up;
-    const int64_t olen = up_size / d.down + ((up_size % d.down) ? 1 : 0);
-    if (d.out_len != olen) {
-      snprintf(buf, sizeof(buf), "ragged_plan: signal %lld out_len %lld, expected %lld", (long long)s,
-               (long long)d.out_len, (long long)olen);
-      set_error(buf);
-      return -GBFIR_ERR_INVALID_DIM;
-    }
-    if ((reinterpret_cast<uintptr_t>(d.in) | reinterpret_cast<uintptr_t>(d.out)) % 8 ||
-        reinterpret_cast<uintptr_t>(d.h) % 4) {
-      snprintf(buf, sizeof(buf), "ragged_plan: signal %lld has a misaligned pointer", (long long)s);
-      set_error(buf);
-      return -GBFIR_ERR_ALIGNMENT;
-    }
     Sig &sg = sigs[(size_t)s];
     sg.shape = rg_shape_for(d.up, d.down, d.h_len);
     sg.g = rg_geometry(d.up, d.down, d.h_len, d.out_len, sg.shape);
@@ -413,6 +431,34 @@ int64_t gbfir_ragged_plan(const gbfir_ragged_desc *descs, int64_t count, int64_t
     info->table_bytes = tb;
     info->window_elems = max_win;
     info->buffers = nbuf;
+    info->precision = GBFIR_PREC_FP32;
+  }
+  return nitems;
+}
+
+int64_t gbfir_ragged_plan_prec(const gbfir_ragged_desc *descs, int64_t count, int32_t precision,
+                               int64_t *tile_table, gbfir_ragged_plan_info *info) {
+  if (precision == GBFIR_PREC_FP32) return gbfir_ragged_plan(descs, count, tile_table, info);
+  if (precision < GBFIR_PREC_FP32 || precision > GBFIR_PREC_BF16X3) {
+    set_error("ragged_plan: unknown precision");
+    return -GBFIR_ERR_INVALID_PARAMETER;
+  }
+  if (descs == nullptr || count <= 0) {
+    set_error("ragged_plan: no descriptors");
+    return -GBFIR_ERR_INVALID_PARAMETER;
+  }
+  const int64_t rc = rg_validate(descs, count);
+  if (rc) return rc;
+  int64_t smem = 0, kchunk = 0;
+  const int64_t nitems = ragged_plan_tc(descs, count, precision, tile_table, &smem, &kchunk);
+  if (nitems < 0) return nitems;
+  if (info) {
+    info->num_tiles = nitems;
+    info->shared_bytes = smem;
+    info->table_bytes = 0;
+    info->window_elems = kchunk;  // the tensor-core plan's K chunk
+    info->buffers = 0;
+    info->precision = precision;
   }
   return nitems;
 }
@@ -423,11 +469,15 @@ int gbfir_ragged_resample(const gbfir_ragged_desc *device_descs, int64_t count, 
   if (!device_descs || !device_tile_table || !info || count <= 0 || info->num_tiles <= 0)
     GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "ragged_resample: empty plan");
   const int64_t nitems = info->num_tiles;
-  if (precision != GBFIR_PREC_FP32)
-    GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "ragged_resample: only the FP32 form is available");
+  if (precision != info->precision)
+    GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "ragged_resample: the plan was made for precision %lld, not %d",
+               (long long)info->precision, (int)precision);
   if (!workspace || workspace_bytes < gbfir_ragged_workspace_size(count, nitems))
     GBFIR_FAIL(GBFIR_ERR_WORKSPACE, "ragged_resample: workspace missing or too small");
   if (reinterpret_cast<uintptr_t>(workspace) % 8) GBFIR_FAIL(GBFIR_ERR_ALIGNMENT, "ragged_resample: workspace");
+  if (precision != GBFIR_PREC_FP32)
+    return ragged_resample_tc(device_descs, device_tile_table, nitems, info->shared_bytes, info->window_elems,
+                              precision, workspace, reinterpret_cast<cudaStream_t>(stream));
   const int64_t table_bytes = info->table_bytes;
   const int64_t smem = info->shared_bytes;
   const int64_t nbuf = info->buffers, win = info->window_elems;

@@ -70,6 +70,12 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst_smem, const void *src_gm
                : "memory");
 }
 
+// Bulk prefetch of `bytes` of global memory into L2 (16-byte aligned address, bytes a
+// multiple of 16); nothing waits for it.
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src_gmem, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src_gmem), "r"(bytes) : "memory");
+}
+
 // TMA tensor store shared -> global of one 3-D box (coordinates in elements, innermost
 // first; the innermost times the element size a multiple of 16 bytes, none negative),
 // tracked by the issuing thread's bulk groups.

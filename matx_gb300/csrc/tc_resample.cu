@@ -259,12 +259,65 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
     s_fail = 0;
     tc::mbar_fence_init();
   }
+  tc::tc_fence_before();
+  __syncthreads();  // the barriers are initialised
+  const XT *xp = reinterpret_cast<const XT *>(p.x);
+  const int ptid = tid - kProdWarp0 * 32;
+  const bool producer = warp >= kProdWarp0 && warp < kProdWarp0 + kProdWarps;
+  // An iteration's raw window (one contiguous run of P*LA samples of the signal from base)
+  // comes in with TMA bulk copies completing on raw_full[slot] when it lies inside the
+  // signal with a 16-byte aligned start; other windows (at the row ends) are staged with
+  // plain loads, zeros outside the signal.  Windows are staged nraw iterations ahead; the
+  // first ones are in flight while the tap matrices are built.
+  auto fetch = [&](int64_t itx, int slot) {
+    const int64_t b = itx / p.iters_per_row;
+    const int64_t q0 = (itx - b * p.iters_per_row) * (int64_t)(128 * p.MT);
+    const XT *row = xp + b * p.x_bstride;
+    const int64_t base = p.path == 0 ? p.rp * q0 + p.k0 : p.down * (p.rp * q0 + p.k0);
+    XT *dst = rawp(slot);
+    const size_t bytes = raw_elems * sizeof(XT);
+    const bool bulk = ((reinterpret_cast<uintptr_t>(row + base) | (uintptr_t)tc::smem_u32(dst)) & 15) == 0 &&
+                      base >= 0 && base + (int64_t)raw_elems <= p.N && bytes % 16 == 0 && bytes < (1u << 20);
+    if (bulk) {
+      // four bulk copies (16-byte multiples) from four lanes, so the pieces are in flight
+      // together; the transaction count is set before any of them is issued
+      if (ptid < 32) {
+        if (ptid == 0) {
+          tc::fence_async_smem();
+          tc::mbar_arrive_expect_tx(&raw_full[slot], (uint32_t)bytes);
+        }
+        __syncwarp();
+        const uint32_t piece = (uint32_t)(((bytes / 4) + 15) & ~(size_t)15);
+        const uint32_t off = (uint32_t)ptid * piece;
+        if (ptid < 4 && off < bytes) {
+          const uint32_t nb = (uint32_t)std::min<size_t>(piece, bytes - off);
+          tc::bulk_copy_g2s(reinterpret_cast<unsigned char *>(dst) + off,
+                            reinterpret_cast<const unsigned char *>(row + base) + off, nb, &raw_full[slot]);
+        }
+      }
+    } else {
+#pragma unroll 4
+      for (int v = ptid; v < (int)raw_elems; v += kNProd) {
+        const int64_t gi = base + v;
+        dst[v] = (gi >= 0 && gi < p.N) ? __ldg(row + gi) : zero_val<XT>();
+      }
+      named_sync(1, kNProd);
+      if (ptid == 0) tc::mbar_arrive_plain(&raw_full[slot]);
+    }
+  };
+  const int nraw = p.nraw;
+  const int64_t my_iters = p.niters > blockIdx.x ? (p.niters - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  if (producer) {
+    if (my_iters > 0) fetch(blockIdx.x, 0);
+    if (nraw == 2 && my_iters > 1) fetch(blockIdx.x + gridDim.x, 1);
+  }
   // The filter's taps, scaled and split into the operand terms once (hterm[t][e] = term t
-  // of scale * h[e], 16-bit), staged in the raw ring (not in use yet), so that the W build
-  // gathers 8 taps per 16-byte store instead of splitting every element.
+  // of scale * h[e], 16-bit), staged in the operand ring (not in use yet), so that the W
+  // build gathers 8 taps per 16-byte store instead of splitting every element.
   const int64_t Lh = p.Lo - p.even;
-  const bool h_staged = (size_t)Lh * 2 * p.terms <= (size_t)p.nraw * raw_elems * sizeof(XT);
-  uint16_t *hterm = reinterpret_cast<uint16_t *>(raw0);
+  const size_t scratch_bytes = (size_t)p.nbuf * NPARTS * p.terms * p.P * xarr;
+  const bool h_staged = (size_t)Lh * 2 * p.terms <= scratch_bytes;
+  uint16_t *hterm = reinterpret_cast<uint16_t *>(xbase);
   auto split_terms = [&](float v, uint16_t (&o)[3]) {
     if (p.fp16) {
       o[0] = __half_as_ushort(__float2half_rn(v));
@@ -310,8 +363,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
                                     : p.c + p.down * (int64_t)(p.Nt - 1) - p.up * p.down * p.k0;
   const int64_t zlen = tp_hi - tp_lo + 1;
   uint16_t *zline = hterm + (h_staged ? (size_t)p.terms * Lh : 0);
-  const bool z_staged = h_staged && zlen > 0 &&
-                        ((size_t)p.terms * Lh + (size_t)p.terms * zlen) * 2 <= (size_t)p.nraw * raw_elems * sizeof(XT);
+  const bool z_staged = h_staged && zlen > 0 && ((size_t)p.terms * Lh + (size_t)p.terms * zlen) * 2 <= scratch_bytes;
   if (z_staged) {
     for (int64_t i = tid; i < p.terms * zlen; i += kWsThreads) {
       const int t = (int)(i / zlen);
@@ -319,8 +371,12 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
     }
   }
   __syncthreads();
-  for (int it = tid; it < p.P * wrows * kch; it += kWsThreads) {
-    const int rr = it / kch, kc = it - rr * kch;
+  // items run row-fastest (consecutive lanes take consecutive rows of one K chunk, so their
+  // 16-byte stores fill whole 128-byte core matrices: conflict-free); a chunk whose tap range
+  // misses the filter is stored as zeros without gathers
+  const int nrows_w = p.P * wrows;
+  for (int it = tid; it < nrows_w * kch; it += kWsThreads) {
+    const int kc = it / nrows_w, rr = it - kc * nrows_w;
     const int pp = rr / wrows, row = rr - pp * wrows;
     const int t = row / p.Nmma, j = row - t * p.Nmma;
     uint32_t w[4] = {0u, 0u, 0u, 0u};
@@ -328,13 +384,16 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
       const int64_t kk = 8 * kc + p.k0;
       const int64_t tp0 = p.path == 0 ? p.c + (int64_t)j * p.down - kk * p.up
                                       : p.c + p.down * (int64_t)j - p.up * (pp + p.down * kk);
-      if (z_staged) {
-        const uint16_t *zt = zline + (size_t)t * zlen + (tp0 - tp_lo);
+      const int64_t tp7 = tp0 + 7 * dtp;  // dtp < 0: the chunk reads taps tp7..tp0
+      if (tp0 >= 0 && tp7 < p.Lo) {
+        if (z_staged) {
+          const uint16_t *zt = zline + (size_t)t * zlen + (tp0 - tp_lo);
 #pragma unroll
-        for (int e = 0; e < 8; e++) w[e >> 1] |= (uint32_t)zt[e * dtp] << (16 * (e & 1));
-      } else {
+          for (int e = 0; e < 8; e++) w[e >> 1] |= (uint32_t)zt[e * dtp] << (16 * (e & 1));
+        } else {
 #pragma unroll
-        for (int e = 0; e < 8; e++) w[e >> 1] |= w_term(t, tp0 + e * dtp) << (16 * (e & 1));
+          for (int e = 0; e < 8; e++) w[e >> 1] |= w_term(t, tp0 + e * dtp) << (16 * (e & 1));
+        }
       }
     }
     *reinterpret_cast<uint4 *>(warr(pp) + tc::kmajor_offset(row, 8 * kc, p.Kp)) = make_uint4(w[0], w[1], w[2], w[3]);
@@ -346,55 +405,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
   const uint32_t tmem = tmem_slot;
   if (tid == 0) GBFIR_TC_TRACE(3, 0, 0);
   const uint32_t set_cols = (uint32_t)(p.MT * NPARTS * p.acols);
-  const XT *xp = reinterpret_cast<const XT *>(p.x);
-  (void)xp;
 
-  if (warp >= kProdWarp0 && warp < kProdWarp0 + kProdWarps) {
+  if (producer) {
     // ================= producers =================
-    // An iteration's raw window (one contiguous run of P*LA samples of the signal from base)
-    // comes in with one TMA bulk copy completing on raw_full[slot] when it lies inside the
-    // signal with a 16-byte aligned start; other windows (at the row ends) are staged with
-    // plain loads, zeros outside the signal.  Windows are staged nraw iterations ahead.
-    const int ptid = tid - kProdWarp0 * 32;
-    auto fetch = [&](int64_t itx, int slot) {
-      const int64_t b = itx / p.iters_per_row;
-      const int64_t q0 = (itx - b * p.iters_per_row) * (int64_t)(128 * p.MT);
-      const XT *row = xp + b * p.x_bstride;
-      const int64_t base = p.path == 0 ? p.rp * q0 + p.k0 : p.down * (p.rp * q0 + p.k0);
-      XT *dst = rawp(slot);
-      const size_t bytes = raw_elems * sizeof(XT);
-      const bool bulk = ((reinterpret_cast<uintptr_t>(row + base) | (uintptr_t)tc::smem_u32(dst)) & 15) == 0 &&
-                        base >= 0 && base + (int64_t)raw_elems <= p.N && bytes % 16 == 0 && bytes < (1u << 20);
-      if (bulk) {
-        // four bulk copies (16-byte multiples) from four lanes, so the pieces are in flight
-        // together; the transaction count is set before any of them is issued
-        if (ptid < 32) {
-          if (ptid == 0) {
-            tc::fence_async_smem();
-            tc::mbar_arrive_expect_tx(&raw_full[slot], (uint32_t)bytes);
-          }
-          __syncwarp();
-          const uint32_t piece = (uint32_t)(((bytes / 4) + 15) & ~(size_t)15);
-          const uint32_t off = (uint32_t)ptid * piece;
-          if (ptid < 4 && off < bytes) {
-            const uint32_t nb = (uint32_t)std::min<size_t>(piece, bytes - off);
-            tc::bulk_copy_g2s(reinterpret_cast<unsigned char *>(dst) + off,
-                              reinterpret_cast<const unsigned char *>(row + base) + off, nb, &raw_full[slot]);
-          }
-        }
-      } else {
-        for (int v = ptid; v < (int)raw_elems; v += kNProd) {
-          const int64_t gi = base + v;
-          dst[v] = (gi >= 0 && gi < p.N) ? row[gi] : zero_val<XT>();
-        }
-        named_sync(1, kNProd);
-        if (ptid == 0) tc::mbar_arrive_plain(&raw_full[slot]);
-      }
-    };
-    const int nraw = p.nraw;
-    const int64_t my_iters = p.niters > blockIdx.x ? (p.niters - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-    if (my_iters > 0) fetch(blockIdx.x, 0);
-    if (nraw == 2 && my_iters > 1) fetch(blockIdx.x + gridDim.x, 1);
     const int nslots = p.nbuf;
     const uint32_t swz = p.rp == 64 ? 7u : 0u;
     const int half = p.LA / 2;
@@ -731,10 +744,11 @@ static TcPlan plan_tc(int64_t up, int64_t down, const TcTaps &taps, int64_t N_in
     return pl;
   }
   const int nparts = xc ? 2 : 1;
-  // bf16x3: rows of fewer than 64 columns concatenate the tap terms along N (3*N fits one
-  // MMA); wider rows issue six MMAs of N into one accumulator, so the epilogue reads one
-  // column block instead of three
-  p.concat = (p.terms == 3 && 3 * p.Nmma <= 256 && p.Nmma < 64) ? 1 : 0;
+  // bf16x3: the tap terms concatenated along N wherever 3*N fits one MMA (measured: three
+  // MMAs of N = 192/128/64 per K-step take half the time of six of N = 64, and the small
+  // terms accumulate apart from a0*b0: 1e-7 rel-L2 for a 301-tap conv where one accumulator
+  // over all six products gave 2e-6); wider rows issue six MMAs of N into one accumulator
+  p.concat = (p.terms == 3 && 3 * p.Nmma <= 256) ? 1 : 0;
   p.acols = p.concat ? 3 * p.Nmma : p.Nmma;
   const int wrows = p.terms * p.Nmma;
   const size_t xalign = rp == 64 ? 1024 : 128;

@@ -21,9 +21,13 @@ from . import resample_out_len, _prec, _stream
 
 
 class RaggedPlan:
-    def __init__(self, signals, outputs=None):
-        """signals: sequence of (x complex64 CUDA 1-D, h float32 CUDA 1-D, up, down)."""
+    def __init__(self, signals, outputs=None, precision="fp32"):
+        """signals: sequence of (x complex64 CUDA 1-D, h float32 CUDA 1-D, up, down).
+        ``precision`` selects the arithmetic of the tap contraction as for resample_poly:
+        "fp32" (row tiles on the CUDA cores) or a tensor-core form ("bf16", "fp16",
+        "bf16x3": column-blocked Toeplitz MMAs); the plan is made for that form."""
         lib = _lib.load()
+        self.precision = _prec(precision)
         n = len(signals)
         if n == 0:
             raise ValueError("RaggedPlan: no signals")
@@ -47,11 +51,12 @@ class RaggedPlan:
             descs[i] = _lib.RaggedDesc(x.data_ptr(), y.data_ptr(), h.data_ptr(), x.shape[0], olen, h.shape[0],
                                        int(up) // g, int(down) // g, 0)
         info = _lib.RaggedPlanInfo()
-        cnt = lib.gbfir_ragged_plan(descs, n, None, ctypes.byref(info))
+        cnt = lib.gbfir_ragged_plan_prec(descs, n, self.precision, None, ctypes.byref(info))
         if cnt < 0:
             _lib.check(-cnt)
         table = np.empty((cnt, 4), dtype=np.int64)
-        cnt2 = lib.gbfir_ragged_plan(descs, n, table.ctypes.data_as(ctypes.c_void_p), ctypes.byref(info))
+        cnt2 = lib.gbfir_ragged_plan_prec(descs, n, self.precision, table.ctypes.data_as(ctypes.c_void_p),
+                                          ctypes.byref(info))
         if cnt2 != cnt:
             _lib.check(5 if cnt2 >= 0 else -cnt2)
         dev = self.inputs[0].device
@@ -64,12 +69,11 @@ class RaggedPlan:
         self.workspace = torch.zeros(ws, dtype=torch.uint8, device=dev)
         self.num_tiles = int(cnt)
 
-    def run(self, precision="fp32"):
-        """One persistent launch over every signal; ``precision`` selects the arithmetic of
-        the tap contraction as for resample_poly."""
+    def run(self):
+        """One persistent launch over every signal, in the plan's arithmetic form."""
         lib = _lib.load()
         _lib.check(lib.gbfir_ragged_resample(
             ctypes.c_void_p(self.d_descs.data_ptr()), self.count, ctypes.c_void_p(self.d_tiles.data_ptr()),
-            ctypes.byref(self.info), _prec(precision), ctypes.c_void_p(self.workspace.data_ptr()),
+            ctypes.byref(self.info), self.precision, ctypes.c_void_p(self.workspace.data_ptr()),
             self.workspace.numel(), _stream()))
         return self.outputs

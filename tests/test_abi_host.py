@@ -230,8 +230,17 @@ def test_ragged_plan_validation(lib):
     assert lib.gbfir_ragged_tile_register(4, 5, 100, 3, 4, 2) == 1     # rows per thread 1 or 2
     assert lib.gbfir_ragged_tile_clear() == 0
     # launch refuses a plan that does not come from the planner (before touching the device)
-    bad = RaggedPlanInfo(n, 300 * 1024, 0, 1, 2)
+    bad = RaggedPlanInfo(n, 300 * 1024, 0, 1, 2, 0)
     assert lib.gbfir_ragged_resample(FAKE, 2, FAKE, ctypes.byref(bad), 0, FAKE, 256, None) == 1
+    # tensor-core plans: items carry each signal's packed block geometry; the launch refuses a
+    # plan made for another precision
+    n3 = lib.gbfir_ragged_plan_prec(d, 2, 3, None, ctypes.byref(info))
+    assert n3 > 0 and info.precision == 3 and info.window_elems in (32, 64)
+    t3 = np.empty((n3, 4), dtype=np.int64)
+    assert lib.gbfir_ragged_plan_prec(d, 2, 3, t3.ctypes.data_as(ctypes.c_void_p), ctypes.byref(info)) == n3
+    assert set(t3[:, 0].tolist()) == {0, 1} and (t3[:, 3] > 0).all()
+    assert lib.gbfir_ragged_resample(FAKE, 2, FAKE, ctypes.byref(info), 0, FAKE, 256, None) == 1
+    assert lib.gbfir_ragged_plan_prec(d, 2, 9, None, ctypes.byref(info)) == -1
 
 
 @pytest.mark.parametrize("updown", [(3, 2), (4, 5), (160, 147), (2, 1), (1, 7), (6, 4)])

@@ -28,3 +28,20 @@ def test_shim_routes_matx_operators(tmp_path):
     for name in ("gbfir_resample_poly", "gbfir_conv1d", "gbfir_channelize_poly", "gbfir_conv1d_axis",
                  "gbfir_filter", "gbfir_conv1d_fft", "gbfir_conv2d"):
         assert name in syms, f"{name} not referenced: MatX's operator did not route to the shim"
+
+
+@pytest.mark.skipif(MATX is None, reason="MatX headers not present")
+def test_shim_routes_expression_inputs(tmp_path):
+    """Operator expressions (conj(x), h * 2.f, img * 0.5f) as inputs route to the C-ABI too,
+    evaluated once into contiguous temporaries."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    obj = tmp_path / "expr.o"
+    cmd = [nvcc, "-std=c++20", "-O0", "--extended-lambda", "-gencode", "arch=compute_103a,code=sm_103a",
+           "-I", os.path.join(MATX, "include"), "-I", os.path.join(MATX, "include", "matx", "kernels"),
+           "-I", os.path.join(ROOT, "include"), "-c", os.path.join(ROOT, "tests", "shim", "matx_shim_expr.cu"),
+           "-o", str(obj)]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    syms = subprocess.run(["nm", "-u", str(obj)], capture_output=True, text=True).stdout
+    for name in ("gbfir_resample_poly", "gbfir_conv1d", "gbfir_channelize_poly", "gbfir_conv2d"):
+        assert name in syms, f"{name} not referenced: an expression input did not route to the shim"
