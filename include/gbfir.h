@@ -358,11 +358,14 @@ GBFIR_API int gbfir_ragged_resample(const gbfir_ragged_desc *device_descs, int64
 /* Override the tile shape the dispatcher picks for resample_poly (autotuner
  * hook; no MatX counterpart).  rows_per_thread in {1,2,4}, col_warps in
  * {1,2,4,8} (or 9..16 with one row per thread), group (outputs per row =
- * group*up) >= 1, buffers in {1,2} (2 = prefetch the next input window while
- * computing), plus 4 to write the outputs through shared memory and TMA tensor
- * stores (complex float signals with real taps, rows of 2, 4 or >= 8 even
- * outputs; other cases store directly).  Zero for a field keeps the built-in
- * heuristic for it.  Process-wide setting, not thread-safe. */
+ * group*up) >= 1, buffers in {1,2,3} (2 = prefetch the next input window while
+ * computing; 3 = the ring form for complex float signals with real taps: one CTA
+ * per SM, a staging warp keeping up to three windows in flight ahead of 16 compute
+ * warps, col_warps 1/2/4/8 giving 16/col_warps row slices; other signals take 2),
+ * plus 4 to write the outputs through shared memory and TMA tensor stores (complex
+ * float signals with real taps, rows of 2, 4 or >= 8 even outputs; other cases
+ * store directly).  Zero for a field keeps the built-in heuristic for it.
+ * Process-wide setting, not thread-safe. */
 GBFIR_API int gbfir_set_resample_tile(int32_t rows_per_thread, int32_t col_warps,
                             int32_t group, int32_t buffers);
 

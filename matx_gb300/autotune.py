@@ -59,7 +59,8 @@ def _key(x: torch.Tensor, h: torch.Tensor, up: int, down: int) -> str:
 
 def candidates(up: int, down: int, tma_store: bool = False):
     g = math.gcd(up, down)
-    nbufs = (1, 2, 5, 6) if tma_store else (1, 2)
+    # complex float signals with real taps: also the ring form (3) and the TMA-store epilogue (+4)
+    nbufs = (1, 2, 3, 5, 6, 7) if tma_store else (1, 2)
     u = up // g
     g0 = 4 // math.gcd(u, 4)
     # odd multiples too: they keep an odd row stride (TMA window copies) for odd down

@@ -551,6 +551,154 @@ __global__ void __launch_bounds__(RQ <= 2 ? 512 : 256)
   if (ostage.buf && lane == 0) tc::bulk_wait_all();
 }
 
+// cp.async completion on an mbarrier: the arrival fires once every cp.async this thread issued
+// before it has landed (.noinc: the barrier's expected count includes the arrival).
+__device__ __forceinline__ void cp_async_mbar_arrive(uint64_t *bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
+}
+
+constexpr int kRingMax = 4;       // window slots of the ring form
+constexpr int kRingThreads = 544; // one staging warp + up to 16 compute warps
+
+// Ring form of the row tile (complex float signal, real taps; one CTA per SM).  Warp 0
+// stages the windows of the CTA's tiles into a ring of p.nbuf (3 or 4) slots, up to
+// p.nbuf - 1 tiles ahead of the compute warps — one TMA bulk copy per window for an odd
+// row stride, cp.async into the conflict-free layout for an even one — and warps 1.. compute
+// as in the two-buffer form.  A full and an empty mbarrier per slot take the place of the
+// CTA-wide barriers, so a compute warp waits only when the copies fall behind and the next
+// windows are already in flight while a tile is computed.  Every wait is bounded; one that
+// gives up records the status read by rowtile_status_take() and ends the CTA's loop.
+template <int RQ, int PAD>
+__global__ void __launch_bounds__(kRingThreads, 1)
+    resample_rowtile_ring(const RsParams p, const __grid_constant__ CUtensorMap omap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ uint64_t full[kRingMax], empty[kRingMax];
+  __shared__ int s_fail;
+  unsigned char *table = smem_raw;
+  float2 *xbuf0 = reinterpret_cast<float2 *>(smem_raw + tap_table_bytes<float, true, false>(p.ncg, p.span));
+  const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+  const int ncw = (int)(blockDim.x >> 5) - 1;
+  const int R = p.nbuf;
+  const float2 *xp = reinterpret_cast<const float2 *>(p.x);
+  build_tap_table<float, true, false>(p, reinterpret_cast<const float *>(p.h), table, tid, blockDim.x);
+  if (tid == 0) {
+    for (int i = 0; i < R; i++) {
+      tc::mbar_init(&full[i], 32);   // the 32 lanes of the staging warp
+      tc::mbar_init(&empty[i], ncw); // lane 0 of every compute warp
+    }
+    s_fail = 0;
+    tc::mbar_fence_init();
+  }
+  __syncthreads();
+  // tile t: its batch row, first row, and (odd strides) the elements its window copy starts
+  // early so that the bulk copy is 16-byte aligned
+  auto origin = [&](int64_t t, int64_t &b, int64_t &q0, int64_t &w0) -> int {
+    b = t / p.tiles_per_row;
+    q0 = (t - b * p.tiles_per_row) * p.QC;
+    const int64_t xs0 = q0 * p.S + p.kmin;
+    int a = 0;
+    if constexpr (PAD == 0) a = (int)((reinterpret_cast<uintptr_t>(xp + b * p.x_bstride + xs0) & 15) / 8);
+    w0 = xs0 - a;
+    return a;
+  };
+
+  if (wid == 0) {
+    // ================= staging warp =================
+    int64_t n = 0;
+    for (int64_t tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++n) {
+      const int slot = (int)(n % R);
+      if (n >= R) {
+        int ok = 1;
+        if (lane == 0) ok = tc::mbar_wait(&empty[slot], (uint32_t)((n / R - 1) & 1)) ? 1 : 0;
+        if (!__shfl_sync(0xffffffffu, ok, 0)) {
+          if (lane == 0) s_fail = 1;
+          break;
+        }
+      }
+      float2 *buf = xbuf0 + (size_t)slot * p.win_alloc;
+      int64_t b, q0, w0;
+      const int a = origin(tile, b, q0, w0);
+      const float2 *row = xp + b * p.x_bstride;
+      if constexpr (PAD > 0) {
+        if (w0 >= 0 && w0 + p.win <= p.N) {
+          for (int e = lane; e < p.win; e += 32) cp_async_zfill<8>(&buf[smem_idx<PAD>(e)], row + w0 + e, true);
+        } else {
+          for (int e = lane; e < p.win; e += 32) {
+            const int64_t gi = w0 + e;
+            const bool ok = gi >= 0 && gi < p.N;
+            cp_async_zfill<8>(&buf[smem_idx<PAD>(e)], ok ? (const void *)(row + gi) : (const void *)row, ok);
+          }
+        }
+        cp_async_mbar_arrive(&full[slot]);
+      } else {
+        const int64_t wl = (p.win + a + 1) / 2 * 2;  // whole 16-byte units
+        const bool aligned = ((reinterpret_cast<uintptr_t>(row + w0) | (uintptr_t)tc::smem_u32(buf)) & 15) == 0;
+        if (aligned && w0 >= 0 && w0 + wl <= p.N) {
+          if (lane == 0) {
+            const uint32_t bytes = (uint32_t)(wl * 8);
+            tc::fence_async_smem();
+            tc::mbar_arrive_expect_tx(&full[slot], bytes);
+            tc::bulk_copy_g2s(buf, row + w0, bytes, &full[slot]);
+          } else {
+            tc::mbar_arrive_plain(&full[slot]);
+          }
+        } else {
+          for (int64_t e = lane; e < wl; e += 32) {
+            const int64_t gi = w0 + e;
+            buf[e] = (gi >= 0 && gi < p.N) ? row[gi] : make_float2(0.f, 0.f);
+          }
+          tc::mbar_arrive_plain(&full[slot]);  // each lane's stores are ordered before its arrival
+        }
+      }
+    }
+    if constexpr (PAD > 0) {
+      cp_async_commit();  // the copies were never grouped: group them, then wait for all
+      cp_async_wait<0>();
+    }
+  } else {
+    // ================= compute warps =================
+    const int cw = wid - 1;
+    const int wr = p.WC <= 8 ? cw / p.WC : 0, wc = p.WC <= 8 ? cw - wr * p.WC : cw;
+    const float scale = (float)p.scale;
+    OutStage ostage{&omap, nullptr, 0, 0};
+    if (p.ostore) {
+      unsigned char *base = smem_raw + p.stg_off;
+      base += (1024 - (tc::smem_u32(base) & 1023)) & 1023;
+      ostage.buf = base + cw * 4096;
+    }
+    int64_t n = 0;
+    for (int64_t tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++n) {
+      const int slot = (int)(n % R);
+      // every lane waits: its own acquire makes the window's bytes visible to it
+      const bool ok = tc::mbar_wait(&full[slot], (uint32_t)((n / R) & 1));
+      if (!__all_sync(0xffffffffu, ok)) {
+        if (lane == 0) s_fail = 1;
+        break;
+      }
+      int64_t b, q0, w0;
+      const int a = origin(tile, b, q0, w0);
+      ostage.b = b;
+      rowtile_compute_c2<RQ, PAD>(p, xbuf0 + (size_t)slot * p.win_alloc, table,
+                                  reinterpret_cast<float2 *>(p.out) + b * p.out_bstride, q0, wr, wc, lane, scale, a,
+                                  ostage);
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive_plain(&empty[slot]);
+    }
+    // the staged boxes are read before the CTA's shared memory goes away
+    if (ostage.buf && lane == 0) tc::bulk_wait_all();
+  }
+  __syncthreads();
+  if (s_fail && tid == 0) {
+    atomicExch(&g_rowtile_status, 1);
+    // copies a stopped loop left in flight: a bounded chance to land before the CTA ends
+    for (int i = 0; i < R; i++) {
+      (void)tc::mbar_wait(&full[i], 0);
+      (void)tc::mbar_wait(&full[i], 1);
+    }
+  }
+  __syncthreads();
+}
+
 // cuTensorMapEncodeTiled through the runtime's driver entry point (the library does not
 // link the driver, so it loads where no GPU driver is installed); null if unavailable.
 using TensorMapEncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -688,10 +836,44 @@ inline int dispatch_rq(RsParams &p, const CUtensorMap &m, int rq, int pad, size_
   return dispatch_rq_pad<T, XC, HC, 4>(p, m, rq, smem, s, threads);
 }
 
+template <int RQ, int PAD>
+inline int launch_ring(RsParams &p, const CUtensorMap &omap, size_t smem, cudaStream_t s, int threads) {
+  auto fn = resample_rowtile_ring<RQ, PAD>;
+  int rc = ensure_smem((const void *)fn, smem, "resample_poly");
+  if (rc) return rc;
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, smem);
+  if (occ < 1) GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "resample_poly: ring tile needs %zu B of shared memory", smem);
+  int64_t grid = (int64_t)num_sms() * occ;
+  if (grid > p.ntiles) grid = p.ntiles;
+  fn<<<(unsigned)grid, (unsigned)threads, smem, s>>>(p, omap);
+  return check_launch("resample_poly");
+}
+
+template <int PAD>
+inline int dispatch_ring_rq(RsParams &p, const CUtensorMap &m, int rq, size_t smem, cudaStream_t s, int threads) {
+  if (rq == 1) return launch_ring<1, PAD>(p, m, smem, s, threads);
+  return launch_ring<2, PAD>(p, m, smem, s, threads);
+}
+
+inline int dispatch_ring(RsParams &p, const CUtensorMap &m, int rq, int pad, size_t smem, cudaStream_t s,
+                         int threads) {
+  switch (pad) {
+    case 0: return dispatch_ring_rq<0>(p, m, rq, smem, s, threads);
+    case 11: return dispatch_ring_rq<11>(p, m, rq, smem, s, threads);
+    case 12: return dispatch_ring_rq<12>(p, m, rq, smem, s, threads);
+    case 13: return dispatch_ring_rq<13>(p, m, rq, smem, s, threads);
+    case 14: return dispatch_ring_rq<14>(p, m, rq, smem, s, threads);
+    case 15: return dispatch_ring_rq<15>(p, m, rq, smem, s, threads);
+    case 16: return dispatch_ring_rq<16>(p, m, rq, smem, s, threads);
+    default: return dispatch_ring_rq<17>(p, m, rq, smem, s, threads);
+  }
+}
+
 // Tile shape knobs: rq rows per thread (1, 2, 4), wc column warps (1..8), G row
 // grouping.  Zero picks the built-in heuristic.
 struct TileChoice {
-  int rq = 0, wc = 0, nbuf = 0;
+  int rq = 0, wc = 0, nbuf = 0;  // nbuf 3: the ring form (staging warp, 3-4 window slots)
   int ostore = -1;  // 1: TMA-store epilogue where the output layout allows it, 0: direct
                     // stores, -1: the epilogue for rows of 8 or more outputs
   int64_t group = 0;
@@ -700,8 +882,10 @@ struct TileChoice {
 // One resampling pass
 //   out[b][m] = scale * sum_k in[b][k] * hh(c + m*dn - k*upk)
 // (forward: dn = down, upk = up; adjoint: dn = up, upk = down, rev = 1).
-// Uses the row tile when it fits in shared memory, else the direct form.
-template <typename T, bool XC, bool HC>
+// Uses the row tile when it fits in shared memory, else the direct form.  RING: the caller
+// may ask for the ring form (complex float signals, real taps); other callers do not
+// instantiate it.
+template <typename T, bool XC, bool HC, bool RING = false>
 inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const void *h, int64_t L, void *out,
                          int64_t out_bstride, int64_t out_len, int64_t batch, int64_t upk, int64_t dn,
                          int64_t c_override, bool odd_extend, int rev, double scale, TileChoice tc, cudaStream_t s) {
@@ -718,10 +902,13 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
     while (wc < 8 && nsg % (wc * 2) == 0) wc *= 2;
   }
   if (wc > nsg || wc < 1 || wc > 16 || (wc <= 8 && 8 % wc != 0)) wc = 1;
+  constexpr bool kRingType = RING && std::is_same<T, float>::value && XC && !HC;
+  bool ring = kRingType && tc.nbuf == 3;
   // row slices per CTA: 8/wc for 1, 2, 4, 8 column warps, one slice (one row per thread)
-  // for 9..16, so the CTA has 8 warps or wc of them
-  const int wr = wc <= 8 ? 8 / wc : 1;
-  const int threads = 32 * wc * wr;
+  // for 9..16, so the CTA has 8 warps or wc of them; the ring form has 16 compute warps
+  // (16/wc slices) or wc, plus its staging warp
+  int wr = wc <= 8 ? (ring ? 16 : 8) / wc : 1;
+  int threads = 32 * wc * wr + (ring ? 32 : 0);
   // even row strides need a conflict-free window layout: the XOR permutation for ctz(S)
   // (complex float signals with real taps), one pad per 16 elements otherwise
   int pad = (geo.S % 2) ? 0 : 4;
@@ -743,7 +930,7 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
   const bool ostore = (tc.ostore == 1 || (tc.ostore < 0 && geo.Nt >= 8)) && std::is_same<T, float>::value && XC && !HC && geo.Nt % 2 == 0 &&
                       ost_rb > 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0 &&
                       (batch == 1 || out_bstride % 2 == 0) && rows_full >= 1;
-  const size_t stg_bytes = ostore ? 1024 + (size_t)(threads / 32) * 4096 : 0;
+  size_t stg_bytes = ostore ? 1024 + (size_t)(threads / 32 - (ring ? 1 : 0)) * 4096 : 0;
   auto smem_for = [&](int rq, int nbuf) -> size_t {
     const int64_t QC = 32LL * rq * wr;
     const int64_t win = (QC - 1) * geo.S + (geo.kmax - geo.kmin) + 1;
@@ -751,14 +938,39 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
     return tap_table_bytes<T, XC, HC>(geo.ncg, geo.span) + (size_t)nbuf * (size_t)alloc * sizeof(XT) + stg_bytes;
   };
   int rq = tc.rq > 0 ? tc.rq : 2;
-  if (sizeof(T) == 8) rq = 1;
-  else if (threads > 256 && rq > 2) rq = 2;  // CTAs of 9-16 column warps: 1 or 2 rows per thread
   int nbuf = tc.nbuf > 0 ? tc.nbuf : 2;
-  // two CTAs per SM: prefer double buffering, then fewer rows, then a single buffer
-  while (smem_for(rq, nbuf) > 110 * 1024 && (rq > 1 || nbuf > 1)) {
-    if (nbuf == 2 && rq == 1) nbuf = 1;
-    else if (rq > 1) rq /= 2;
-    else nbuf = 1;
+  if (ring) {
+    // one CTA per SM of 17 warps (120 registers a thread: one or two rows per thread); four
+    // window slots, else three, else fewer rows per thread; the two-buffer form where even
+    // one row per thread does not fit
+    if (rq > 2) rq = 2;
+    nbuf = 4;
+    while (smem_for(rq, nbuf) > 225 * 1024 && (nbuf > 3 || rq > 1)) {
+      if (nbuf == 4) nbuf = 3;
+      else {
+        rq /= 2;
+        nbuf = 4;
+      }
+    }
+    if (smem_for(rq, nbuf) > 225 * 1024) {
+      ring = false;
+      wr = wc <= 8 ? 8 / wc : 1;
+      threads = 32 * wc * wr;
+      stg_bytes = ostore ? 1024 + (size_t)(threads / 32) * 4096 : 0;
+      rq = tc.rq > 0 ? tc.rq : 2;
+      nbuf = 2;
+    }
+  }
+  if (!ring) {
+    if (nbuf > 2) nbuf = 2;
+    if (sizeof(T) == 8) rq = 1;
+    else if (threads > 256 && rq > 2) rq = 2;  // CTAs of 9-16 column warps: 1 or 2 rows per thread
+    // two CTAs per SM: prefer double buffering, then fewer rows, then a single buffer
+    while (smem_for(rq, nbuf) > 110 * 1024 && (rq > 1 || nbuf > 1)) {
+      if (nbuf == 2 && rq == 1) nbuf = 1;
+      else if (rq > 1) rq /= 2;
+      else nbuf = 1;
+    }
   }
   const size_t smem = smem_for(rq, nbuf);
 
@@ -778,7 +990,7 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
   p.scale = scale;
   p.rev = rev;
   p.nbuf = nbuf;
-  if (smem <= 200 * 1024) {
+  if (smem <= (ring ? 225 : 200) * 1024) {
     p.Nt = geo.Nt;
     p.S = geo.S;
     p.ncg = geo.ncg;
@@ -813,6 +1025,9 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
         p.rows_full = rows_full;
         p.stg_off = (int32_t)(smem - stg_bytes);
       }
+    }
+    if constexpr (kRingType) {
+      if (ring) return dispatch_ring(p, omap, rq, pad, smem, s, threads);
     }
     return dispatch_rq<T, XC, HC>(p, omap, rq, pad, smem, s, threads);
   }

@@ -21,7 +21,8 @@
 //
 // Pipeline (persistent, warp-specialised, 384 threads): a stage is (tile of rows, column
 // block, K chunk).  Warps 1-7 materialise A into a 2-slot ring; warp 0 lane 0 issues the MMAs
-// into one of two TMEM accumulator sets (one per (tile, block)); warps 8-11 drain a set
+// into one of two TMEM accumulator sets (one per (tile, block); bf16x3: a leading and a
+// correction accumulator per set, summed in FP32 on the way out); warps 8-11 drain a set
 // through a padded shared staging tile and store whole (complex) outputs, a warp per row at a
 // time, coalesced.  The ragged launch takes work items (runs of tiles of one signal) from an
 // atomic counter; between items every role is idle, the CTA rebuilds W for the item's signal
@@ -135,8 +136,15 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_blocks_kernel(const TbParams
   const int sstride = p.NBmax + 4;
   float *stage = reinterpret_cast<float *>(abase + (size_t)2 * p.terms * abytes);
 
-  // two accumulator sets of NBmax columns, rounded up to a power of two >= 32
-  const uint32_t tcols = 2 * p.NBmax <= 32 ? 32u : 2 * p.NBmax <= 64 ? 64u : 2 * p.NBmax <= 128 ? 128u : 256u;
+  // two accumulator sets of acc_cols columns, rounded up to a power of two >= 32.  bf16x3
+  // keeps the leading product a0*b0 alone in the first NBmax columns of a set and the five
+  // smaller ones in the next NBmax.  Every MMA instruction loses about one FP32 rounding of
+  // its accumulator (six products a K-step into one accumulator measured 1.7e-6 rel-L2 at 475
+  // taps), so the big sum takes one loss per K-step instead of six and the correction sum's
+  // losses are 2^-8 smaller.
+  const int acc_cols = p.terms == 3 ? 2 * p.NBmax : p.NBmax;
+  const uint32_t tcols = 2 * acc_cols <= 32 ? 32u : 2 * acc_cols <= 64 ? 64u : 2 * acc_cols <= 128 ? 128u
+                         : 2 * acc_cols <= 256 ? 256u : 512u;
   if (warp == 0) tc::tmem_alloc(&tmem_slot, tcols);
   if (tid == 0) {
     for (int i = 0; i < 2; i++) {
@@ -404,15 +412,20 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_blocks_kernel(const TbParams
           }
           GBFIR_TC_TRACE(1, (int)k, 1);
           tc::tc_fence_after();
-          const uint32_t d = tmem + (uint32_t)(set * p.NBmax);
+          const uint32_t d = tmem + (uint32_t)(set * acc_cols);
           const int nks = min(Kc, g.Kb - Kc * kcn) / 16;
           for (int pr = 0; pr < npairs; pr++) {
             const int tx = p.terms == 3 ? (int)((kTx >> (4 * pr)) & 15u) : 0;
             const int tw = p.terms == 3 ? (int)((kTw >> (4 * pr)) & 15u) : 0;
+            // bf16x3: (0,0), the last pair, into the leading accumulator; the rest, first of them
+            // pair 0, into the correction accumulator NBmax columns on
+            const bool lead = pr == npairs - 1;
+            const uint32_t dd = d + (p.terms == 3 && !lead ? (uint32_t)p.NBmax : 0u);
+            const bool first_pair = lead || pr == 0;
             uint64_t ad = tc::smem_desc(tc::smem_u32(amat(slot, tx)), 128u, asbo);
             uint64_t bd = tc::smem_desc(tc::smem_u32(wmat(b, tw)) + (uint32_t)(kcn * (Kc / 8) * 128), 128u, wsbo);
             for (int ks = 0; ks < nks; ks++) {
-              tc::mma_f16(d, ad, bd, idesc, (kcn > 0 || pr > 0 || ks > 0) ? 1u : 0u);
+              tc::mma_f16(dd, ad, bd, idesc, (kcn > 0 || !first_pair || ks > 0) ? 1u : 0u);
               ad += 16;  // +256 B: two core matrices along K
               bd += 16;
             }
@@ -447,9 +460,14 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_blocks_kernel(const TbParams
         tc::tc_fence_after();
         float *srow_p = stage + (size_t)srow * sstride;
         for (int col = 0; col < g.NB; col += 16) {
-          uint32_t r[16];
-          tc::tmem_ld16(tmem + lane_base + (uint32_t)(set * p.NBmax + col), r);
+          uint32_t r[16], rc[16];
+          tc::tmem_ld16(tmem + lane_base + (uint32_t)(set * acc_cols + col), r);
+          if (p.terms == 3) tc::tmem_ld16(tmem + lane_base + (uint32_t)(set * acc_cols + p.NBmax + col), rc);
           tc::tmem_ld_wait();
+          if (p.terms == 3) {
+#pragma unroll
+            for (int q = 0; q < 16; q++) r[q] = __float_as_uint(__uint_as_float(r[q]) + __uint_as_float(rc[q]));
+          }
 #pragma unroll
           for (int q = 0; q < 16; q += 4)
             *reinterpret_cast<float4 *>(srow_p + col + q) =

@@ -28,7 +28,9 @@
 // so one K-step is three MMAs — a0*[b0|b1|b2] into D[0:3N), a1*[b0|b1] into D[N:3N), a2*b0
 // into D[2N:3N) — and the epilogue sums the three column blocks: exactly the six products
 // of order <= 2, with the small terms accumulated apart from a0*b0.  Wider rows issue the
-// six products as six MMAs of N columns into one accumulator.
+// six products as six MMAs of N columns: into one accumulator for bands of up to 8 K-steps,
+// else a0*b0 into one and the five smaller products into a second (every MMA instruction
+// costs the accumulator about one FP32 rounding, so long bands keep the big sum's count low).
 //
 // Pipeline (persistent, warp-specialised CTA; roles below).  A stage covers MT M-tiles
 // of 128 rows; raw input is staged two stages ahead with cp.async, converted into a
@@ -69,8 +71,11 @@ struct TcParams {
   int32_t nsets;    // TMEM accumulator sets (1 or 2)
   int32_t nraw;     // raw staging slots: 2 = stage two iterations ahead, 1 = one ahead
   int32_t rp;       // Hankel row pitch in samples: 8 (no swizzle) or 64 (128-byte swizzle)
-  int32_t concat;   // bf16x3: 1 = tap terms concatenated along N, 0 = six MMAs into one
-  int32_t acols;    // TMEM accumulator columns per (M-tile, part): 3*Nmma (concat) or Nmma
+  int32_t concat;   // bf16x3: 1 = tap terms concatenated along N, 0 = six MMAs of N columns
+  int32_t split;    // bf16x3 without concat: 1 = a0*b0 and the five smaller products in two
+                    // accumulators (long K bands), 0 = all six in one
+  int32_t acols;    // TMEM accumulator columns per (M-tile, part): 3*Nmma (concat), 2*Nmma
+                    // (split) or Nmma
 };
 
 // Bounded-wait status of the tensor-core kernels (1 = a wait gave up); read and
@@ -172,8 +177,10 @@ __device__ __forceinline__ void tcr_drain_half(const TcParams &p, uint32_t tb,
           for (int i = 0; i < 4; i++) {
             const int r = 4 * grp + i;
             if constexpr (BLK == 3)
-              v[i] = (__uint_as_float(rb[g][part][0][r]) + __uint_as_float(rb[g][part][1][r])) +
-                     __uint_as_float(rb[g][part][2][r]);
+              v[i] = __uint_as_float(rb[g][part][0][r]) +
+                     (__uint_as_float(rb[g][part][1][r]) + __uint_as_float(rb[g][part][2][r]));
+            else if constexpr (BLK == 2)
+              v[i] = __uint_as_float(rb[g][part][0][r]) + __uint_as_float(rb[g][part][1][r]);
             else
               v[i] = __uint_as_float(rb[g][part][0][r]);
           }
@@ -203,7 +210,9 @@ __device__ __forceinline__ void tcr_drain_half(const TcParams &p, uint32_t tb,
 #pragma unroll
       for (int i = 0; i < 4; i++) {
         if constexpr (BLK == 3)
-          v[i] = (__uint_as_float(r[part][0][i]) + __uint_as_float(r[part][1][i])) + __uint_as_float(r[part][2][i]);
+          v[i] = __uint_as_float(r[part][0][i]) + (__uint_as_float(r[part][1][i]) + __uint_as_float(r[part][2][i]));
+        else if constexpr (BLK == 2)
+          v[i] = __uint_as_float(r[part][0][i]) + __uint_as_float(r[part][1][i]);
         else
           v[i] = __uint_as_float(r[part][0][i]);
       }
@@ -587,8 +596,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
             }
           }
         } else if (p.terms == 3) {
-          // six MMAs of N columns into one accumulator per K-step, products of order <= 2
-          // (signal term tx, tap term tw), smallest first: (1,1) (2,0) (0,2) (1,0) (0,1) (0,0)
+          // six MMAs of N columns per K-step, products of order <= 2 (signal term tx, tap
+          // term tw), smallest first: (1,1) (2,0) (0,2) (1,0) (0,1) (0,0); split: the last,
+          // a0*b0, into the first N columns and the other five into the next N
           constexpr uint32_t kTx = 0x001021u, kTw = 0x010201u;
           for (int a = 0; a < nacc; a++) {
             const uint32_t d = dset + (uint32_t)(a * p.acols);
@@ -598,7 +608,10 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
                 for (int pr = 0; pr < 6; pr++) {
                   const int tx = (int)((kTx >> (4 * pr)) & 15u), tw = (int)((kTw >> (4 * pr)) & 15u);
                   const uint64_t bd = bd0 + (uint64_t)tw * term_step + (uint64_t)(16 * ks);
-                  tc::mma_f16(d, a_desc(a, tx, pp, ks), bd, idesc1, (pp > 0 || ks > 0 || pr > 0) ? 1u : 0u);
+                  const bool small = p.split && pr < 5;
+                  const bool first = p.split ? (pr == 0 || pr == 5) : pr == 0;
+                  tc::mma_f16(d + (small ? (uint32_t)p.Nmma : 0u), a_desc(a, tx, pp, ks), bd, idesc1,
+                              (pp > 0 || ks > 0 || !first) ? 1u : 0u);
                 }
               }
             }
@@ -638,12 +651,13 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
       const int64_t b = it / p.iters_per_row;
       const int64_t q0 = (it - b * p.iters_per_row) * (int64_t)(128 * p.MT);
       XT *orow = reinterpret_cast<XT *>(p.out) + b * p.out_bstride;
-      const bool blocks3 = p.terms == 3 && p.concat;
+      const bool blocks3 = p.terms == 3 && p.concat, blocks2 = p.terms == 3 && p.split;
       for (int m = 0; m < p.MT; m++) {
         for (int half = 0; half < 2; half++) {
           const int64_t qa = q0 + 128 * m + 32 * quarter + 16 * half + (lane >> 2);
           const uint32_t tb = dset + ((uint32_t)(32 * quarter + 16 * half) << 16) + (uint32_t)(m * NPARTS * p.acols);
           if (blocks3) tcr_drain_half<XC, 3>(p, tb, orow, qa, lane);
+          else if (blocks2) tcr_drain_half<XC, 2>(p, tb, orow, qa, lane);
           else tcr_drain_half<XC, 1>(p, tb, orow, qa, lane);
         }
       }
@@ -747,9 +761,11 @@ static TcPlan plan_tc(int64_t up, int64_t down, const TcTaps &taps, int64_t N_in
   // bf16x3: the tap terms concatenated along N wherever 3*N fits one MMA (measured: three
   // MMAs of N = 192/128/64 per K-step take half the time of six of N = 64, and the small
   // terms accumulate apart from a0*b0: 1e-7 rel-L2 for a 301-tap conv where one accumulator
-  // over all six products gave 2e-6); wider rows issue six MMAs of N into one accumulator
+  // over all six products gave 2e-6); wider rows issue six MMAs of N per K-step, into two
+  // accumulators (a0*b0 apart from the rest) where the band is longer than 8 K-steps
   p.concat = (p.terms == 3 && 3 * p.Nmma <= 256) ? 1 : 0;
-  p.acols = p.concat ? 3 * p.Nmma : p.Nmma;
+  p.split = (p.terms == 3 && !p.concat && p.P * (p.Kp / 16) > 8) ? 1 : 0;
+  p.acols = p.concat ? 3 * p.Nmma : p.split ? 2 * p.Nmma : p.Nmma;
   const int wrows = p.terms * p.Nmma;
   const size_t xalign = rp == 64 ? 1024 : 128;
   auto smem_for = [&](int MT, int nraw, int nslots) -> size_t {

@@ -284,6 +284,42 @@ def test_resample_tma_store_epilogue(mx, orc, case):
     assert rel_l2(host(y_tma), orc.resample_poly(x, h, up, down)) < FP32_TOL, case
 
 
+@pytest.mark.parametrize("case", [
+    # (up, down, batch, N, (rows per thread, column warps, group)): even row strides (cp.async
+    # into the XOR layout), odd ones (bulk copies), windows past the signal ends, partial
+    # last rows and tiles, and many tiles per CTA so that the ring wraps many times
+    (3, 2, 2, 20001, (2, 2, 8)), (3, 2, 3, 20000, (1, 1, 4)), (4, 5, 1, 20003, (2, 2, 3)),
+    (4, 5, 2, 20000, (1, 1, 1)), (160, 147, 2, 20011, (1, 10, 1)), (160, 147, 1, 20000, (2, 16, 1)),
+    (1, 2, 2, 9999, (2, 2, 2)), (2, 1, 3, 7777, (1, 4, 0)), (3, 2, 64, 1 << 18, (1, 1, 2)),
+    (4, 5, 64, 1 << 18, (2, 1, 1)),
+])
+def test_resample_ring_form(mx, orc, case):
+    """Buffers = 3 is the ring form (a staging warp, 3-4 window slots, mbarriers instead of
+    CTA barriers): the same arithmetic as the two-buffer form, so bit for bit the same
+    outputs, with direct and with TMA-store epilogues; rows checked against the oracle."""
+    import torch
+    up, down, B, N, (rq, wc, g) = case
+    rng = np.random.default_rng(seed_of("ring", *case[:4]))
+    x = (rng.standard_normal((B, N)) + 1j * rng.standard_normal((B, N))).astype(np.complex64)
+    h = kaiser_filter(up, down).astype(np.float32)
+    xd, hd = dev(x), dev(h)
+    try:
+        mx.set_resample_tile(rq, wc, g, 2)
+        y2 = mx.resample_poly(xd, hd, up, down)
+        mx.set_resample_tile(rq, wc, g, 3)
+        y3 = mx.resample_poly(xd, hd, up, down)
+        mx.set_resample_tile(rq, wc, g, 7)
+        y7 = mx.resample_poly(xd, hd, up, down)
+        torch.cuda.synchronize()
+        assert mx._lib.load().gbfir_tc_status() == 0
+    finally:
+        mx.set_resample_tile(0, 0, 0, 0)
+    assert torch.equal(y3, y2), case
+    assert torch.equal(y7, y2), case
+    rows = [0, B - 1] if B > 1 else [0]
+    assert rel_l2(host(y3[rows]), orc.resample_poly(x[rows], h, up, down, nthreads=2)) < FP32_TOL, case
+
+
 @pytest.mark.parametrize("updown", [(3, 2), (4, 5), (160, 147)])
 def test_resample_config_rows(mx, orc, updown):
     # C2 at full size: 64 x 2^20 complex Gaussian; sampled rows against the oracle,

@@ -61,7 +61,7 @@ def test_tc_resample_vs_fp64(mx, orc, updown, form, cplx):
     assert rel_l2(y, r) < TOL[form], (updown, form, rel_l2(y, r))
 
 
-@pytest.mark.parametrize("L", [30, 31, 2, 1, 301])
+@pytest.mark.parametrize("L", [30, 31, 2, 1, 301, 401, 801])
 def test_tc_resample_filter_lengths(mx, orc, L):
     import torch
     rng = np.random.default_rng(L)
