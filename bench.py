@@ -990,13 +990,14 @@ def main():
             tile = tuple(int(v) for v in t.split(","))
             autotune.register(u, d, len(taps_np[RATIOS.index((u, d))]), tile)
             tiles[r] = {"rows_per_thread": tile[0], "col_warps": tile[1], "group": tile[2], "buffers": tile[3] & 3,
-                        "tma_store": bool(tile[3] & 4), "fixed": True}
+                        "tma_store": bool(tile[3] & 4), "paired": bool(tile[3] & 8), "fixed": True}
     elif not args.no_tune and prec == "fp32":
         from matx_gb300 import autotune
         for (u, d), h, o in zip(RATIOS, taps, outs):
             r = autotune.tune_resample(x, h, u, d, out=o, use_cache=False)
             tiles[f"{u}/{d}"] = {"rows_per_thread": r.best[0], "col_warps": r.best[1], "group": r.best[2],
-                                 "buffers": r.best[3] & 3, "tma_store": bool(r.best[3] & 4), "ms": r.best_ms,
+                                 "buffers": r.best[3] & 3, "tma_store": bool(r.best[3] & 4),
+                                 "paired": bool(r.best[3] & 8), "ms": r.best_ms,
                                  "heuristic_ms": r.default_ms}
 
     for _ in range(args.warmup):

@@ -59,8 +59,14 @@ def _key(x: torch.Tensor, h: torch.Tensor, up: int, down: int) -> str:
 
 def candidates(up: int, down: int, tma_store: bool = False):
     g = math.gcd(up, down)
-    # complex float signals with real taps: also the ring form (3) and the TMA-store epilogue (+4)
-    nbufs = (1, 2, 3, 5, 6, 7) if tma_store else (1, 2)
+    # complex float signals with real taps: also the ring form (3), the TMA-store epilogue (+4)
+    # and, where the row stride down*group is even, the paired walk (+8)
+    base = (1, 2, 3, 5, 6, 7) if tma_store else (1, 2)
+
+    def nbufs_for(grp):
+        if tma_store and ((down // g) * grp) % 2 == 0:
+            return base + (9, 10, 11, 13, 14, 15)
+        return base
     u = up // g
     g0 = 4 // math.gcd(u, 4)
     # odd multiples too: they keep an odd row stride (TMA window copies) for odd down
@@ -71,7 +77,7 @@ def candidates(up: int, down: int, tma_store: bool = False):
                 nsg = (u * grp + 7) // 8
                 if wc > max(1, nsg):
                     continue
-                for nb in nbufs:
+                for nb in nbufs_for(grp):
                     yield (rq, wc, grp, nb)
     # one row slice of 9..16 column warps that divide the super-groups evenly (one or two
     # rows per thread): balanced warps where 1, 2, 4 or 8 leave some with an extra super-group
@@ -80,7 +86,7 @@ def candidates(up: int, down: int, tma_store: bool = False):
         for wc in range(9, 17):
             if nsg % wc == 0:
                 for rq in (1, 2):
-                    for nb in nbufs:
+                    for nb in nbufs_for(grp):
                         yield (rq, wc, grp, nb)
 
 

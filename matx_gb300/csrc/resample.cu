@@ -34,9 +34,9 @@ static bool valid_tile(int rq, int wc, int group, int nbuf) {
   // column warps: 1, 2, 4, 8 (8/wc row slices per CTA) or 9..16 (one row slice, rows per thread 1 or 2)
   // buffers: 1 or 2 window buffers (0 = heuristic) or 3 = the ring form (a staging warp and
   // 3-4 window slots; complex float signals with real taps, else 2), plus 4 for the
-  // TMA-store epilogue
+  // TMA-store epilogue, plus 8 for the ring form's paired walk (even row strides)
   return (rq == 0 || rq == 1 || rq == 2 || rq == 4) && (wc >= 0 && wc <= 16 && (wc <= 8 ? 8 % (wc ? wc : 1) == 0 : rq <= 2)) &&
-         group >= 0 && group <= 64 && (nbuf & ~7) == 0;
+         group >= 0 && group <= 64 && (nbuf & ~15) == 0;
 }
 
 // Identity (up == down after the gcd): out = in, with real->complex widening.
@@ -77,8 +77,10 @@ static int run_resample(const gbfir_buf &out, const gbfir_buf &in, const gbfir_b
   if (g_wc_override) tc.wc = g_wc_override;
   if (g_group_override) tc.group = g_group_override;
   if (g_nbuf_override) tc.nbuf = g_nbuf_override;
-  // buffers + 4 asks for the TMA-store epilogue; an explicit 1 or 2 without it, direct stores
+  // buffers + 4 asks for the TMA-store epilogue (an explicit 1, 2 or 3 without it: direct
+  // stores), + 8 the ring form's paired walk
   tc.ostore = (tc.nbuf & 4) ? 1 : tc.nbuf ? 0 : -1;
+  tc.pair = (tc.nbuf & 8) != 0;
   tc.nbuf &= 3;
   return resample_pass<T, XC, HC, true>(in.ptr, in.batch_stride, in.len, h.ptr, h.len, out.ptr, out.batch_stride, out.len,
                                   out.batch, up, down, -1, true, 0, (double)up, tc, s);

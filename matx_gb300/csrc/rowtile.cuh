@@ -28,6 +28,14 @@
 
 namespace gbfir {
 
+// Timing hooks of the ring form's roles (role, stage, event); they compile to nothing unless
+// a tracing build defines them.
+#ifndef GBFIR_TC_TRACE
+#define GBFIR_TC_TRACE(role, stage, event) \
+  do {                                     \
+  } while (0)
+#endif
+
 // Bounded-wait status of the row-tile kernels of this translation unit (1 = a window copy
 // did not complete within the spin limit); read and cleared through rowtile_status_take().
 static __device__ int32_t g_rowtile_status;
@@ -63,6 +71,7 @@ struct RsParams {
   int32_t ost_rb;    // bytes of one row of a stored box (16, 32 or 64)
   int32_t stg_off;   // byte offset of the store staging area in dynamic shared memory
   int64_t rows_full; // rows holding Nt outputs (the tensor map's row count)
+  int32_t pair;      // 1: bands start at even k and rows read two samples per 16-byte load
 };
 
 // Output staging of one warp for the TMA-store epilogue: two buffers of 32 rows x ost_rb
@@ -117,6 +126,14 @@ __device__ __forceinline__ int smem_idx(int p) {
   }
 }
 
+// First k that column group g (phases 4g..4g+3) reads.  In the paired form it is rounded
+// down to even (at most one leading zero tap), so every row's reads start on a 16-byte pair
+// of complex samples when the row stride is even.
+__host__ __device__ inline int64_t band_start(int64_t c, int64_t g, int64_t down, int64_t Lo, int64_t up, bool pair) {
+  const int64_t k = ceil_div(c + 4 * g * down - Lo + 1, up);
+  return pair ? floor_div(k, 2) * 2 : k;
+}
+
 // table[g*span + kk] holds the 4 taps he[c + (4g+jj)*down - (kl0(g)+kk)*up] (reversed when
 // rev, 0 outside); goff[g] = kl0(g) - kmin is where band g starts in the tile window.
 template <typename T, bool XC, bool HC>
@@ -132,7 +149,7 @@ __device__ __forceinline__ void build_tap_table(const RsParams &p, const typenam
     const int rem = e - g * (p.span * 4);
     const int kk = rem >> 2, jj = rem & 3;
     const int64_t j = 4 * (int64_t)g + jj;
-    const int64_t kl0 = ceil_div(p.c + 4 * (int64_t)g * p.down - p.Lo + 1, p.up);
+    const int64_t kl0 = band_start(p.c, g, p.down, p.Lo, p.up, p.pair != 0);
     const int64_t tp = p.c + j * p.down - (kl0 + kk) * p.up;
     HT v = zero_val<HT>();
     if (j < p.Nt && tp >= 0 && tp < p.Lo) {
@@ -142,7 +159,7 @@ __device__ __forceinline__ void build_tap_table(const RsParams &p, const typenam
     table[g * p.span + kk].v[jj] = v;
   }
   for (int g = tid; g < p.ncg; g += nthreads)
-    goff[g] = (int)(ceil_div(p.c + 4 * (int64_t)g * p.down - p.Lo + 1, p.up) - p.kmin);
+    goff[g] = (int)(band_start(p.c, g, p.down, p.Lo, p.up, p.pair != 0) - p.kmin);
 }
 
 __device__ __forceinline__ const int *tap_goff(const RsParams &p, const unsigned char *table_raw, size_t entry) {
@@ -153,6 +170,64 @@ __device__ __forceinline__ const int *tap_goff(const RsParams &p, const unsigned
 // fma / mul, so the values equal two scalar fmaf / __fmul_rn calls.
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+
+// The 8 phases of super-group sg for a thread's RQ rows, scaled, to the output: through the
+// warp's staging buffer and a TMA tensor store when os.buf is set, else direct stores (four
+// 16-byte stores per whole, aligned row).
+template <int RQ>
+__device__ __forceinline__ void c2_store_rows(const RsParams &p, const float2 (&acc)[RQ][8], int sg, int64_t q0,
+                                              int rbase, int lane, float2 sc, float2 *orow, OutStage &os) {
+  const int Nt = (int)p.Nt;
+  const int j0 = 8 * sg;
+  const int ncol = min(8, Nt - j0);
+#pragma unroll
+  for (int i = 0; i < RQ; i++) {
+    const int64_t n0 = (q0 + rbase + 32 * i) * p.Nt + j0;
+    const int64_t left = p.out_len - n0;
+    const int nv = left < ncol ? (left > 0 ? (int)left : 0) : ncol;
+    float2 *dst = orow + n0;
+    if (os.buf) {
+      // stage the warp's 32 rows x 8 phases (swizzled like the tensor map: 16-byte chunk
+      // u of row r at chunk u ^ f(r), conflict-free), then one lane stores the box; rows
+      // past rows_full are clipped by the map and the one partial row is stored here
+      unsigned char *buf = os.buf + (os.n & 1) * 2048;
+      if (lane == 0 && os.n >= 2) tc::bulk_wait_read<1>();
+      __syncwarp();
+      const int rb = p.ost_rb;
+      const int sw = rb == 64 ? ((lane >> 1) & 3) : rb == 32 ? ((lane >> 2) & 1) : 0;
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        if (u * 16 < rb) {
+          const float2 lo = mul2(acc[i][2 * u], sc), hi = mul2(acc[i][2 * u + 1], sc);
+          *reinterpret_cast<float4 *>(buf + lane * rb + ((u ^ sw) << 4)) = make_float4(lo.x, lo.y, hi.x, hi.y);
+        }
+      }
+      tc::fence_async_smem();
+      __syncwarp();
+      if (lane == 0) {
+        tc::tma_store_3d(os.map, buf, 2 * j0, (int)(q0 + rbase - lane + 32 * i), (int)os.b);
+        tc::bulk_commit();
+      }
+      os.n++;
+      if (q0 + rbase + 32 * i == p.rows_full) {
+#pragma unroll
+        for (int jj = 0; jj < 8; jj++)
+          if (jj < nv) dst[jj] = mul2(acc[i][jj], sc);
+      }
+    } else if (nv == 8 && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0)) {
+      float4 *d4 = reinterpret_cast<float4 *>(dst);
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const float2 lo = mul2(acc[i][2 * u], sc), hi = mul2(acc[i][2 * u + 1], sc);
+        d4[u] = make_float4(lo.x, lo.y, hi.x, hi.y);
+      }
+    } else {
+#pragma unroll
+      for (int jj = 0; jj < 8; jj++)
+        if (jj < nv) dst[jj] = mul2(acc[i][jj], sc);
+    }
+  }
+}
 
 // Complex float signal x real float taps, the hot case: the same three-range walk as the
 // generic form below with (re, im) accumulated by one f32x2 FMA per sample and phase
@@ -233,55 +308,128 @@ __device__ __forceinline__ void rowtile_compute_c2(const RsParams &p, const floa
         }
       }
     }
-    const int j0 = 8 * sg;
-    const int ncol = min(8, Nt - j0);
+    c2_store_rows<RQ>(p, acc, sg, q0, rbase, lane, sc, orow, os);
+  }
+}
+
+// Paired form of the window (even row strides): 16-byte units of two complex samples.  PAD =
+// 20 is the plain layout (S/2 odd: the 8 lanes of a quarter-warp, which share one 128-byte
+// wavefront of 16-byte loads, hit 8 different units mod 8); PAD = 20 + t, t = ctz(S/2) (1..7),
+// XORs the low min(t, 3) bits of the unit index with the bits from max(t, 3) up, a
+// permutation inside each block of 8 units that is conflict-free for those strides.
+template <int PAD>
+__device__ __forceinline__ int unit_idx(int u) {
+  if constexpr (PAD > 20) {
+    constexpr int t = PAD - 20, sh = t > 3 ? t : 3, m = (1 << (t < 3 ? t : 3)) - 1;
+    return u ^ ((u >> sh) & m);
+  } else {
+    return u;
+  }
+}
+
+// cp.async of one 16-byte unit reading `src_bytes` (0, 8 or 16) of it, zeros for the rest.
+__device__ __forceinline__ void cp_async16_part(void *smem_dst, const void *gmem_src, int src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(tc::smem_u32(smem_dst)), "l"(gmem_src),
+               "r"(src_bytes)
+               : "memory");
+}
+
+// The paired walk of rowtile_compute_c2: every band starts at an even k and the row stride is
+// even, so each row reads samples k and k+1 with one 16-byte load and the loop runs two k a
+// step — half the window loads and index arithmetic for the same f32x2 FMAs, in the same
+// order (a leading zero tap adds +-0).  The window is addressed in units of two samples.
+template <int RQ, int PAD>
+__device__ __forceinline__ void rowtile_compute_c2pair(const RsParams &p, const float2 *cur,
+                                                       const unsigned char *table_raw, float2 *orow, int64_t q0,
+                                                       int wr, int wc, int lane, float scale, OutStage &os) {
+  using TV = TapVec<float, false>;
+  const TV *table = reinterpret_cast<const TV *>(table_raw);
+  const int *goff = tap_goff(p, table_raw, sizeof(TV));
+  const float4 *cu = reinterpret_cast<const float4 *>(cur);
+  const int nsg = (p.ncg + 1) / 2;
+  const int rbase = wr * 32 * RQ + lane;
+  const float2 sc = make_float2(scale, scale);
+  const int S2 = (int)(p.S >> 1);
+  for (int sg = wc; sg < nsg; sg += p.WC) {
+    const int gA = 2 * sg, gB = 2 * sg + 1;
+    const bool hasB = gB < p.ncg;
+    const int oA = goff[gA];               // even
+    const int d = hasB ? goff[gB] - oA : 0;  // even
+    int ub[RQ];                            // unit of each row's band start
 #pragma unroll
-    for (int i = 0; i < RQ; i++) {
-      const int64_t n0 = (q0 + rbase + 32 * i) * p.Nt + j0;
-      const int64_t left = p.out_len - n0;
-      const int nv = left < ncol ? (left > 0 ? (int)left : 0) : ncol;
-      float2 *dst = orow + n0;
-      if (os.buf) {
-        // stage the warp's 32 rows x 8 phases (swizzled like the tensor map: 16-byte chunk
-        // u of row r at chunk u ^ f(r), conflict-free), then one lane stores the box; rows
-        // past rows_full are clipped by the map and the one partial row is stored here
-        unsigned char *buf = os.buf + (os.n & 1) * 2048;
-        if (lane == 0 && os.n >= 2) tc::bulk_wait_read<1>();
-        __syncwarp();
-        const int rb = p.ost_rb;
-        const int sw = rb == 64 ? ((lane >> 1) & 3) : rb == 32 ? ((lane >> 2) & 1) : 0;
+    for (int i = 0; i < RQ; i++) ub[i] = (rbase + 32 * i) * S2 + (oA >> 1);
+    float2 acc[RQ][8];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-          if (u * 16 < rb) {
-            const float2 lo = mul2(acc[i][2 * u], sc), hi = mul2(acc[i][2 * u + 1], sc);
-            *reinterpret_cast<float4 *>(buf + lane * rb + ((u ^ sw) << 4)) = make_float4(lo.x, lo.y, hi.x, hi.y);
-          }
-        }
-        tc::fence_async_smem();
-        __syncwarp();
-        if (lane == 0) {
-          tc::tma_store_3d(os.map, buf, 2 * j0, (int)(q0 + rbase - lane + 32 * i), (int)os.b);
-          tc::bulk_commit();
-        }
-        os.n++;
-        if (q0 + rbase + 32 * i == p.rows_full) {
+    for (int i = 0; i < RQ; i++)
 #pragma unroll
-          for (int jj = 0; jj < 8; jj++)
-            if (jj < nv) dst[jj] = mul2(acc[i][jj], sc);
-        }
-      } else if (nv == 8 && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0)) {
-        float4 *d4 = reinterpret_cast<float4 *>(dst);
+      for (int jj = 0; jj < 8; jj++) acc[i][jj] = make_float2(0.f, 0.f);
+    const TV *tA = table + gA * p.span;
+    const TV *tB = table + (hasB ? gB : gA) * p.span;
+    const int e1 = hasB ? min(d, p.span) : p.span;  // even: span and d are
+    for (int kk = 0; kk < e1; kk += 2) {
+      const float4 a = *reinterpret_cast<const float4 *>(tA[kk].v);
+      const float4 a2 = *reinterpret_cast<const float4 *>(tA[kk + 1].v);
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-          const float2 lo = mul2(acc[i][2 * u], sc), hi = mul2(acc[i][2 * u + 1], sc);
-          d4[u] = make_float4(lo.x, lo.y, hi.x, hi.y);
-        }
-      } else {
-#pragma unroll
-        for (int jj = 0; jj < 8; jj++)
-          if (jj < nv) dst[jj] = mul2(acc[i][jj], sc);
+      for (int i = 0; i < RQ; i++) {
+        const float4 xv = cu[unit_idx<PAD>(ub[i] + (kk >> 1))];
+        const float2 x0 = make_float2(xv.x, xv.y), x1 = make_float2(xv.z, xv.w);
+        acc[i][0] = fma2(x0, make_float2(a.x, a.x), acc[i][0]);
+        acc[i][1] = fma2(x0, make_float2(a.y, a.y), acc[i][1]);
+        acc[i][2] = fma2(x0, make_float2(a.z, a.z), acc[i][2]);
+        acc[i][3] = fma2(x0, make_float2(a.w, a.w), acc[i][3]);
+        acc[i][0] = fma2(x1, make_float2(a2.x, a2.x), acc[i][0]);
+        acc[i][1] = fma2(x1, make_float2(a2.y, a2.y), acc[i][1]);
+        acc[i][2] = fma2(x1, make_float2(a2.z, a2.z), acc[i][2]);
+        acc[i][3] = fma2(x1, make_float2(a2.w, a2.w), acc[i][3]);
       }
     }
+    if (hasB) {
+      for (int kk = d; kk < p.span; kk += 2) {
+        const float4 a = *reinterpret_cast<const float4 *>(tA[kk].v);
+        const float4 a2 = *reinterpret_cast<const float4 *>(tA[kk + 1].v);
+        const float4 b = *reinterpret_cast<const float4 *>(tB[kk - d].v);
+        const float4 b2 = *reinterpret_cast<const float4 *>(tB[kk - d + 1].v);
+#pragma unroll
+        for (int i = 0; i < RQ; i++) {
+          const float4 xv = cu[unit_idx<PAD>(ub[i] + (kk >> 1))];
+          const float2 x0 = make_float2(xv.x, xv.y), x1 = make_float2(xv.z, xv.w);
+          acc[i][0] = fma2(x0, make_float2(a.x, a.x), acc[i][0]);
+          acc[i][1] = fma2(x0, make_float2(a.y, a.y), acc[i][1]);
+          acc[i][2] = fma2(x0, make_float2(a.z, a.z), acc[i][2]);
+          acc[i][3] = fma2(x0, make_float2(a.w, a.w), acc[i][3]);
+          acc[i][4] = fma2(x0, make_float2(b.x, b.x), acc[i][4]);
+          acc[i][5] = fma2(x0, make_float2(b.y, b.y), acc[i][5]);
+          acc[i][6] = fma2(x0, make_float2(b.z, b.z), acc[i][6]);
+          acc[i][7] = fma2(x0, make_float2(b.w, b.w), acc[i][7]);
+          acc[i][0] = fma2(x1, make_float2(a2.x, a2.x), acc[i][0]);
+          acc[i][1] = fma2(x1, make_float2(a2.y, a2.y), acc[i][1]);
+          acc[i][2] = fma2(x1, make_float2(a2.z, a2.z), acc[i][2]);
+          acc[i][3] = fma2(x1, make_float2(a2.w, a2.w), acc[i][3]);
+          acc[i][4] = fma2(x1, make_float2(b2.x, b2.x), acc[i][4]);
+          acc[i][5] = fma2(x1, make_float2(b2.y, b2.y), acc[i][5]);
+          acc[i][6] = fma2(x1, make_float2(b2.z, b2.z), acc[i][6]);
+          acc[i][7] = fma2(x1, make_float2(b2.w, b2.w), acc[i][7]);
+        }
+      }
+      for (int kk = max(p.span, d); kk < d + p.span; kk += 2) {
+        const float4 b = *reinterpret_cast<const float4 *>(tB[kk - d].v);
+        const float4 b2 = *reinterpret_cast<const float4 *>(tB[kk - d + 1].v);
+#pragma unroll
+        for (int i = 0; i < RQ; i++) {
+          const float4 xv = cu[unit_idx<PAD>(ub[i] + (kk >> 1))];
+          const float2 x0 = make_float2(xv.x, xv.y), x1 = make_float2(xv.z, xv.w);
+          acc[i][4] = fma2(x0, make_float2(b.x, b.x), acc[i][4]);
+          acc[i][5] = fma2(x0, make_float2(b.y, b.y), acc[i][5]);
+          acc[i][6] = fma2(x0, make_float2(b.z, b.z), acc[i][6]);
+          acc[i][7] = fma2(x0, make_float2(b.w, b.w), acc[i][7]);
+          acc[i][4] = fma2(x1, make_float2(b2.x, b2.x), acc[i][4]);
+          acc[i][5] = fma2(x1, make_float2(b2.y, b2.y), acc[i][5]);
+          acc[i][6] = fma2(x1, make_float2(b2.z, b2.z), acc[i][6]);
+          acc[i][7] = fma2(x1, make_float2(b2.w, b2.w), acc[i][7]);
+        }
+      }
+    }
+    c2_store_rows<RQ>(p, acc, sg, q0, rbase, lane, sc, orow, os);
   }
 }
 
@@ -295,7 +443,10 @@ __device__ __forceinline__ void rowtile_compute(const RsParams &p, const typenam
                                                 typename val_of<T, XC || HC>::type *orow, int64_t q0, int wr, int wc,
                                                 int lane, T scale, int woff, OutStage &os) {
   if constexpr (std::is_same<T, float>::value && XC && !HC) {
-    rowtile_compute_c2<RQ, PAD>(p, cur, table_raw, orow, q0, wr, wc, lane, scale, woff, os);
+    if constexpr (PAD >= 20)
+      rowtile_compute_c2pair<RQ, PAD>(p, cur, table_raw, orow, q0, wr, wc, lane, scale, os);
+    else
+      rowtile_compute_c2<RQ, PAD>(p, cur, table_raw, orow, q0, wr, wc, lane, scale, woff, os);
   } else {
     using XT = typename val_of<T, XC>::type;
     constexpr bool OC = XC || HC;
@@ -419,16 +570,26 @@ __global__ void __launch_bounds__(RQ <= 2 ? 512 : 256)
     }
   }
 
-  if constexpr (PAD > 0) {
+  if constexpr (PAD > 0 && PAD != 20) {
     // Even row stride: the window is stored in a bank-conflict-free layout (an element
-    // permutation inside blocks of 16, or one pad per 16), which a bulk copy cannot
-    // produce; stage it with cp.async (zero-filled outside the signal).
+    // permutation inside blocks of 16, a unit permutation of the paired walk, or one pad per
+    // 16), which a bulk copy cannot produce; stage it with cp.async (zero-filled outside the
+    // signal).
     auto issue_loads = [&](int64_t tile, XT *buf) {
       const int64_t b = tile / p.tiles_per_row;
       const int64_t q0 = (tile - b * p.tiles_per_row) * p.QC;
       const int64_t xs0 = q0 * p.S + p.kmin;
       const XT *row = xp + b * p.x_bstride;
-      if (xs0 >= 0 && xs0 + p.win <= p.N) {
+      if constexpr (PAD > 20) {
+        // units of two samples (xs0 is even); the last may hold one sample of the signal
+        float4 *bu = reinterpret_cast<float4 *>(buf);
+        const int nu = (p.win + 1) >> 1;
+        for (int u = tid; u < nu; u += blockDim.x) {
+          const int64_t gi = xs0 + 2 * u;
+          const int nb = (gi >= 0 && gi < p.N) ? (gi + 1 < p.N ? 16 : 8) : 0;
+          cp_async16_part(&bu[unit_idx<PAD>(u)], nb ? (const void *)(row + gi) : (const void *)row, nb);
+        }
+      } else if (xs0 >= 0 && xs0 + p.win <= p.N) {
         const XT *src = row + xs0;
         for (int e = tid; e < p.win; e += blockDim.x) cp_async_zfill<sizeof(XT)>(&buf[smem_idx<PAD>(e)], src + e, true);
       } else {
@@ -557,14 +718,16 @@ __device__ __forceinline__ void cp_async_mbar_arrive(uint64_t *bar) {
   asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
 }
 
+
 constexpr int kRingMax = 4;       // window slots of the ring form
 constexpr int kRingThreads = 544; // one staging warp + up to 16 compute warps
 
 // Ring form of the row tile (complex float signal, real taps; one CTA per SM).  Warp 0
 // stages the windows of the CTA's tiles into a ring of p.nbuf (3 or 4) slots, up to
 // p.nbuf - 1 tiles ahead of the compute warps — one TMA bulk copy per window for an odd
-// row stride, cp.async into the conflict-free layout for an even one — and warps 1.. compute
-// as in the two-buffer form.  A full and an empty mbarrier per slot take the place of the
+// row stride or the plain paired layout (PAD 0, 20), cp.async into the conflict-free
+// layouts otherwise (per sample for PAD 11..17, per 16-byte unit for PAD 21..27) — and warps
+// 1.. compute as in the two-buffer form (PAD >= 20: the paired walk).  A full and an empty mbarrier per slot take the place of the
 // CTA-wide barriers, so a compute warp waits only when the copies fall behind and the next
 // windows are already in flight while a tile is computed.  Every wait is bounded; one that
 // gives up records the status read by rowtile_status_take() and ends the CTA's loop.
@@ -580,6 +743,7 @@ __global__ void __launch_bounds__(kRingThreads, 1)
   const int ncw = (int)(blockDim.x >> 5) - 1;
   const int R = p.nbuf;
   const float2 *xp = reinterpret_cast<const float2 *>(p.x);
+  if (tid == 0) GBFIR_TC_TRACE(3, 0, 1);
   build_tap_table<float, true, false>(p, reinterpret_cast<const float *>(p.h), table, tid, blockDim.x);
   if (tid == 0) {
     for (int i = 0; i < R; i++) {
@@ -602,11 +766,13 @@ __global__ void __launch_bounds__(kRingThreads, 1)
     return a;
   };
 
+  if (tid == 0) GBFIR_TC_TRACE(3, 0, 0);
   if (wid == 0) {
     // ================= staging warp =================
     int64_t n = 0;
     for (int64_t tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++n) {
       const int slot = (int)(n % R);
+      if (lane == 0) GBFIR_TC_TRACE(0, (int)n, 0);
       if (n >= R) {
         int ok = 1;
         if (lane == 0) ok = tc::mbar_wait(&empty[slot], (uint32_t)((n / R - 1) & 1)) ? 1 : 0;
@@ -619,7 +785,21 @@ __global__ void __launch_bounds__(kRingThreads, 1)
       int64_t b, q0, w0;
       const int a = origin(tile, b, q0, w0);
       const float2 *row = xp + b * p.x_bstride;
-      if constexpr (PAD > 0) {
+      if constexpr (PAD > 20) {
+        // units of two samples (w0 is even); the last may hold one sample of the signal
+        float4 *bu = reinterpret_cast<float4 *>(buf);
+        const int nu = (p.win + 1) >> 1;
+        if (w0 >= 0 && w0 + 2 * (int64_t)nu <= p.N) {
+          for (int u = lane; u < nu; u += 32) cp_async16_part(&bu[unit_idx<PAD>(u)], row + w0 + 2 * u, 16);
+        } else {
+          for (int u = lane; u < nu; u += 32) {
+            const int64_t gi = w0 + 2 * u;
+            const int nb = (gi >= 0 && gi < p.N) ? (gi + 1 < p.N ? 16 : 8) : 0;
+            cp_async16_part(&bu[unit_idx<PAD>(u)], nb ? (const void *)(row + gi) : (const void *)row, nb);
+          }
+        }
+        cp_async_mbar_arrive(&full[slot]);
+      } else if constexpr (PAD > 0 && PAD != 20) {
         if (w0 >= 0 && w0 + p.win <= p.N) {
           for (int e = lane; e < p.win; e += 32) cp_async_zfill<8>(&buf[smem_idx<PAD>(e)], row + w0 + e, true);
         } else {
@@ -650,8 +830,9 @@ __global__ void __launch_bounds__(kRingThreads, 1)
           tc::mbar_arrive_plain(&full[slot]);  // each lane's stores are ordered before its arrival
         }
       }
+      if (lane == 0) GBFIR_TC_TRACE(0, (int)n, 1);
     }
-    if constexpr (PAD > 0) {
+    if constexpr (PAD != 0 && PAD != 20) {
       cp_async_commit();  // the copies were never grouped: group them, then wait for all
       cp_async_wait<0>();
     }
@@ -669,20 +850,29 @@ __global__ void __launch_bounds__(kRingThreads, 1)
     int64_t n = 0;
     for (int64_t tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++n) {
       const int slot = (int)(n % R);
+      const int trole = cw == 0 ? 1 : cw == ncw - 1 ? 2 : -1;
+      if (lane == 0 && trole > 0) GBFIR_TC_TRACE(trole, (int)n, 0);
       // every lane waits: its own acquire makes the window's bytes visible to it
       const bool ok = tc::mbar_wait(&full[slot], (uint32_t)((n / R) & 1));
       if (!__all_sync(0xffffffffu, ok)) {
         if (lane == 0) s_fail = 1;
         break;
       }
+      if (lane == 0 && trole > 0) GBFIR_TC_TRACE(trole, (int)n, 1);
       int64_t b, q0, w0;
       const int a = origin(tile, b, q0, w0);
       ostage.b = b;
-      rowtile_compute_c2<RQ, PAD>(p, xbuf0 + (size_t)slot * p.win_alloc, table,
-                                  reinterpret_cast<float2 *>(p.out) + b * p.out_bstride, q0, wr, wc, lane, scale, a,
-                                  ostage);
+      if constexpr (PAD >= 20)
+        rowtile_compute_c2pair<RQ, PAD>(p, xbuf0 + (size_t)slot * p.win_alloc, table,
+                                        reinterpret_cast<float2 *>(p.out) + b * p.out_bstride, q0, wr, wc, lane, scale,
+                                        ostage);
+      else
+        rowtile_compute_c2<RQ, PAD>(p, xbuf0 + (size_t)slot * p.win_alloc, table,
+                                    reinterpret_cast<float2 *>(p.out) + b * p.out_bstride, q0, wr, wc, lane, scale, a,
+                                    ostage);
       __syncwarp();
       if (lane == 0) tc::mbar_arrive_plain(&empty[slot]);
+      if (lane == 0 && trole > 0) GBFIR_TC_TRACE(trole, (int)n, 2);
     }
     // the staged boxes are read before the CTA's shared memory goes away
     if (ostage.buf && lane == 0) tc::bulk_wait_all();
@@ -724,7 +914,7 @@ struct RsGeom {
 };
 
 inline RsGeom plan_geometry(int64_t up, int64_t down, int64_t L, int64_t out_len, int64_t G, int64_t c_override = -1,
-                            bool odd_extend = true) {
+                            bool odd_extend = true, bool pair = false) {
   RsGeom g{};
   g.up = up;
   g.down = down;
@@ -738,14 +928,14 @@ inline RsGeom plan_geometry(int64_t up, int64_t down, int64_t L, int64_t out_len
   for (int64_t grp = 0; grp < g.ncg; grp++) {
     const int64_t j0 = 4 * grp;
     const int64_t jl = std::min<int64_t>(j0 + 3, g.Nt - 1);
-    const int64_t kl0 = ceil_div(g.c + j0 * down - g.Lo + 1, up);
+    const int64_t kl0 = band_start(g.c, grp, down, g.Lo, up, pair);
     const int64_t kh = floor_div(g.c + jl * down, up);
     span = std::max<int64_t>(span, kh - kl0 + 1);
   }
   span = (span + 1) & ~1LL;  // even, for the 2x unrolled band loop
   g.span = (int32_t)span;
-  g.kmin = ceil_div(g.c - g.Lo + 1, up);
-  g.kmax = ceil_div(g.c + 4 * (int64_t)(g.ncg - 1) * down - g.Lo + 1, up) + span - 1;
+  g.kmin = band_start(g.c, 0, down, g.Lo, up, pair);
+  g.kmax = band_start(g.c, g.ncg - 1, down, g.Lo, up, pair) + span - 1;
   g.rows = (out_len + g.Nt - 1) / g.Nt;
   return g;
 }
@@ -866,7 +1056,37 @@ inline int dispatch_ring(RsParams &p, const CUtensorMap &m, int rq, int pad, siz
     case 14: return dispatch_ring_rq<14>(p, m, rq, smem, s, threads);
     case 15: return dispatch_ring_rq<15>(p, m, rq, smem, s, threads);
     case 16: return dispatch_ring_rq<16>(p, m, rq, smem, s, threads);
-    default: return dispatch_ring_rq<17>(p, m, rq, smem, s, threads);
+    case 17: return dispatch_ring_rq<17>(p, m, rq, smem, s, threads);
+    case 20: return dispatch_ring_rq<20>(p, m, rq, smem, s, threads);
+    case 21: return dispatch_ring_rq<21>(p, m, rq, smem, s, threads);
+    case 22: return dispatch_ring_rq<22>(p, m, rq, smem, s, threads);
+    case 23: return dispatch_ring_rq<23>(p, m, rq, smem, s, threads);
+    case 24: return dispatch_ring_rq<24>(p, m, rq, smem, s, threads);
+    case 25: return dispatch_ring_rq<25>(p, m, rq, smem, s, threads);
+    case 26: return dispatch_ring_rq<26>(p, m, rq, smem, s, threads);
+    default: return dispatch_ring_rq<27>(p, m, rq, smem, s, threads);
+  }
+}
+
+// The two-buffer form's paired walk (complex float signal, real taps): pad 20..27.
+template <int PAD>
+inline int dispatch_pair_rq(RsParams &p, const CUtensorMap &m, int rq, size_t smem, cudaStream_t s, int threads) {
+  if (rq == 1) return launch_rowtile<float, true, false, 1, PAD>(p, m, smem, s, threads);
+  if (rq == 2) return launch_rowtile<float, true, false, 2, PAD>(p, m, smem, s, threads);
+  return launch_rowtile<float, true, false, 4, PAD>(p, m, smem, s, threads);
+}
+
+inline int dispatch_pair(RsParams &p, const CUtensorMap &m, int rq, int pad, size_t smem, cudaStream_t s,
+                         int threads) {
+  switch (pad) {
+    case 20: return dispatch_pair_rq<20>(p, m, rq, smem, s, threads);
+    case 21: return dispatch_pair_rq<21>(p, m, rq, smem, s, threads);
+    case 22: return dispatch_pair_rq<22>(p, m, rq, smem, s, threads);
+    case 23: return dispatch_pair_rq<23>(p, m, rq, smem, s, threads);
+    case 24: return dispatch_pair_rq<24>(p, m, rq, smem, s, threads);
+    case 25: return dispatch_pair_rq<25>(p, m, rq, smem, s, threads);
+    case 26: return dispatch_pair_rq<26>(p, m, rq, smem, s, threads);
+    default: return dispatch_pair_rq<27>(p, m, rq, smem, s, threads);
   }
 }
 
@@ -876,6 +1096,7 @@ struct TileChoice {
   int rq = 0, wc = 0, nbuf = 0;  // nbuf 3: the ring form (staging warp, 3-4 window slots)
   int ostore = -1;  // 1: TMA-store epilogue where the output layout allows it, 0: direct
                     // stores, -1: the epilogue for rows of 8 or more outputs
+  bool pair = false;  // the paired walk where the row stride is even
   int64_t group = 0;
 };
 
@@ -909,14 +1130,27 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
   // (16/wc slices) or wc, plus its staging warp
   int wr = wc <= 8 ? (ring ? 16 : 8) / wc : 1;
   int threads = 32 * wc * wr + (ring ? 32 : 0);
+  // the paired walk: an even row stride and 16-byte aligned signal rows; its bands start at
+  // even k
+  int t2 = 0;
+  while (t2 < 8 && (((geo.S >> 1) >> t2) & 1) == 0) t2++;
+  const bool pair = kRingType && tc.pair && geo.S % 2 == 0 && t2 <= 7 && (reinterpret_cast<uintptr_t>(in) & 15) == 0 &&
+                    (batch == 1 || in_bstride % 2 == 0);
+  if (pair) geo = plan_geometry(upk, dn, L, out_len, G, c_override, odd_extend, true);
   // even row strides need a conflict-free window layout: the XOR permutation for ctz(S)
-  // (complex float signals with real taps), one pad per 16 elements otherwise
-  int pad = (geo.S % 2) ? 0 : 4;
-  if (pad && std::is_same<T, float>::value && XC && !HC) {
-    int t = 0;
-    while (t < 7 && ((geo.S >> t) & 1) == 0) t++;
-    pad = 10 + t;
-  }
+  // (complex float signals with real taps), one pad per 16 elements otherwise; the paired
+  // walk takes the unit layout for ctz(S/2)
+  auto pad_for = [&](bool paired) -> int {
+    if (paired) return 20 + t2;
+    int pd = (geo.S % 2) ? 0 : 4;
+    if (pd && std::is_same<T, float>::value && XC && !HC) {
+      int t = 0;
+      while (t < 7 && ((geo.S >> t) & 1) == 0) t++;
+      pd = 10 + t;
+    }
+    return pd;
+  };
+  int pad = pad_for(pair);
   // window buffer: padded layout for even S; for odd S room for the 16-byte-aligned bulk copy
   constexpr int64_t G16 = 16 / (int64_t)sizeof(XT);
   auto window_alloc = [&](int64_t win) -> int64_t {
@@ -990,6 +1224,7 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
   p.scale = scale;
   p.rev = rev;
   p.nbuf = nbuf;
+  p.pair = pair ? 1 : 0;
   if (smem <= (ring ? 225 : 200) * 1024) {
     p.Nt = geo.Nt;
     p.S = geo.S;
@@ -1028,6 +1263,7 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
     }
     if constexpr (kRingType) {
       if (ring) return dispatch_ring(p, omap, rq, pad, smem, s, threads);
+      if (pair) return dispatch_pair(p, omap, rq, pad, smem, s, threads);
     }
     return dispatch_rq<T, XC, HC>(p, omap, rq, pad, smem, s, threads);
   }

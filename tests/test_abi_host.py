@@ -2,6 +2,7 @@
 header declares, and its host-side validation returns the MatX error classes
 before any device work (fake, never-dereferenced pointers)."""
 import ctypes
+import math
 import os
 import re
 
@@ -181,7 +182,7 @@ def test_channelize_validation(lib):
 
 def test_resample_tile_hook(lib):
     assert lib.gbfir_set_resample_tile(3, 1, 1, 0) == 1
-    assert lib.gbfir_set_resample_tile(2, 4, 1, 8) == 1
+    assert lib.gbfir_set_resample_tile(2, 4, 1, 16) == 1
     assert lib.gbfir_set_resample_tile(2, 4, 1, 1) == 0
     assert lib.gbfir_set_resample_tile(2, 4, 1, 3) == 0   # the ring form
     assert lib.gbfir_set_resample_tile(0, 0, 0, 0) == 0
@@ -257,7 +258,9 @@ def test_tuner_candidates_are_valid_tiles(lib, updown, tma_store):
         for rq, wc, grp, nb in cands:
             assert lib.gbfir_resample_tile_register(up, down, 61, rq, wc, grp, nb) == 0, (rq, wc, grp, nb)
             assert (nb & 4 == 0) or tma_store
-        for bad in ((3, 1, 4, 1), (1, 3, 4, 1), (4, 12, 4, 1), (1, 1, 65, 1), (1, 1, 4, 16), (1, 1, 4, 8),
+            g = math.gcd(up, down)
+            assert (nb & 8 == 0) or (tma_store and (down // g * grp) % 2 == 0)
+        for bad in ((3, 1, 4, 1), (1, 3, 4, 1), (4, 12, 4, 1), (1, 1, 65, 1), (1, 1, 4, 16), (1, 1, 4, 32),
                     (1, 17, 4, 1), (-1, 1, 4, 1)):
             assert lib.gbfir_resample_tile_register(up, down, 61, *bad) != 0, bad
         assert lib.gbfir_resample_tile_register(0, down, 61, 1, 1, 4, 1) != 0

@@ -291,12 +291,19 @@ def test_resample_tma_store_epilogue(mx, orc, case):
     (3, 2, 2, 20001, (2, 2, 8)), (3, 2, 3, 20000, (1, 1, 4)), (4, 5, 1, 20003, (2, 2, 3)),
     (4, 5, 2, 20000, (1, 1, 1)), (160, 147, 2, 20011, (1, 10, 1)), (160, 147, 1, 20000, (2, 16, 1)),
     (1, 2, 2, 9999, (2, 2, 2)), (2, 1, 3, 7777, (1, 4, 0)), (3, 2, 64, 1 << 18, (1, 1, 2)),
-    (4, 5, 64, 1 << 18, (2, 1, 1)),
+    (4, 5, 64, 1 << 18, (2, 1, 1)), (3, 2, 2, 20001, (4, 2, 8)), (160, 147, 2, 20011, (4, 8, 1)),
+    (4, 5, 64, 1 << 18, (4, 1, 3)),
+    # paired walk: S/2 odd (plain layout, bulk copies) and S/2 = 2^t * odd, t = 1..4 (unit XOR)
+    (3, 2, 2, 20001, (2, 2, 3)), (3, 2, 3, 20011, (2, 8, 20)), (4, 5, 2, 20000, (2, 2, 2)),
+    (4, 5, 2, 20003, (1, 1, 4)), (160, 147, 2, 20011, (2, 10, 2)), (3, 2, 64, 1 << 18, (2, 4, 12)),
+    (1, 2, 2, 9999, (2, 1, 8)), (4, 5, 64, 1 << 18, (2, 1, 6)), (3, 2, 2, 30000, (1, 8, 32)),
 ])
 def test_resample_ring_form(mx, orc, case):
     """Buffers = 3 is the ring form (a staging warp, 3-4 window slots, mbarriers instead of
-    CTA barriers): the same arithmetic as the two-buffer form, so bit for bit the same
-    outputs, with direct and with TMA-store epilogues; rows checked against the oracle."""
+    CTA barriers) and + 8 the paired walk (two samples per load, bands from even k): the same
+    multiply-adds in the same order as the two-buffer form (a leading zero tap adds +-0), so
+    bit for bit the same outputs, with direct and with TMA-store epilogues; rows checked
+    against the oracle."""
     import torch
     up, down, B, N, (rq, wc, g) = case
     rng = np.random.default_rng(seed_of("ring", *case[:4]))
@@ -306,16 +313,19 @@ def test_resample_ring_form(mx, orc, case):
     try:
         mx.set_resample_tile(rq, wc, g, 2)
         y2 = mx.resample_poly(xd, hd, up, down)
-        mx.set_resample_tile(rq, wc, g, 3)
-        y3 = mx.resample_poly(xd, hd, up, down)
-        mx.set_resample_tile(rq, wc, g, 7)
-        y7 = mx.resample_poly(xd, hd, up, down)
+        ys = {}
+        # ring; + TMA-store epilogue; + paired walk (even strides), also in the one- and
+        # two-buffer forms
+        for nb in (3, 7, 11, 15, 9, 10, 14):
+            mx.set_resample_tile(rq, wc, g, nb)
+            ys[nb] = mx.resample_poly(xd, hd, up, down)
         torch.cuda.synchronize()
         assert mx._lib.load().gbfir_tc_status() == 0
     finally:
         mx.set_resample_tile(0, 0, 0, 0)
-    assert torch.equal(y3, y2), case
-    assert torch.equal(y7, y2), case
+    for nb, y in ys.items():
+        assert torch.equal(y, y2), (case, nb)
+    y3 = ys[3]
     rows = [0, B - 1] if B > 1 else [0]
     assert rel_l2(host(y3[rows]), orc.resample_poly(x[rows], h, up, down, nthreads=2)) < FP32_TOL, case
 
