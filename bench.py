@@ -213,11 +213,16 @@ def _flush_l2(buf):
 
 
 def _timed(fn, steps, flush, stream):
-    """Sum of per-launch CUDA-event times of fn over `steps` calls, L2 flushed before each."""
+    """Mean per-launch CUDA-event time of fn over `steps` calls, L2 flushed before each.  A
+    ~50 us device-side delay between the flush and the start event keeps the GPU busy while
+    the host dispatches fn, so the timed region holds the launch's device time only (for
+    launches of a few tens of microseconds the host's dispatch path would otherwise show up
+    as idle time between the events)."""
     import torch
     total = 0.0
     for _ in range(steps):
         flush()
+        torch.cuda._sleep(100_000)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         fn()

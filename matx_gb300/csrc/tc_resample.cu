@@ -380,33 +380,45 @@ __global__ void __launch_bounds__(kWsThreads, 1) tc_resample_kernel(const TcPara
     }
   }
   __syncthreads();
-  // items run row-fastest (consecutive lanes take consecutive rows of one K chunk, so their
-  // 16-byte stores fill whole 128-byte core matrices: conflict-free); a chunk whose tap range
-  // misses the filter is stored as zeros without gathers
+  if (tid == 0) GBFIR_TC_TRACE(3, 2, 0);
+  // A thread owns one row of W and every tpr-th of its 8-wide K chunks (consecutive lanes take
+  // consecutive rows of one chunk, so their 16-byte stores fill whole 128-byte core matrices:
+  // conflict-free); the row's constants are derived once, and along the row the tap position
+  // steps by 8*dtp per chunk (32-bit: every position lies within a few Kp*up of the filter).
+  // A chunk whose tap range misses the filter is stored as zeros without gathers.
   const int nrows_w = p.P * wrows;
-  for (int it = tid; it < nrows_w * kch; it += kWsThreads) {
-    const int kc = it / nrows_w, rr = it - kc * nrows_w;
+  const int tpr = kWsThreads >= nrows_w ? kWsThreads / nrows_w : 1;  // threads per row
+  const int dt = (int)dtp;
+  for (int sl = tid; sl < nrows_w * tpr; sl += kWsThreads) {
+    const int rr = sl % nrows_w, kc0 = sl / nrows_w;
     const int pp = rr / wrows, row = rr - pp * wrows;
     const int t = row / p.Nmma, j = row - t * p.Nmma;
-    uint32_t w[4] = {0u, 0u, 0u, 0u};
-    if (j < p.Nt) {
-      const int64_t kk = 8 * kc + p.k0;
-      const int64_t tp0 = p.path == 0 ? p.c + (int64_t)j * p.down - kk * p.up
-                                      : p.c + p.down * (int64_t)j - p.up * (pp + p.down * kk);
-      const int64_t tp7 = tp0 + 7 * dtp;  // dtp < 0: the chunk reads taps tp7..tp0
-      if (tp0 >= 0 && tp7 < p.Lo) {
+    unsigned char *wrow = warr(pp);
+    const bool live = j < p.Nt;
+    // tap position of chunk 0's first element
+    const int tpj = (int)(p.path == 0 ? p.c + (int64_t)j * p.down - p.k0 * p.up
+                                      : p.c + p.down * (int64_t)j - p.up * (pp + p.down * p.k0));
+    const uint16_t *zt0 = zline + (size_t)t * zlen;
+    const int ztl = (int)tp_lo;
+    const int Lo = (int)p.Lo;
+    for (int kc = kc0; kc < kch; kc += tpr) {
+      uint32_t w[4] = {0u, 0u, 0u, 0u};
+      const int tp0 = tpj + 8 * kc * dt;
+      const int tp7 = tp0 + 7 * dt;  // dt < 0: the chunk reads taps tp7..tp0
+      if (live && tp0 >= 0 && tp7 < Lo) {
         if (z_staged) {
-          const uint16_t *zt = zline + (size_t)t * zlen + (tp0 - tp_lo);
+          const uint16_t *zt = zt0 + (tp0 - ztl);
 #pragma unroll
-          for (int e = 0; e < 8; e++) w[e >> 1] |= (uint32_t)zt[e * dtp] << (16 * (e & 1));
+          for (int e = 0; e < 8; e++) w[e >> 1] |= (uint32_t)zt[e * dt] << (16 * (e & 1));
         } else {
 #pragma unroll
-          for (int e = 0; e < 8; e++) w[e >> 1] |= w_term(t, tp0 + e * dtp) << (16 * (e & 1));
+          for (int e = 0; e < 8; e++) w[e >> 1] |= w_term(t, tp0 + e * dt) << (16 * (e & 1));
         }
       }
+      *reinterpret_cast<uint4 *>(wrow + tc::kmajor_offset(row, 8 * kc, p.Kp)) = make_uint4(w[0], w[1], w[2], w[3]);
     }
-    *reinterpret_cast<uint4 *>(warr(pp) + tc::kmajor_offset(row, 8 * kc, p.Kp)) = make_uint4(w[0], w[1], w[2], w[3]);
   }
+  if (tid == 0) GBFIR_TC_TRACE(3, 3, 0);
   tc::fence_async_smem();
   tc::tc_fence_before();
   __syncthreads();
