@@ -364,7 +364,9 @@ GBFIR_API int gbfir_ragged_resample(const gbfir_ragged_desc *device_descs, int64
  * warps, col_warps 1/2/4/8 giving 16/col_warps row slices; other signals take 2),
  * plus 4 to write the outputs through shared memory and TMA tensor stores (complex
  * float signals with real taps, rows of 2, 4 or >= 8 even outputs; other cases
- * store directly).  Zero for a field keeps the built-in heuristic for it.
+ * store directly), plus 8 for the paired walk (even row strides: two samples per
+ * 16-byte load, bands from even k).  Zero for a field keeps the built-in heuristic
+ * for it.
  * Process-wide setting, not thread-safe. */
 GBFIR_API int gbfir_set_resample_tile(int32_t rows_per_thread, int32_t col_warps,
                             int32_t group, int32_t buffers);

@@ -720,17 +720,25 @@ __device__ __forceinline__ void cp_async_mbar_arrive(uint64_t *bar) {
 
 
 constexpr int kRingMax = 4;       // window slots of the ring form
-constexpr int kRingThreads = 544; // one staging warp + up to 16 compute warps
+constexpr int kRingStageMax = 2;  // staging warps of the ring form (ring_stages)
+constexpr int kRingThreads = 32 * (kRingStageMax + 16);  // + up to 16 compute warps
 
-// Ring form of the row tile (complex float signal, real taps; one CTA per SM).  Warp 0
-// stages the windows of the CTA's tiles into a ring of p.nbuf (3 or 4) slots, up to
-// p.nbuf - 1 tiles ahead of the compute warps — one TMA bulk copy per window for an odd
-// row stride or the plain paired layout (PAD 0, 20), cp.async into the conflict-free
-// layouts otherwise (per sample for PAD 11..17, per 16-byte unit for PAD 21..27) — and warps
-// 1.. compute as in the two-buffer form (PAD >= 20: the paired walk).  A full and an empty mbarrier per slot take the place of the
-// CTA-wide barriers, so a compute warp waits only when the copies fall behind and the next
-// windows are already in flight while a tile is computed.  Every wait is bounded; one that
-// gives up records the status read by rowtile_status_take() and ends the CTA's loop.
+// Staging warps of the ring form for a window layout: two where the window is one bulk copy
+// (PAD 0, 20), one where cp.async stages it per sample or unit.  Measured on the fixed-tile
+// step (two runs each, same box): 3/2 (PAD 22) 0.302 ms with one, 0.322 with two; 4/5 (PAD
+// 20) 0.248 with one, 0.239 with two.  A count chosen at run time instead cost 4-13 %.
+__host__ __device__ constexpr int ring_stages(int pad) { return (pad == 0 || pad == 20) ? 2 : 1; }
+
+// Ring form of the row tile (complex float signal, real taps; one CTA per SM).  The first
+// ring_stages(PAD) warps stage the windows of the CTA's tiles into a ring of p.nbuf (3 or 4)
+// slots, up to p.nbuf - 1 tiles ahead of the compute warps — one TMA bulk copy per window for an odd row stride or the plain paired layout (PAD
+// 0, 20), cp.async into the conflict-free layouts otherwise (per sample for PAD 11..17, per
+// 16-byte unit for PAD 21..27; two staging warps take alternate 32-element groups) — and
+// the other warps compute as in the two-buffer form (PAD >= 20: the paired walk).  A full and an empty
+// mbarrier per slot take the place of the CTA-wide barriers, so a compute warp waits only
+// when the copies fall behind and the next windows are already in flight while a tile is
+// computed.  Every wait is bounded; one that gives up records the status read by
+// rowtile_status_take() and ends the CTA's loop.
 template <int RQ, int PAD>
 __global__ void __launch_bounds__(kRingThreads, 1)
     resample_rowtile_ring(const RsParams p, const __grid_constant__ CUtensorMap omap) {
@@ -740,14 +748,15 @@ __global__ void __launch_bounds__(kRingThreads, 1)
   unsigned char *table = smem_raw;
   float2 *xbuf0 = reinterpret_cast<float2 *>(smem_raw + tap_table_bytes<float, true, false>(p.ncg, p.span));
   const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
-  const int ncw = (int)(blockDim.x >> 5) - 1;
+  constexpr int nstage = ring_stages(PAD);
+  const int ncw = (int)(blockDim.x >> 5) - nstage;
   const int R = p.nbuf;
   const float2 *xp = reinterpret_cast<const float2 *>(p.x);
   if (tid == 0) GBFIR_TC_TRACE(3, 0, 1);
   build_tap_table<float, true, false>(p, reinterpret_cast<const float *>(p.h), table, tid, blockDim.x);
   if (tid == 0) {
     for (int i = 0; i < R; i++) {
-      tc::mbar_init(&full[i], 32);   // the 32 lanes of the staging warp
+      tc::mbar_init(&full[i], 32 * nstage);  // every lane of the staging warps
       tc::mbar_init(&empty[i], ncw); // lane 0 of every compute warp
     }
     s_fail = 0;
@@ -767,15 +776,16 @@ __global__ void __launch_bounds__(kRingThreads, 1)
   };
 
   if (tid == 0) GBFIR_TC_TRACE(3, 0, 0);
-  if (wid == 0) {
-    // ================= staging warp =================
+  if (wid < nstage) {
+    // ================= staging warps =================
+    const int sl = wid * 32 + lane, nsl = 32 * nstage;  // this lane's share of a window
     int64_t n = 0;
     for (int64_t tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++n) {
       const int slot = (int)(n % R);
-      if (lane == 0) GBFIR_TC_TRACE(0, (int)n, 0);
+      if (sl == 0) GBFIR_TC_TRACE(0, (int)n, 0);
       if (n >= R) {
         int ok = 1;
-        if (lane == 0) ok = tc::mbar_wait(&empty[slot], (uint32_t)((n / R - 1) & 1)) ? 1 : 0;
+        if (lane == 0) ok = tc::mbar_wait_sleep(&empty[slot], (uint32_t)((n / R - 1) & 1)) ? 1 : 0;
         if (!__shfl_sync(0xffffffffu, ok, 0)) {
           if (lane == 0) s_fail = 1;
           break;
@@ -790,9 +800,9 @@ __global__ void __launch_bounds__(kRingThreads, 1)
         float4 *bu = reinterpret_cast<float4 *>(buf);
         const int nu = (p.win + 1) >> 1;
         if (w0 >= 0 && w0 + 2 * (int64_t)nu <= p.N) {
-          for (int u = lane; u < nu; u += 32) cp_async16_part(&bu[unit_idx<PAD>(u)], row + w0 + 2 * u, 16);
+          for (int u = sl; u < nu; u += nsl) cp_async16_part(&bu[unit_idx<PAD>(u)], row + w0 + 2 * u, 16);
         } else {
-          for (int u = lane; u < nu; u += 32) {
+          for (int u = sl; u < nu; u += nsl) {
             const int64_t gi = w0 + 2 * u;
             const int nb = (gi >= 0 && gi < p.N) ? (gi + 1 < p.N ? 16 : 8) : 0;
             cp_async16_part(&bu[unit_idx<PAD>(u)], nb ? (const void *)(row + gi) : (const void *)row, nb);
@@ -801,9 +811,9 @@ __global__ void __launch_bounds__(kRingThreads, 1)
         cp_async_mbar_arrive(&full[slot]);
       } else if constexpr (PAD > 0 && PAD != 20) {
         if (w0 >= 0 && w0 + p.win <= p.N) {
-          for (int e = lane; e < p.win; e += 32) cp_async_zfill<8>(&buf[smem_idx<PAD>(e)], row + w0 + e, true);
+          for (int e = sl; e < p.win; e += nsl) cp_async_zfill<8>(&buf[smem_idx<PAD>(e)], row + w0 + e, true);
         } else {
-          for (int e = lane; e < p.win; e += 32) {
+          for (int e = sl; e < p.win; e += nsl) {
             const int64_t gi = w0 + e;
             const bool ok = gi >= 0 && gi < p.N;
             cp_async_zfill<8>(&buf[smem_idx<PAD>(e)], ok ? (const void *)(row + gi) : (const void *)row, ok);
@@ -814,7 +824,7 @@ __global__ void __launch_bounds__(kRingThreads, 1)
         const int64_t wl = (p.win + a + 1) / 2 * 2;  // whole 16-byte units
         const bool aligned = ((reinterpret_cast<uintptr_t>(row + w0) | (uintptr_t)tc::smem_u32(buf)) & 15) == 0;
         if (aligned && w0 >= 0 && w0 + wl <= p.N) {
-          if (lane == 0) {
+          if (sl == 0) {
             const uint32_t bytes = (uint32_t)(wl * 8);
             tc::fence_async_smem();
             tc::mbar_arrive_expect_tx(&full[slot], bytes);
@@ -823,14 +833,14 @@ __global__ void __launch_bounds__(kRingThreads, 1)
             tc::mbar_arrive_plain(&full[slot]);
           }
         } else {
-          for (int64_t e = lane; e < wl; e += 32) {
+          for (int64_t e = sl; e < wl; e += nsl) {
             const int64_t gi = w0 + e;
             buf[e] = (gi >= 0 && gi < p.N) ? row[gi] : make_float2(0.f, 0.f);
           }
           tc::mbar_arrive_plain(&full[slot]);  // each lane's stores are ordered before its arrival
         }
       }
-      if (lane == 0) GBFIR_TC_TRACE(0, (int)n, 1);
+      if (sl == 0) GBFIR_TC_TRACE(0, (int)n, 1);
     }
     if constexpr (PAD != 0 && PAD != 20) {
       cp_async_commit();  // the copies were never grouped: group them, then wait for all
@@ -838,7 +848,7 @@ __global__ void __launch_bounds__(kRingThreads, 1)
     }
   } else {
     // ================= compute warps =================
-    const int cw = wid - 1;
+    const int cw = wid - nstage;
     const int wr = p.WC <= 8 ? cw / p.WC : 0, wc = p.WC <= 8 ? cw - wr * p.WC : cw;
     const float scale = (float)p.scale;
     OutStage ostage{&omap, nullptr, 0, 0};
@@ -853,7 +863,7 @@ __global__ void __launch_bounds__(kRingThreads, 1)
       const int trole = cw == 0 ? 1 : cw == ncw - 1 ? 2 : -1;
       if (lane == 0 && trole > 0) GBFIR_TC_TRACE(trole, (int)n, 0);
       // every lane waits: its own acquire makes the window's bytes visible to it
-      const bool ok = tc::mbar_wait(&full[slot], (uint32_t)((n / R) & 1));
+      const bool ok = tc::mbar_wait_sleep(&full[slot], (uint32_t)((n / R) & 1));
       if (!__all_sync(0xffffffffu, ok)) {
         if (lane == 0) s_fail = 1;
         break;
@@ -1127,9 +1137,8 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
   bool ring = kRingType && tc.nbuf == 3;
   // row slices per CTA: 8/wc for 1, 2, 4, 8 column warps, one slice (one row per thread)
   // for 9..16, so the CTA has 8 warps or wc of them; the ring form has 16 compute warps
-  // (16/wc slices) or wc, plus its staging warp
+  // (16/wc slices) or wc, plus its staging warps
   int wr = wc <= 8 ? (ring ? 16 : 8) / wc : 1;
-  int threads = 32 * wc * wr + (ring ? 32 : 0);
   // the paired walk: an even row stride and 16-byte aligned signal rows; its bands start at
   // even k
   int t2 = 0;
@@ -1151,6 +1160,8 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
     return pd;
   };
   int pad = pad_for(pair);
+  const int nstage = ring_stages(pad);
+  int threads = 32 * wc * wr + (ring ? 32 * nstage : 0);
   // window buffer: padded layout for even S; for odd S room for the 16-byte-aligned bulk copy
   constexpr int64_t G16 = 16 / (int64_t)sizeof(XT);
   auto window_alloc = [&](int64_t win) -> int64_t {
@@ -1164,7 +1175,7 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
   const bool ostore = (tc.ostore == 1 || (tc.ostore < 0 && geo.Nt >= 8)) && std::is_same<T, float>::value && XC && !HC && geo.Nt % 2 == 0 &&
                       ost_rb > 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0 &&
                       (batch == 1 || out_bstride % 2 == 0) && rows_full >= 1;
-  size_t stg_bytes = ostore ? 1024 + (size_t)(threads / 32 - (ring ? 1 : 0)) * 4096 : 0;
+  size_t stg_bytes = ostore ? 1024 + (size_t)(threads / 32 - (ring ? nstage : 0)) * 4096 : 0;
   auto smem_for = [&](int rq, int nbuf) -> size_t {
     const int64_t QC = 32LL * rq * wr;
     const int64_t win = (QC - 1) * geo.S + (geo.kmax - geo.kmin) + 1;
@@ -1174,7 +1185,7 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
   int rq = tc.rq > 0 ? tc.rq : 2;
   int nbuf = tc.nbuf > 0 ? tc.nbuf : 2;
   if (ring) {
-    // one CTA per SM of 17 warps (120 registers a thread: one or two rows per thread); four
+    // one CTA per SM of up to 18 warps (112 registers a thread: one or two rows per thread); four
     // window slots, else three, else fewer rows per thread; the two-buffer form where even
     // one row per thread does not fit
     if (rq > 2) rq = 2;

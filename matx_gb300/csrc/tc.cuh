@@ -50,6 +50,26 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
   return false;
 }
 
+// Bounded wait whose polls let the thread sleep until the phase completes or about
+// kSleepHintNs have passed, so waiting warps leave the issue slots to the warps that work;
+// gives up (returns false) after kSleepLimit polls, well under a second.
+constexpr uint32_t kSleepHintNs = 200;
+constexpr uint32_t kSleepLimit = 1u << 21;
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kSleepLimit; i++) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(kSleepHintNs)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 // Arrive on `bar` and add `bytes` to the transaction count it waits for.
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
   asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
