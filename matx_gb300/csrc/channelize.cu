@@ -22,6 +22,8 @@
 //   * DFT, M = M1*M2 <= 256 (powers of two): four-step FFT, radix-M1 and radix-M2
 //     passes in registers, twiddle W_M^(c2*k1) between them, padded layouts so both
 //     passes are bank-conflict free.  Other M: direct DFT with a twiddle table.
+//   * D == M with M = 32 or 64 (float, real taps): the warp-FFT form below keeps F and the
+//     DFT in registers (shuffles across the warp) instead.
 #include "common.cuh"
 
 namespace gbfir {
@@ -42,7 +44,8 @@ struct ChParams {
   int32_t W;           // window samples
   int32_t tap_stride;  // D==M: row stride of the [c][p] tap table
   int32_t Mf, Mp;      // F/Y row stride, A row stride
-  int32_t r2_elems;    // elements in region 2 (window / A / generic Y)
+  int32_t r2_elems;    // elements in region 2 (window / A / generic Y); warp-FFT form: window buffer stride
+  int32_t out_aligned; // warp-FFT form: 16-byte stores of bin pairs are aligned
 };
 
 // W_16^k = exp(+2*pi*i*k/16), k = 0..7 (cos/sin of multiples of pi/8).
@@ -340,6 +343,189 @@ __global__ void __launch_bounds__(kChThreads) channelize_fused(const ChParams p)
   }
 }
 
+// ---- warp-FFT form: D == M with M = 32 or 64, float, real taps ----
+// A warp owns E = 8 consecutive output steps and all M channels (lane L: channel L and, for
+// M = 64, channel L + 32).  It runs the branch filters in registers exactly as the fused
+// kernel does (same taps, same multiply-add order), then the M-point DFT of each step across
+// the warp: radix-2 decimation in frequency, for M = 64 one stage inside the lane (channels
+// n and n + 32) and then five stages across lanes with shuffles (lane distance 16 .. 1, the
+// upper lane of a pair taking (partner - own) times its twiddle).  Lane L then holds bin
+// bitrev5(L) (M = 32), or bins 2*bitrev5(L) and 2*bitrev5(L) + 1 (M = 64), so each step's M
+// outputs leave as one store instruction per warp: 8 or 16 bytes a lane, the whole output
+// row.  F and Y never touch shared memory; the input window is double-buffered with
+// cp.async, the next tile's window in flight while the current one is filtered.
+__device__ __forceinline__ float2 cmulf(float2 a, float2 w) {
+  return make_float2(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x);
+}
+__device__ __forceinline__ int bitrev5(int v) { return (int)(__brev((unsigned)v) >> 27); }
+
+template <bool XC, int M>
+__global__ void __launch_bounds__(kChThreads) channelize_warpfft(const ChParams p) {
+  using XT = typename val_of<float, XC>::type;
+  constexpr int C = M / 32;  // channels per lane
+  constexpr int E = kChE;    // steps per warp item
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *taps = reinterpret_cast<float *>(smem_raw);  // [c][pp], rows of tap_stride
+  const size_t toff = ((size_t)M * p.tap_stride * sizeof(float) + 15) & ~(size_t)15;
+  XT *wbuf0 = reinterpret_cast<XT *>(smem_raw + toff);
+  XT *wbuf1 = wbuf0 + p.r2_elems;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const float *hp = reinterpret_cast<const float *>(p.h);
+  const XT *xp = reinterpret_cast<const XT *>(p.x);
+  float2 *op = reinterpret_cast<float2 *>(p.out);
+
+  for (int e = tid; e < M * p.tap_stride; e += kChThreads) {
+    const int c = e / p.tap_stride, pp = e - c * p.tap_stride;
+    const int64_t idx = (int64_t)pp * M + c;
+    taps[e] = (pp < p.P && idx < p.L) ? hp[idx] : 0.f;
+  }
+  // twiddles exp(+2*pi*i*m/M) of this lane, arguments reduced exactly in integers
+  float2 w0 = make_float2(1.f, 0.f), ws[4];
+  if constexpr (M == 64) sincospif((float)(2 * lane) / 64.f, &w0.y, &w0.x);
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int s = 16 >> i, ex = (lane & (s - 1)) * (16 / s);  // W_{2s}^(L mod s) = W_32^ex
+    sincospif((float)(2 * ex) / 32.f, &ws[i].y, &ws[i].x);
+  }
+
+  auto issue = [&](int64_t tile, XT *buf) {
+    const int64_t b = tile / p.tiles_per_row;
+    const int64_t t0 = (tile - b * p.tiles_per_row) * p.TT;
+    const XT *row = xp + b * p.x_bstride;
+    const int64_t w0i = t0 * p.D + p.D - (p.Ppad + 1) * p.M;
+    for (int e = tid; e < p.W; e += kChThreads) {
+      const int64_t gi = w0i + e;
+      const bool ok = gi >= 0 && gi < p.N;
+      cp_async_zfill<sizeof(XT)>(&buf[e], ok ? (const void *)(row + gi) : (const void *)row, ok);
+    }
+  };
+  int64_t tile = blockIdx.x;
+  if (tile < p.ntiles) issue(tile, wbuf0);
+  cp_async_commit();
+  const int Pp = (int)p.Ppad;
+  for (int it = 0; tile < p.ntiles; tile += gridDim.x, ++it) {
+    const XT *win = (it & 1) ? wbuf1 : wbuf0;
+    const int64_t next = tile + gridDim.x;
+    if (next < p.ntiles) issue(next, (it & 1) ? wbuf0 : wbuf1);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();  // this tile's window (and, the first time, the taps) is in
+    const int64_t b = tile / p.tiles_per_row;
+    const int64_t t0 = (tile - b * p.tiles_per_row) * p.TT;
+    float2 *orow = op + b * p.out_bstride;
+    for (int r = warp; r < p.TT / E; r += kChThreads / 32) {
+      Acc<float, XC> acc[C][E];
+#pragma unroll
+      for (int ci = 0; ci < C; ci++) {
+        const int c = lane + 32 * ci, sc = M - 1 - c;
+#pragma unroll
+        for (int e = 0; e < E; e++) acc[ci][e].zero();
+        const float *th = taps + (size_t)c * p.tap_stride;
+        XT cur[E], prv[E];
+        int rowi = r * E + Pp;  // window row of (t = t0 + r*E, p = 0)
+#pragma unroll
+        for (int e = 0; e < E; e++) cur[e] = win[(rowi + e) * M + sc];
+        for (int kb = 0; kb < Pp; kb += E) {
+          rowi -= E;
+#pragma unroll
+          for (int e = 0; e < E; e++) prv[e] = win[(rowi + e) * M + sc];
+          float tv[E];
+#pragma unroll
+          for (int kk = 0; kk < E; kk++) tv[kk] = th[kb + kk];
+#pragma unroll
+          for (int kk = 0; kk < E; kk++) {
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+              const XT xv = (e >= kk) ? cur[e - kk] : prv[E + e - kk];
+              mac<float, XC, false>(acc[ci][e], xv, tv[kk]);
+            }
+          }
+#pragma unroll
+          for (int e = 0; e < E; e++) cur[e] = prv[e];
+        }
+      }
+      const int kb5 = bitrev5(lane);
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        float2 a, bv = make_float2(0.f, 0.f);
+        if constexpr (XC) a = make_float2(acc[0][e].re, acc[0][e].im);
+        else a = make_float2(acc[0][e].re, 0.f);
+        if constexpr (C == 2) {
+          if constexpr (XC) bv = make_float2(acc[1][e].re, acc[1][e].im);
+          else bv = make_float2(acc[1][e].re, 0.f);
+          // channels n and n + 32: even bins from the sum, odd bins from the twiddled difference
+          const float2 sum = make_float2(a.x + bv.x, a.y + bv.y);
+          bv = cmulf(make_float2(a.x - bv.x, a.y - bv.y), w0);
+          a = sum;
+        }
+#pragma unroll
+        for (int i = 0; i < 5; i++) {
+          const int s = 16 >> i;
+          const bool up = (lane & s) != 0;
+          {
+            const float2 pa = make_float2(__shfl_xor_sync(0xffffffffu, a.x, s), __shfl_xor_sync(0xffffffffu, a.y, s));
+            const float2 d = make_float2(pa.x - a.x, pa.y - a.y);
+            a = up ? (i < 4 ? cmulf(d, ws[i]) : d) : make_float2(a.x + pa.x, a.y + pa.y);
+          }
+          if constexpr (C == 2) {
+            const float2 pb = make_float2(__shfl_xor_sync(0xffffffffu, bv.x, s), __shfl_xor_sync(0xffffffffu, bv.y, s));
+            const float2 d = make_float2(pb.x - bv.x, pb.y - bv.y);
+            bv = up ? (i < 4 ? cmulf(d, ws[i]) : d) : make_float2(bv.x + pb.x, bv.y + pb.y);
+          }
+        }
+        const int64_t t = t0 + r * E + e;
+        if (t < p.T) {
+          float2 *dst = orow + t * M;
+          if constexpr (C == 2) {
+            if (p.out_aligned) *reinterpret_cast<float4 *>(dst + 2 * kb5) = make_float4(a.x, a.y, bv.x, bv.y);
+            else {
+              dst[2 * kb5] = a;
+              dst[2 * kb5 + 1] = bv;
+            }
+          } else {
+            dst[kb5] = a;
+          }
+        }
+      }
+    }
+    __syncthreads();  // the window is read before the next-next tile's copy reuses the buffer
+  }
+  cp_async_wait<0>();
+}
+
+template <bool XC, int M>
+static int launch_warpfft(ChParams &p, int64_t batch, cudaStream_t s) {
+  using XT = typename val_of<float, XC>::type;
+  p.tap_stride = (int)(p.Ppad + ((p.Ppad % 8) == 0 ? 4 : 0));
+  const size_t taps_b = ((size_t)M * p.tap_stride * sizeof(float) + 15) & ~(size_t)15;
+  // steps per tile: 64 (one 8-step item per warp), more while two CTAs still share an SM
+  auto smem_for = [&](int TT) -> size_t {
+    const int64_t W = (int64_t)(TT - 1) * p.D + (p.Ppad + 1) * p.M;
+    const int64_t stride = (W + 1) / 2 * 2;  // buffers 16-byte aligned
+    return taps_b + 2 * (size_t)stride * sizeof(XT);
+  };
+  int TT = 64;
+  while (smem_for(TT + 64) <= 110 * 1024) TT += 64;
+  const size_t smem = smem_for(TT);
+  if (smem > 200 * 1024) return -1;
+  p.TT = TT;
+  p.W = (int32_t)((int64_t)(TT - 1) * p.D + (p.Ppad + 1) * p.M);
+  p.r2_elems = (p.W + 1) / 2 * 2;
+  p.tiles_per_row = (p.T + TT - 1) / TT;
+  p.ntiles = p.tiles_per_row * batch;
+  p.out_aligned = (reinterpret_cast<uintptr_t>(p.out) & 15) == 0 && (batch == 1 || p.out_bstride % 2 == 0) ? 1 : 0;
+  auto fn = channelize_warpfft<XC, M>;
+  int rc = ensure_smem((const void *)fn, smem, "channelize_poly");
+  if (rc) return rc;
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kChThreads, smem);
+  if (occ < 1) occ = 1;
+  int64_t grid = (int64_t)num_sms() * occ;
+  if (grid > p.ntiles) grid = p.ntiles;
+  fn<<<(unsigned)grid, kChThreads, smem, s>>>(p);
+  return check_launch("channelize_poly");
+}
+
 // ---- split path for large M*P: FIR into the output, then an in-place row DFT ----
 // Used when the fused tile does not fit in shared memory.  The FIR reads x and h
 // through L1 (lanes over channels read consecutive samples), writes F[t][c] into
@@ -497,6 +683,13 @@ static int launch_ch(ChParams &p, int64_t batch, cudaStream_t s) {
 
 template <typename T, bool XC, bool HC>
 static int dispatch_ch(ChParams &p, int64_t batch, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4 && !HC) {
+    // D == M with M = 32 or 64: the warp-FFT form (the fused kernel where its tile does not fit)
+    if (p.D == p.M && (p.M == 32 || p.M == 64)) {
+      const int rc = p.M == 32 ? launch_warpfft<XC, 32>(p, batch, s) : launch_warpfft<XC, 64>(p, batch, s);
+      if (rc >= 0) return rc;
+    }
+  }
   if constexpr (sizeof(T) == 4) {
     switch (p.M) {
       case 2: return launch_ch<T, XC, HC, 2, 1>(p, batch, s);
