@@ -36,11 +36,14 @@ constexpr int64_t kRgWindowCap = 6144;  // samples per window the heuristic aims
 __host__ __device__ inline int64_t rg_pack(int rq, int wc, int group) {
   return (int64_t)rq | ((int64_t)wc << 4) | ((int64_t)group << 8);
 }
+// shape bit of a signal whose tiles take the paired walk (even row stride, 16-byte aligned
+// signal): set by the planner, not by the tile registry
+constexpr int64_t kRgPair = (int64_t)1 << 16;
 
 // Row-tile geometry of one ragged signal; identical on host and device.
 struct RgGeom {
   int64_t up, down, Lo, c, Nt, S, kmin, kmax, rows;
-  int32_t even, ncg, span, WC, QC, RQ, identity;
+  int32_t even, ncg, span, WC, QC, RQ, identity, pair;
 };
 
 __host__ __device__ inline int64_t gcd_hd(int64_t a, int64_t b) {
@@ -85,17 +88,19 @@ __host__ __device__ inline RgGeom rg_geometry(int64_t up, int64_t down, int64_t 
   g.Nt = up * G;
   g.S = down * G;
   g.ncg = (int32_t)((g.Nt + 3) / 4);
+  // the paired walk needs an even row stride with ctz(S/2) <= 7 (rowtile.cuh's unit layouts)
+  g.pair = ((shape & kRgPair) && g.S % 2 == 0 && ((g.S >> 1) & 255) != 0) ? 1 : 0;
   int64_t span = 1;
   for (int64_t grp = 0; grp < g.ncg; grp++) {
     const int64_t j0 = 4 * grp;
     const int64_t jl = (j0 + 3 < g.Nt - 1) ? j0 + 3 : g.Nt - 1;
-    const int64_t kl0 = ceil_div(g.c + j0 * down - g.Lo + 1, up);
+    const int64_t kl0 = band_start(g.c, grp, down, g.Lo, up, g.pair != 0);
     const int64_t kh = floor_div(g.c + jl * down, up);
     if (kh - kl0 + 1 > span) span = kh - kl0 + 1;
   }
   g.span = (int32_t)((span + 1) & ~1LL);
-  g.kmin = ceil_div(g.c - g.Lo + 1, up);
-  g.kmax = ceil_div(g.c + 4 * (int64_t)(g.ncg - 1) * down - g.Lo + 1, up) + g.span - 1;
+  g.kmin = band_start(g.c, 0, down, g.Lo, up, g.pair != 0);
+  g.kmax = band_start(g.c, g.ncg - 1, down, g.Lo, up, g.pair != 0) + g.span - 1;
   g.rows = (out_len + g.Nt - 1) / g.Nt;
   const int nsg = (g.ncg + 1) / 2;
   g.RQ = (srq == 1 || srq == 2) ? srq : 1;
@@ -136,7 +141,16 @@ __device__ __forceinline__ void rg_run_item(const RsParams &p, int64_t row0, int
   const int ntl = (int)((nrows + p.QC - 1) / p.QC);
   auto issue = [&](int t, float2 *buf) {
     const int64_t xs0 = (row0 + (int64_t)t * p.QC) * p.S + p.kmin;
-    if (xs0 >= 0 && xs0 + p.win <= p.N) {
+    if constexpr (PAD >= 20) {
+      // paired walk: units of two samples (xs0 is even); the last may hold one of the signal
+      float4 *bu = reinterpret_cast<float4 *>(buf);
+      const int nu = (p.win + 1) >> 1;
+      for (int u = tid; u < nu; u += kRgThreads) {
+        const int64_t gi = xs0 + 2 * u;
+        const int nb = (gi >= 0 && gi < p.N) ? (gi + 1 < p.N ? 16 : 8) : 0;
+        cp_async16_part(&bu[unit_idx<PAD>(u)], nb ? (const void *)(row + gi) : (const void *)row, nb);
+      }
+    } else if (xs0 >= 0 && xs0 + p.win <= p.N) {
       const float2 *src = row + xs0;
       for (int e = tid; e < p.win; e += kRgThreads) cp_async_zfill<8>(&buf[smem_idx<PAD>(e)], src + e, true);
     } else {
@@ -181,7 +195,15 @@ __device__ __forceinline__ void rg_dispatch_pad(int pad, const RsParams &p, int6
     case 14: rg_run_item<RQ, 14>(p, row0, nrows, b0, b1, nbuf, table, tid); break;
     case 15: rg_run_item<RQ, 15>(p, row0, nrows, b0, b1, nbuf, table, tid); break;
     case 16: rg_run_item<RQ, 16>(p, row0, nrows, b0, b1, nbuf, table, tid); break;
-    default: rg_run_item<RQ, 17>(p, row0, nrows, b0, b1, nbuf, table, tid); break;
+    case 17: rg_run_item<RQ, 17>(p, row0, nrows, b0, b1, nbuf, table, tid); break;
+    case 20: rg_run_item<RQ, 20>(p, row0, nrows, b0, b1, nbuf, table, tid); break;
+    case 21: rg_run_item<RQ, 21>(p, row0, nrows, b0, b1, nbuf, table, tid); break;
+    case 22: rg_run_item<RQ, 22>(p, row0, nrows, b0, b1, nbuf, table, tid); break;
+    case 23: rg_run_item<RQ, 23>(p, row0, nrows, b0, b1, nbuf, table, tid); break;
+    case 24: rg_run_item<RQ, 24>(p, row0, nrows, b0, b1, nbuf, table, tid); break;
+    case 25: rg_run_item<RQ, 25>(p, row0, nrows, b0, b1, nbuf, table, tid); break;
+    case 26: rg_run_item<RQ, 26>(p, row0, nrows, b0, b1, nbuf, table, tid); break;
+    default: rg_run_item<RQ, 27>(p, row0, nrows, b0, b1, nbuf, table, tid); break;
   }
 }
 
@@ -226,13 +248,21 @@ __global__ void __launch_bounds__(kRgThreads) ragged_rowtile(const RgParams rp) 
       p.WC = g.WC;
       p.win = (int32_t)rg_window(g);
       p.scale = (double)g.up;
+      p.pair = g.pair;
       s_p = p;
       s_identity = g.identity;
       s_rq = g.RQ;
-      // even row strides: the conflict-free XOR window layout for t = ctz(S) (rowtile.cuh)
+      // even row strides: the conflict-free XOR window layout for t = ctz(S), or the paired
+      // walk's unit layout for ctz(S/2) (rowtile.cuh)
       int t = 0;
       while (t < 7 && ((g.S >> t) & 1) == 0) t++;
-      s_pad = t ? 10 + t : 0;
+      if (g.pair) {
+        int t2 = 0;
+        while (t2 < 7 && (((g.S >> 1) >> t2) & 1) == 0) t2++;
+        s_pad = 20 + t2;
+      } else {
+        s_pad = t ? 10 + t : 0;
+      }
     }
     __syncthreads();
     const RsParams &p = s_p;
@@ -372,6 +402,8 @@ int64_t gbfir_ragged_plan(const gbfir_ragged_desc *descs, int64_t count, int64_t
     const gbfir_ragged_desc &d = descs[s];
     Sig &sg = sigs[(size_t)s];
     sg.shape = rg_shape_for(d.up, d.down, d.h_len);
+    // the paired walk where the signal is 16-byte aligned (its row stride decides the rest)
+    if ((reinterpret_cast<uintptr_t>(d.in) & 15) == 0) sg.shape |= kRgPair;
     sg.g = rg_geometry(d.up, d.down, d.h_len, d.out_len, sg.shape);
     const RgGeom &g = sg.g;
     if (!g.identity) {
@@ -385,6 +417,9 @@ int64_t gbfir_ragged_plan(const gbfir_ragged_desc *descs, int64_t count, int64_t
     total += sg.tile_cost * (double)sg.ntiles;
   }
   const int64_t tb = (max_table + 15) & ~15LL;
+  // whole 16-byte units per buffer, so the second buffer keeps the 16-byte alignment the paired
+  // walk's unit copies and loads need
+  max_win = (max_win + 1) / 2 * 2;
   int nbuf = 2;
   int64_t smem = tb + 2 * max_win * 8;
   if (smem > 200 * 1024) {

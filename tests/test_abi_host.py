@@ -221,14 +221,17 @@ def test_ragged_plan_validation(lib):
         assert runs[0][0] == 0 and all(nr > 0 for _, nr in runs)
         assert all(a[0] + a[1] == b[0] for a, b in zip(runs, runs[1:]))
     assert info.buffers in (1, 2) and info.window_elems > 0
+    assert info.window_elems % 2 == 0 and info.table_bytes % 16 == 0   # 16-byte aligned buffers
     assert info.table_bytes + info.buffers * info.window_elems * 8 <= info.shared_bytes
     # a registered tile shape reaches the items of its rate and tap-length bucket
     assert lib.gbfir_ragged_tile_register(8, 10, 100, 2, 4, 2) == 0   # (4,5), taps 65..128
     n2 = lib.gbfir_ragged_plan(d, 2, None, ctypes.byref(info))
     t2 = np.empty((n2, 4), dtype=np.int64)
     lib.gbfir_ragged_plan(d, 2, t2.ctypes.data_as(ctypes.c_void_p), ctypes.byref(info))
-    assert set(t2[t2[:, 0] == 1, 3].tolist()) == {2 | (4 << 4) | (2 << 8)}
-    assert set(t2[t2[:, 0] == 0, 3].tolist()) == {0}
+    # (bit 16: the paired walk, set by the planner for 16-byte aligned signals)
+    assert set((t2[t2[:, 0] == 1, 3] & 0xFFFF).tolist()) == {2 | (4 << 4) | (2 << 8)}
+    assert set((t2[t2[:, 0] == 0, 3] & 0xFFFF).tolist()) == {0}
+    assert all(int(v) & (1 << 16) for v in t2[:, 3])
     assert lib.gbfir_ragged_tile_register(4, 5, 100, 3, 4, 2) == 1     # rows per thread 1 or 2
     assert lib.gbfir_ragged_tile_clear() == 0
     # launch refuses a plan that does not come from the planner (before touching the device)
