@@ -166,12 +166,19 @@ __global__ void __launch_bounds__(kDhThreads) rowtile_dh(const DhParams p) {
 }
 
 // dh[m] = scale * sum_p partial[p][m + off]  (fixed order over the partial rows)
+// One warp per tap: lane l sums the partials l, l + 32, ... in FP64, then the 32 lane sums
+// are added in a fixed shuffle tree — a fixed order, so the result is deterministic — and the
+// partials' loads of a warp are in flight together instead of one dependent chain per tap.
 __global__ void dh_reduce(const double *partial, int64_t nparts, int64_t Lo, int64_t off, int64_t L, double scale,
                           float *dh) {
-  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < L; m += (int64_t)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t m = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); m < L; m += nwarps) {
     double s = 0.0;
-    for (int64_t q = 0; q < nparts; q++) s += partial[q * Lo + m + off];
-    dh[m] = (float)(s * scale);
+    for (int64_t q = lane; q < nparts; q += 32) s += partial[q * Lo + m + off];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) s += __shfl_xor_sync(0xffffffffu, s, d);
+    if (lane == 0) dh[m] = (float)(s * scale);
   }
 }
 
@@ -328,7 +335,7 @@ static int run_dh(DhPlan &pl, int64_t batch, int64_t L, int64_t even_off, double
     rc = check_launch("backward dh (direct)");
     if (rc) return rc;
   }
-  dh_reduce<<<(unsigned)std::max<int64_t>(1, (L + 255) / 256), 256, 0, s>>>(p.partial, pl.grid, p.Lo, even_off, L,
+  dh_reduce<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((L + 7) / 8, 4 * num_sms())), 256, 0, s>>>(p.partial, pl.grid, p.Lo, even_off, L,
                                                                             scale, dh);
   return check_launch("backward dh reduce");
 }
