@@ -672,7 +672,7 @@ def measure_fwdbwd(args, rank, world, dev, steps=None):
     stream = torch.cuda.current_stream()
     res = {}
     steps = steps or max(3, min(args.steps, 100))
-    total_macs, total_ms = 0, 0.0
+    total_macs, total_ms, total_gms = 0, 0.0, 0.0
     for up, down in ((3, 2), (1, 1)):
         h = (torch.randn(L, device=dev, generator=g) / L ** 0.5).requires_grad_(True)
         href = torch.from_numpy(signal.firwin(L, 1.0 / max(up, down, 2), window=("kaiser", 5.0))
@@ -692,6 +692,7 @@ def measure_fwdbwd(args, rank, world, dev, steps=None):
         l0 = mx.launch_count()
         ms = _timed(step, steps, lambda: _flush_l2(flushbuf), stream)
         launches = mx.launch_count() - l0
+        gms = _graphed_timed(step, steps, lambda: _flush_l2(flushbuf), stream)
         # conv1d SAME: every output uses the taps that overlap the signal
         fmacs = (sum(min(L, n + L // 2 + 1, N - n + L // 2) for n in range(N)) * B if conv
                  else mac_count(N, L, up, down) * B)
@@ -699,8 +700,14 @@ def measure_fwdbwd(args, rank, world, dev, steps=None):
         key = "conv1d_same" if conv else f"{up}/{down}"
         res[key] = {"ms": ms, "gmacs": macs / (ms * 1e-3) / 1e9, "fwd_macs": fmacs,
                     "library_launches_per_step": launches / steps}
+        if isinstance(gms, float):
+            res[key]["graph_ms"] = gms
+            res[key]["graph_gmacs"] = macs / (gms * 1e-3) / 1e9
+        else:
+            res[key]["graph_ms"] = gms
         total_macs += macs
         total_ms += ms
+        total_gms = total_gms + gms if isinstance(gms, float) and isinstance(total_gms, float) else None
         if (up, down) == (3, 2):
             oracle_res = None
             try:
@@ -733,6 +740,10 @@ def measure_fwdbwd(args, rank, world, dev, steps=None):
                     step_f()
                 msf = _timed(step_f, steps, lambda: _flush_l2(flushbuf), stream)
                 forms[form] = {"ms": msf, "gmacs": macs / (msf * 1e-3) / 1e9, "vs_fp32": ms / msf}
+                gmsf = _graphed_timed(step_f, steps, lambda: _flush_l2(flushbuf), stream)
+                forms[form]["graph_ms"] = gmsf
+                if isinstance(gmsf, float) and isinstance(gms, float):
+                    forms[form]["graph_vs_fp32"] = gms / gmsf
                 if oracle_res is not None:
                     forms[form]["rel_l2_vs_fp64"] = _fwdbwd_errors(x, h, up, down, form, oracle_res)
             res["3/2"]["forms"] = forms
@@ -743,7 +754,32 @@ def measure_fwdbwd(args, rank, world, dev, steps=None):
             "config": {"workload": "differentiable FIR 256x16384 f32, 127 taps: resample_poly (3,2) and "
                                    "conv1d SAME; MSE loss, torch.autograd through the hand-written adjoints",
                        "l2": "flushed (256 MB write) before every timed step"},
+            "graph_ms_per_step": total_gms,
+            "graph_value": (total_macs / (total_gms * 1e-3) / 1e9) if total_gms else None,
             "per_ratio": res}
+
+
+def _graphed_timed(fn, steps, flush, stream):
+    """The step fn (forward, loss and backward through torch.autograd) captured once in a CUDA
+    graph and timed per replay like _timed: the same kernels with the host's per-launch
+    dispatch (autograd bookkeeping, Python) out of the way, as a training loop that graphs its
+    step runs it.  A string if the capture fails."""
+    import torch
+    try:
+        sg = torch.cuda.Stream()
+        sg.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(sg):
+            for _ in range(2):
+                fn()
+        torch.cuda.current_stream().wait_stream(sg)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            fn()
+        graph.replay()
+        torch.cuda.synchronize()
+        return _timed(graph.replay, steps, flush, stream)
+    except Exception as e:  # noqa: BLE001
+        return "unavailable: " + str(e)[:140]
 
 
 def run_fwdbwd(args, rank, world, dev):
@@ -891,7 +927,8 @@ def measure_configs(args, rank, world, dev):
                                            "tensor_peak_tflops", "tensor_peak_kind", "rel_l2_vs_fp64_row0",
                                            "forms", "config")),
             ("C3_channelize", measure_channelize, ("forms", "config")),
-            ("C4_fwdbwd", measure_fwdbwd, ("ms_per_step", "value", "unit", "per_ratio", "config")),
+            ("C4_fwdbwd", measure_fwdbwd, ("ms_per_step", "value", "unit", "graph_ms_per_step", "graph_value",
+                                           "per_ratio", "config")),
             ("C5_ragged", measure_ragged, ("ms_per_step", "value", "unit", "hbm_frac", "per_signal_launches_ms",
                                            "speedup_vs_per_signal", "forms", "tiles", "config")))
     for name, fn, keys in plan:
