@@ -246,11 +246,15 @@ GBFIR_API int gbfir_conv1d_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_b
                      gbfir_buf h, int32_t mode, void *workspace,
                      size_t workspace_bytes, gbfir_stream_t stream);
 
-/* gbfir_resample_poly_bwd with a choice of arithmetic for dx: precision != FP32 computes
- * dx on the tensor cores as a Toeplitz MMA pass over gy (the transposed resampler, taps
- * reversed, rates swapped; same coverage rules as the forward forms, NOT_SUPPORTED
- * otherwise).  dh always comes from the FP32 row-tile reduction with FP64 cross-block sums.
- * Other arguments and results are those of gbfir_resample_poly_bwd. */
+/* gbfir_resample_poly_bwd with a choice of arithmetic: precision != FP32 computes dx on the
+ * tensor cores as a Toeplitz MMA pass over gy (the transposed resampler, taps reversed,
+ * rates swapped; same coverage rules as the forward forms, NOT_SUPPORTED otherwise), and dh
+ * as a GEMM over the signal rows (input Hankel slab x gradient rows, FP32 in tensor memory
+ * per CTA, FP64 across CTAs, deterministic).  Where the tap gradient's row tile does not fit
+ * the tensor-core kernel (rows of up * G phases within 256 MMA columns whose input band
+ * fits two accumulators, e.g. 160/147 with thousands of taps), dh comes from the FP32
+ * row-tile reduction instead.  Other arguments and results are those of
+ * gbfir_resample_poly_bwd. */
 GBFIR_API int gbfir_resample_poly_bwd_prec(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x,
                                            gbfir_buf h, int64_t up, int64_t down, int32_t precision,
                                            void *workspace, size_t workspace_bytes, gbfir_stream_t stream);

@@ -43,8 +43,9 @@ def resample_poly_bwd(gy: torch.Tensor, x: torch.Tensor, h: torch.Tensor, up: in
                       need_dx: bool = True, need_dh: bool = True, precision="fp32"):
     """(dx, dh) of y = resample_poly(x, h, up, down) for upstream gradient gy.
 
-    ``precision`` other than "fp32" computes dx on the tensor cores (bf16, fp16 or
-    bf16x3 Toeplitz MMAs); dh always comes from the FP32 reduction with FP64 sums.
+    ``precision`` other than "fp32" computes dx (bf16, fp16 or bf16x3 Toeplitz MMAs) and
+    dh (a GEMM over the signal rows, FP64 across CTAs) on the tensor cores; dh falls back
+    to the FP32 reduction where its row tile does not fit the tensor-core kernel.
     """
     lib = _lib.load()
     gy = gy.contiguous()
@@ -112,7 +113,7 @@ class Conv1dFn(torch.autograd.Function):
 
 
 def resample_poly(x: torch.Tensor, h: torch.Tensor, up: int, down: int, precision="fp32") -> torch.Tensor:
-    """Differentiable resample_poly; ``precision`` selects the forward and dL/dx arithmetic."""
+    """Differentiable resample_poly; ``precision`` selects the forward, dL/dx and dL/dh arithmetic."""
     if x.dtype != torch.float32 or h.dtype != torch.float32 or h.dim() != 1:
         raise TypeError("matx_gb300.autograd.resample_poly: real float32 x and a 1-D float32 filter")
     return ResamplePolyFn.apply(x, h, up, down, precision)

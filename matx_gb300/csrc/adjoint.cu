@@ -305,6 +305,13 @@ static DhPlan plan_dh(const float *x, int64_t x_bstride, int64_t N, const float 
   return pl;
 }
 
+static int reduce_dh(const double *partial, int64_t nparts, int64_t Lo, int64_t even_off, int64_t L, double scale,
+                     float *dh, cudaStream_t s) {
+  dh_reduce<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((L + 7) / 8, 4 * num_sms())), 256, 0, s>>>(
+      partial, nparts, Lo, even_off, L, scale, dh);
+  return check_launch("backward dh reduce");
+}
+
 static int run_dh(DhPlan &pl, int64_t batch, int64_t L, int64_t even_off, double scale, float *dh, void *ws,
                   size_t ws_bytes, cudaStream_t s) {
   DhParams &p = pl.p;
@@ -335,9 +342,27 @@ static int run_dh(DhPlan &pl, int64_t batch, int64_t L, int64_t even_off, double
     rc = check_launch("backward dh (direct)");
     if (rc) return rc;
   }
-  dh_reduce<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((L + 7) / 8, 4 * num_sms())), 256, 0, s>>>(p.partial, pl.grid, p.Lo, even_off, L,
-                                                                            scale, dh);
-  return check_launch("backward dh reduce");
+  return reduce_dh(p.partial, pl.grid, p.Lo, even_off, L, scale, dh, s);
+}
+
+int tc_dh_partials(const float *x, int64_t x_bstride, int64_t N, const float *gy, int64_t gy_bstride, int64_t out_len,
+                   int64_t batch, int64_t up, int64_t down, int64_t Lo, int64_t c, int precision, double *partial,
+                   size_t partial_bytes, int64_t *nparts, cudaStream_t s);
+
+// dh on the tensor cores (tc_dh.cu) where a row tile fits, else the FP32 reduction above.
+static int run_dh_prec(DhPlan &pl, int precision, int64_t batch, int64_t L, int64_t even_off, double scale, float *dh,
+                       void *ws, size_t ws_bytes, cudaStream_t s) {
+  if (precision != GBFIR_PREC_FP32) {
+    const DhParams &p = pl.p;
+    if (ws == nullptr || reinterpret_cast<uintptr_t>(ws) % 8)
+      GBFIR_FAIL(GBFIR_ERR_WORKSPACE, "backward dh: needs an 8-byte aligned workspace");
+    int64_t nparts = 0;
+    const int rc = tc_dh_partials(p.x, p.x_bstride, p.N, p.gy, p.gy_bstride, p.out_len, batch, p.up, p.down, p.Lo,
+                                  p.c, precision, reinterpret_cast<double *>(ws), ws_bytes, &nparts, s);
+    if (rc == GBFIR_SUCCESS) return reduce_dh(reinterpret_cast<double *>(ws), nparts, p.Lo, even_off, L, scale, dh, s);
+    if (rc != GBFIR_ERR_NOT_SUPPORTED) return rc;
+  }
+  return run_dh(pl, batch, L, even_off, scale, dh, ws, ws_bytes, s);
 }
 
 
@@ -458,7 +483,8 @@ static int resample_bwd_impl(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf
       DhPlan pl = plan_dh((const float *)x.ptr, x.batch_stride, x.len, (const float *)gy.ptr, gy.batch_stride, gy.len,
                           x.batch, h.len, up, down, -1, true);
       const int64_t even = (h.len % 2) == 0;
-      return run_dh(pl, x.batch, h.len, even, (double)up, (float *)dh.ptr, workspace, workspace_bytes, s);
+      return run_dh_prec(pl, precision, x.batch, h.len, even, (double)up, (float *)dh.ptr, workspace, workspace_bytes,
+                         s);
     }
     return GBFIR_SUCCESS;
   } catch (...) {

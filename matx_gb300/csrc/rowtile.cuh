@@ -110,11 +110,17 @@ __host__ __device__ inline size_t tap_table_bytes(int64_t ncg, int64_t span) {
 // 8-byte slots of 128 bytes).  PAD = 10 + t, t = ctz(S) (1..7): XOR the low min(t, 4) bits
 // of the index with the bits from max(t, 4) up, a permutation inside each block of 16
 // elements that is conflict-free for every even S below 256; PAD = 1 is the t = 3 form;
-// PAD = 4, 5, 6 put one pad element after every 2^PAD elements (the other element types);
-// PAD = 0 is the plain layout (odd S).
+// PAD = 30 + t: the same for 4-byte real samples (32 lanes at stride S hit 32 distinct
+// banks), a permutation inside each block of 32 elements; PAD = 4 puts one pad element
+// after every 16 elements (the other element types); PAD = 0 is the plain layout (odd S).
 template <int PAD>
 __device__ __forceinline__ int smem_idx(int p) {
-  if constexpr (PAD > 10) {
+  if constexpr (PAD > 30) {
+    // 4-byte elements (real float), row stride S with t = PAD - 30 trailing zero bits: the
+    // row bits above the bank bits are XORed into them, a permutation inside blocks of 32
+    constexpr int t = PAD - 30, sh = t > 5 ? t : 5, m = (1 << (t < 5 ? t : 5)) - 1;
+    return p ^ ((p >> sh) & m);
+  } else if constexpr (PAD > 10) {
     constexpr int t = PAD - 10, sh = t > 4 ? t : 4, m = (1 << (t < 4 ? t : 4)) - 1;
     return p ^ ((p >> sh) & m);
   } else if constexpr (PAD == 1) {
@@ -671,7 +677,7 @@ __global__ void __launch_bounds__(RQ <= 2 ? 512 : 256)
 
   if constexpr (PAD > 0 && PAD != 20) {
     // Even row stride: the window is stored in a bank-conflict-free layout (an element
-    // permutation inside blocks of 16, a unit permutation of the paired walk, or one pad per
+    // permutation inside blocks of 16 or 32, a unit permutation of the paired walk, or one pad per
     // 16), which a bulk copy cannot produce; stage it with cp.async (zero-filled outside the
     // signal).
     auto issue_loads = [&](int64_t tile, XT *buf) {
@@ -679,7 +685,7 @@ __global__ void __launch_bounds__(RQ <= 2 ? 512 : 256)
       const int64_t q0 = (tile - b * p.tiles_per_row) * p.QC;
       const int64_t xs0 = q0 * p.S + p.kmin;
       const XT *row = xp + b * p.x_bstride;
-      if constexpr (PAD > 20) {
+      if constexpr (PAD > 20 && PAD < 30) {
         // units of two samples (xs0 is even); the last may hold one sample of the signal
         float4 *bu = reinterpret_cast<float4 *>(buf);
         const int nu = (p.win + 1) >> 1;
@@ -1116,11 +1122,23 @@ inline int dispatch_rq_pad(RsParams &p, const CUtensorMap &m, int rq, size_t sme
   return launch_rowtile<T, XC, HC, 1, PAD>(p, m, smem, s, threads);
 }
 
-// pad: 0 (odd row stride) or the pad shift 4, 5, 6 of the window layout
+// pad: 0 (odd row stride), 4 (one pad per 16), or the XOR layouts 11..17 (complex float
+// samples) and 31..37 (real float samples)
 template <typename T, bool XC, bool HC>
 inline int dispatch_rq(RsParams &p, const CUtensorMap &m, int rq, int pad, size_t smem, cudaStream_t s,
                        int threads) {
   if (pad == 0) return dispatch_rq_pad<T, XC, HC, 0>(p, m, rq, smem, s, threads);
+  if constexpr (std::is_same<T, float>::value && !XC && !HC) {
+    switch (pad) {
+      case 31: return dispatch_rq_pad<T, XC, HC, 31>(p, m, rq, smem, s, threads);
+      case 32: return dispatch_rq_pad<T, XC, HC, 32>(p, m, rq, smem, s, threads);
+      case 33: return dispatch_rq_pad<T, XC, HC, 33>(p, m, rq, smem, s, threads);
+      case 34: return dispatch_rq_pad<T, XC, HC, 34>(p, m, rq, smem, s, threads);
+      case 35: return dispatch_rq_pad<T, XC, HC, 35>(p, m, rq, smem, s, threads);
+      case 36: return dispatch_rq_pad<T, XC, HC, 36>(p, m, rq, smem, s, threads);
+      default: return dispatch_rq_pad<T, XC, HC, 37>(p, m, rq, smem, s, threads);
+    }
+  }
   if constexpr (std::is_same<T, float>::value && XC && !HC) {
     switch (pad) {
       case 11: return dispatch_rq_pad<T, XC, HC, 11>(p, m, rq, smem, s, threads);
@@ -1221,7 +1239,9 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
                          int64_t c_override, bool odd_extend, int rev, double scale, TileChoice tc, cudaStream_t s) {
   using XT = typename val_of<T, XC>::type;
   using HT = typename val_of<T, HC>::type;
-  const int64_t G = tc.group > 0 ? tc.group : 4 / gcd64(upk, 4);
+  // real float rows: Nt a multiple of 8, so every thread's 8-phase super-groups are whole
+  constexpr bool kReal32 = std::is_same<T, float>::value && !XC && !HC;
+  const int64_t G = tc.group > 0 ? tc.group : kReal32 ? 8 / gcd64(upk, 8) : 4 / gcd64(upk, 4);
   RsGeom geo = plan_geometry(upk, dn, L, out_len, G, c_override, odd_extend);
   const int nsg = (geo.ncg + 1) / 2;
   int wc = 1;
@@ -1251,10 +1271,10 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
   auto pad_for = [&](bool paired) -> int {
     if (paired) return 20 + t2;
     int pd = (geo.S % 2) ? 0 : 4;
-    if (pd && std::is_same<T, float>::value && XC && !HC) {
+    if (pd && ((std::is_same<T, float>::value && XC && !HC) || kReal32)) {
       int t = 0;
       while (t < 7 && ((geo.S >> t) & 1) == 0) t++;
-      pd = 10 + t;
+      pd = (kReal32 ? 30 : 10) + t;
     }
     return pd;
   };
@@ -1264,6 +1284,7 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
   // window buffer: padded layout for even S; for odd S room for the 16-byte-aligned bulk copy
   constexpr int64_t G16 = 16 / (int64_t)sizeof(XT);
   auto window_alloc = [&](int64_t win) -> int64_t {
+    if (pad > 30) return (win + 31) / 32 * 32;             // permutations inside blocks of 32
     if (pad == 1 || pad > 10) return (win + 15) / 16 * 16;  // the permutations stay inside blocks of 16
     return pad ? win + (win >> pad) + 1 : (win + 3 * G16 - 1) / G16 * G16;
   };

@@ -1,0 +1,413 @@
+// tc_dh.cu — the tap gradient dL/dh of resample_poly on the tensor cores (tcgen05; bf16,
+// fp16, bf16x3 split precision; FP32 accumulate in TMEM, FP64 across CTAs).  No MatX
+// counterpart: MatX has no adjoints; the gradient it must agree with is the one composed
+// from MatX's corr (include/matx/transforms/corr.h:60-69) over the forward of
+// include/matx/transforms/resample_poly.h:212-281.
+//
+// Math.  The forward is y[b][n] = scale * sum_i x[b][i] * he[c + n*down - i*up].  Cut the
+// outputs into rows of Nt = up*G (row q holds n = q*Nt + j) and read each row's inputs from
+// i = q*S + kmin + k (S = down*G).  The tap an (n, i) pair uses,
+//   t = c + j*down - (kmin + k)*up,
+// does not depend on q, so the tap gradient is a GEMM reduced over the rows:
+//   dB[k][j] = sum_{b,q} X[q][k] * GY[q][j],   X[q][k] = x[b][q*S + kmin + k],
+//                                              GY[q][j] = gy[b][q*Nt + j],
+//   dh[t] = scale * sum_{(k, j) -> t} dB[k][j].
+// dB is a (band of W input positions) x (Nt phases) matrix: M = k in MT tiles of 128 TMEM
+// lanes, N = j (Nt padded to NP, a multiple of 16), K = rows, 16 per MMA.  Each CTA reduces
+// its share of the rows in TMEM (a persistent CTA per SM, rows in stages of KR), then folds
+// its dB onto the taps in FP64, in a fixed order, into its row of partials; a second kernel
+// adds the CTAs' partials in a fixed order.  The result is deterministic.
+//
+// Pipeline (384 threads): warps 1-11 materialise each stage's operands straight from global
+// memory — the X Hankel slab and the GY slab, split into the operand terms, in the
+// no-swizzle K-major layout — into a 2-slot ring; warp 0 lane 0 issues the MMAs.  bf16x3
+// keeps the leading product x0*g0 in its own accumulator and the five smaller products in a
+// second one (every MMA costs about one FP32 rounding of its accumulator).  At the end warps
+// 0-3 drain TMEM through shared memory and every thread folds taps.  Every mbarrier wait is
+// bounded: one that gives up sets the status word read by gbfir_tc_status().
+#include <algorithm>
+
+#include "common.cuh"
+#include "tc.cuh"
+
+namespace gbfir {
+
+__device__ int32_t g_tcd_status;
+
+int tc_dh_status_take() {
+  int32_t v = 0, zero = 0;
+  if (cudaMemcpyFromSymbol(&v, g_tcd_status, sizeof(v)) != cudaSuccess) return -1;
+  cudaMemcpyToSymbol(g_tcd_status, &zero, sizeof(zero));
+  return v;
+}
+
+constexpr int kTdThreads = 384;
+constexpr int kTdProd0 = 1, kTdProdWarps = 11;
+constexpr int kTdNProd = kTdProdWarps * 32;
+constexpr int kTdBatch = 4;     // producer items whose loads are in flight together
+constexpr int kTdMaxItems = 8;  // producer items per thread and stage (planner bound)
+
+struct TdParams {
+  const float *x;
+  int64_t x_bstride, N;
+  const float *gy;
+  int64_t gy_bstride, out_len;
+  int64_t up, down, Lo, c, kmin, inv_down;
+  int64_t Nt, S;
+  int32_t NP, MT, KR, terms, fp16;
+  int64_t tiles_per_row, ntiles;
+  double *partial;  // [gridDim.x][Lo]
+};
+
+__device__ __forceinline__ void td_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+__global__ void __launch_bounds__(kTdThreads, 1) tc_dh_kernel(const TdParams p) {
+  extern __shared__ __align__(1024) unsigned char smem_dyn[];
+  __shared__ uint64_t op_full[2], op_empty[2], acc_full;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_fail, s_pok, s_aok;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  // ring slot: X tiles [terms][MT][128 x KR] then GY tiles [terms][NP x KR], bf16/fp16
+  unsigned char *smem = smem_dyn + ((1024u - (tc::smem_u32(smem_dyn) & 1023u)) & 1023u);
+  const int KR = p.KR;
+  const uint32_t abytes = 128u * (uint32_t)KR * 2u, bbytes = (uint32_t)p.NP * KR * 2u;
+  const size_t slot_bytes = ((size_t)p.MT * abytes + bbytes) * p.terms;
+  auto amat = [&](int slot, int mt, int t) { return smem + slot * slot_bytes + ((size_t)t * p.MT + mt) * abytes; };
+  auto bmat = [&](int slot, int t) {
+    return smem + slot * slot_bytes + (size_t)p.terms * p.MT * abytes + (size_t)t * bbytes;
+  };
+  const bool split = p.terms == 3;
+  const int acc_cols = p.MT * p.NP;  // M-tile mt in columns [mt*NP, mt*NP + NP)
+  const int need = split ? 2 * acc_cols : acc_cols;
+  const uint32_t tcols = need <= 32 ? 32u : need <= 64 ? 64u : need <= 128 ? 128u : need <= 256 ? 256u : 512u;
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, tcols);
+  if (tid == 0) {
+    for (int i = 0; i < 2; i++) {
+      tc::mbar_init(&op_full[i], 1);
+      tc::mbar_init(&op_empty[i], 1);
+    }
+    tc::mbar_init(&acc_full, 1);
+    s_fail = 0;
+    tc::mbar_fence_init();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const int64_t my_tiles = p.ntiles > blockIdx.x ? (p.ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+
+  if (warp >= kTdProd0) {
+    // ================= producers =================
+    // items: (X row m, 8-row K chunk) then (GY phase n, 8-row K chunk); lanes take
+    // consecutive m (n): the 8 loads of an item are rows apart, a warp's loads coalesced,
+    // and its 16-byte stores fill whole 128-byte core matrices.  A thread's items are the
+    // same in every stage (only the rows move), so their offsets are worked out once.
+    const int ptid = tid - kTdProd0 * 32;
+    const int mrows = p.MT * 128, kch = KR / 8;
+    const int nA = mrows * kch, nitems = nA + p.NP * kch;
+    const int Si = (int)p.S, Nti = (int)p.Nt;
+    int it_g[kTdMaxItems];       // element offset from the stage's first sample (X) or gradient (GY)
+    uint32_t it_s[kTdMaxItems];  // byte offset of term 0 in the ring slot; bit 31: GY item, bit 30: zero
+#pragma unroll
+    for (int j = 0; j < kTdMaxItems; j++) {
+      const int itm = ptid + j * kTdNProd;
+      it_g[j] = 0;
+      it_s[j] = 1u << 30;
+      if (itm < nA) {
+        const int kc = itm / mrows, m = itm - kc * mrows;
+        it_g[j] = 8 * kc * Si + m;
+        it_s[j] = (uint32_t)(m >> 7) * abytes + tc::kmajor_offset((uint32_t)(m & 127), 8u * kc, (uint32_t)KR);
+      } else if (itm < nitems) {
+        const int i2 = itm - nA;
+        const int kc = i2 / p.NP, n = i2 - kc * p.NP;
+        it_g[j] = 8 * kc * Nti + n;
+        it_s[j] = (1u << 31) | (n < Nti ? 0u : 1u << 30) |
+                  ((uint32_t)p.terms * p.MT * abytes + tc::kmajor_offset((uint32_t)n, 8u * kc, (uint32_t)KR));
+      }
+    }
+    const uint32_t tstride_a = (uint32_t)p.MT * abytes;
+    for (int64_t i = 0; i < my_tiles; ++i) {
+      const int slot = (int)(i & 1);
+      if (ptid == 0) s_pok = i < 2 ? 1 : (tc::mbar_wait(&op_empty[slot], (uint32_t)(((i - 2) >> 1) & 1)) ? 1 : 0);
+      td_sync(1, kTdNProd);
+      if (!s_pok) {
+        s_fail = 1;
+        break;
+      }
+      const int64_t t = blockIdx.x + i * (int64_t)gridDim.x;
+      const int64_t b = t / p.tiles_per_row;
+      const int64_t q0 = (t - b * p.tiles_per_row) * KR;
+      const int64_t xbase = q0 * p.S + p.kmin, gbase = q0 * p.Nt;
+      const float *xr = p.x + b * p.x_bstride;
+      const float *gr = p.gy + b * p.gy_bstride;
+      unsigned char *sbase = smem + slot * slot_bytes;
+#pragma unroll
+      for (int j0 = 0; j0 < kTdMaxItems; j0 += kTdBatch) {
+        if (ptid + j0 * kTdNProd >= nitems) break;
+        float v[kTdBatch][8];
+        // every load of the batch is issued before any conversion
+#pragma unroll
+        for (int bi = 0; bi < kTdBatch; bi++) {
+          const int j = j0 + bi;
+          const uint32_t sd = it_s[j];
+          if (sd & (1u << 30)) {
+#pragma unroll
+            for (int e = 0; e < 8; e++) v[bi][e] = 0.f;
+          } else if (!(sd >> 31)) {
+            const int64_t g0 = xbase + it_g[j];
+            const float *src = xr + g0;
+            if (g0 >= 0 && g0 + 7 * (int64_t)Si < p.N) {
+#pragma unroll
+              for (int e = 0; e < 8; e++) v[bi][e] = __ldg(src + e * Si);
+            } else {
+#pragma unroll
+              for (int e = 0; e < 8; e++) {
+                const int64_t gi = g0 + e * (int64_t)Si;
+                v[bi][e] = (gi >= 0 && gi < p.N) ? __ldg(xr + gi) : 0.f;
+              }
+            }
+          } else {
+            const int64_t g0 = gbase + it_g[j];
+            const float *src = gr + g0;
+            if (g0 + 7 * (int64_t)Nti < p.out_len) {
+#pragma unroll
+              for (int e = 0; e < 8; e++) v[bi][e] = __ldg(src + e * Nti);
+            } else {
+#pragma unroll
+              for (int e = 0; e < 8; e++) v[bi][e] = g0 + e * (int64_t)Nti < p.out_len ? __ldg(src + e * Nti) : 0.f;
+            }
+          }
+        }
+#pragma unroll
+        for (int bi = 0; bi < kTdBatch; bi++) {
+          const int j = j0 + bi;
+          if (ptid + j * kTdNProd >= nitems) break;
+          uint32_t w[3][4];
+#pragma unroll
+          for (int e2 = 0; e2 < 4; e2++) {
+            const float2 f = make_float2(v[bi][2 * e2], v[bi][2 * e2 + 1]);
+            if (p.fp16) {
+              const __half2 hh = __floats2half2_rn(f.x, f.y);
+              w[0][e2] = *reinterpret_cast<const uint32_t *>(&hh);
+              w[1][e2] = w[2][e2] = 0u;
+            } else {
+              __nv_bfloat162 t0, t1, t2;
+              tc::split3_bf16x2(f, t0, t1, t2);
+              w[0][e2] = *reinterpret_cast<uint32_t *>(&t0);
+              w[1][e2] = *reinterpret_cast<uint32_t *>(&t1);
+              w[2][e2] = *reinterpret_cast<uint32_t *>(&t2);
+            }
+          }
+          const uint32_t sd = it_s[j];
+          unsigned char *dst = sbase + (sd & 0x3FFFFFFFu);
+          const uint32_t ts = (sd >> 31) ? bbytes : tstride_a;
+          *reinterpret_cast<uint4 *>(dst) = make_uint4(w[0][0], w[0][1], w[0][2], w[0][3]);
+          if (p.terms == 3) {
+            *reinterpret_cast<uint4 *>(dst + ts) = make_uint4(w[1][0], w[1][1], w[1][2], w[1][3]);
+            *reinterpret_cast<uint4 *>(dst + 2 * ts) = make_uint4(w[2][0], w[2][1], w[2][2], w[2][3]);
+          }
+        }
+      }
+      tc::fence_async_smem();
+      td_sync(1, kTdNProd);
+      if (ptid == 0) tc::mbar_arrive_plain(&op_full[slot]);
+    }
+  } else if (lane == 0) {
+    // ================= MMA issuer (warp 0, one thread) =================
+    const uint32_t idesc = tc::idesc_f16(128, (uint32_t)p.NP, p.fp16 ? 0u : 1u);
+    const uint32_t sbo = (uint32_t)(KR / 8) * 128u;
+    // products of order <= 2 (signal term tx, gradient term tg), smallest first; the last,
+    // x0*g0, goes to the leading accumulator
+    constexpr uint32_t kTx = 0x001021u, kTg = 0x010201u;
+    const int npairs = split ? 6 : 1;
+    for (int64_t i = 0; i < my_tiles; ++i) {
+      const int slot = (int)(i & 1);
+      if (!tc::mbar_wait(&op_full[slot], (uint32_t)((i >> 1) & 1))) {
+        s_fail = 1;
+        break;
+      }
+      tc::tc_fence_after();
+      for (int mt = 0; mt < p.MT; mt++) {
+        for (int pr = 0; pr < npairs; pr++) {
+          const int tx = split ? (int)((kTx >> (4 * pr)) & 15u) : 0;
+          const int tg = split ? (int)((kTg >> (4 * pr)) & 15u) : 0;
+          const bool lead = pr == npairs - 1;
+          const uint32_t d = tmem + (uint32_t)(mt * p.NP) + (split && !lead ? (uint32_t)acc_cols : 0u);
+          const bool first_pair = lead || pr == 0;
+          uint64_t ad = tc::smem_desc(tc::smem_u32(amat(slot, mt, tx)), 128u, sbo);
+          uint64_t bd = tc::smem_desc(tc::smem_u32(bmat(slot, tg)), 128u, sbo);
+          for (int ks = 0; ks < KR / 16; ks++) {
+            tc::mma_f16(d, ad, bd, idesc, (i > 0 || !first_pair || ks > 0) ? 1u : 0u);
+            ad += 16;  // +256 B: two core matrices along K
+            bd += 16;
+          }
+        }
+      }
+      tc::mma_commit(&op_empty[slot]);
+    }
+    // arrives once every MMA issued above has completed (at once if there were none)
+    tc::mma_commit(&acc_full);
+  }
+
+  // ================= drain and fold =================
+  if (tid == 0) s_aok = tc::mbar_wait(&acc_full, 0u) ? 1 : 0;
+  __syncthreads();
+  const bool have = my_tiles > 0 && s_aok && !s_fail;
+  const int sstride = p.NP + 4;
+  float *stage = reinterpret_cast<float *>(smem);  // [MT*128][NP + 4] FP32, over the idle ring
+  tc::tc_fence_after();
+  if (have && warp < 4) {
+    const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+    for (int mt = 0; mt < p.MT; mt++) {
+      float *srow = stage + (size_t)(mt * 128 + 32 * warp + lane) * sstride;
+      for (int col = 0; col < p.NP; col += 16) {
+        uint32_t r[16], rc[16];
+        tc::tmem_ld16(tmem + lane_base + (uint32_t)(mt * p.NP + col), r);
+        if (split) tc::tmem_ld16(tmem + lane_base + (uint32_t)(acc_cols + mt * p.NP + col), rc);
+        tc::tmem_ld_wait();
+        if (split) {
+#pragma unroll
+          for (int q = 0; q < 16; q++) r[q] = __float_as_uint(__uint_as_float(r[q]) + __uint_as_float(rc[q]));
+        }
+#pragma unroll
+        for (int q = 0; q < 16; q += 4)
+          *reinterpret_cast<float4 *>(srow + col + q) = make_float4(
+              __uint_as_float(r[q]), __uint_as_float(r[q + 1]), __uint_as_float(r[q + 2]), __uint_as_float(r[q + 3]));
+      }
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  // tap t collects dB[k][j] over the phases j = j0, j0 + up, ... (j*down = t - c mod up),
+  // k = (c + j*down - t)/up - kmin, in increasing j: a fixed order
+  double *part = p.partial + (size_t)blockIdx.x * p.Lo;
+  const int mrows = p.MT * 128;
+  for (int64_t tp = tid; tp < p.Lo; tp += kTdThreads) {
+    double s = 0.0;
+    if (have) {
+      int64_t res = (tp - p.c) % p.up;
+      if (res < 0) res += p.up;
+      for (int64_t j = (res * p.inv_down) % p.up; j < p.Nt; j += p.up) {
+        const int64_t k = (p.c + j * p.down - tp) / p.up - p.kmin;
+        if (k >= 0 && k < mrows) s += (double)stage[(size_t)k * sstride + j];
+      }
+    }
+    part[tp] = s;
+  }
+  if ((s_fail || !s_aok) && tid == 0 && my_tiles > 0) atomicExch(&g_tcd_status, 1);
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, tcols);
+  }
+}
+
+// Plan of one tap-gradient launch.
+struct TdPlan {
+  TdParams p;
+  size_t smem;
+  int64_t grid;
+  bool ok;
+};
+
+static int64_t td_inverse(int64_t a, int64_t m) {
+  if (m == 1) return 0;
+  a %= m;
+  for (int64_t v = 1; v < m; v++)
+    if ((a * v) % m == 1) return v;
+  return 0;
+}
+
+// Rows of Nt = up*G phases: the G with the least MMA and operand work per output
+// ((MT*NP + MT*128 + NP) / Nt), NP = Nt padded to 16 <= 256 and MT*NP <= 256 (two FP32
+// accumulators within the 512 TMEM columns; the FP32 staging of dB within the ring); rows
+// per stage KR = 64, 32 or 16, the largest whose two ring slots fit.
+static TdPlan plan_tc_dh(int64_t up, int64_t down, int64_t Lo, int64_t c, int64_t out_len, int64_t batch,
+                         int precision) {
+  TdPlan pl{};
+  TdParams &p = pl.p;
+  p.terms = precision == GBFIR_PREC_BF16X3 ? 3 : 1;
+  p.fp16 = precision == GBFIR_PREC_FP16;
+  const int64_t kmin = ceil_div(c - Lo + 1, up);
+  const size_t budget = 200 * 1024;
+  auto ring_bytes = [&](int64_t MT, int64_t NP, int kr) { return 2 * ((size_t)MT * 128 + NP) * kr * 2 * p.terms; };
+  double best = 0.0;
+  int64_t bestG = 0;
+  for (int64_t G = 1; up * G <= 256; G++) {
+    const int64_t Nt = up * G, NP = (Nt + 15) / 16 * 16;
+    const int64_t W = floor_div(c + (Nt - 1) * down, up) - kmin + 1;
+    const int64_t MT = (W + 127) / 128;
+    if (MT * NP > 256 || ring_bytes(MT, NP, 16) > budget || (MT * 128 + NP) * 2 > (int64_t)kTdMaxItems * kTdNProd)
+      continue;
+    const double cost = (double)(MT * NP + MT * 128 + NP) / (double)Nt;
+    if (bestG == 0 || cost < best - 1e-9) {
+      best = cost;
+      bestG = G;
+    }
+  }
+  if (bestG == 0) return pl;
+  p.up = up;
+  p.down = down;
+  p.Lo = Lo;
+  p.c = c;
+  p.kmin = kmin;
+  p.inv_down = td_inverse(down, up);
+  p.Nt = up * bestG;
+  p.S = down * bestG;
+  p.NP = (int32_t)((p.Nt + 15) / 16 * 16);
+  p.MT = (int32_t)((floor_div(c + (p.Nt - 1) * down, up) - kmin + 1 + 127) / 128);
+  // rows per stage: the ring's two slots fit, and each producer thread has at most
+  // kTdMaxItems items (8-row chunks of an X row or a GY phase) per stage
+  auto items = [&](int kr) { return ((int64_t)p.MT * 128 + p.NP) * (kr / 8); };
+  p.KR = 0;
+  for (int kr : {64, 32, 16}) {
+    if (ring_bytes(p.MT, p.NP, kr) <= budget && items(kr) <= (int64_t)kTdMaxItems * kTdNProd) {
+      p.KR = kr;
+      break;
+    }
+  }
+  if (p.KR == 0) return pl;
+  const size_t ring = ring_bytes(p.MT, p.NP, p.KR);
+  const size_t staging = (size_t)p.MT * 128 * (p.NP + 4) * 4;
+  pl.smem = 1024 + std::max(ring, staging);
+  const int64_t rows = (out_len + p.Nt - 1) / p.Nt;
+  p.tiles_per_row = (rows + p.KR - 1) / p.KR;
+  p.ntiles = p.tiles_per_row * batch;
+  pl.grid = std::max<int64_t>(1, std::min<int64_t>(p.ntiles, num_sms()));
+  pl.ok = true;
+  return pl;
+}
+
+// The per-CTA FP64 partials of dh_e[t] = sum over (n, i) with c + n*down - i*up = t of
+// gy[n]*x[i] (extended taps t in [0, Lo)), written to partial[0 .. nparts)[Lo]; returns
+// GBFIR_ERR_NOT_SUPPORTED (nothing launched) where no row tile fits.
+int tc_dh_partials(const float *x, int64_t x_bstride, int64_t N, const float *gy, int64_t gy_bstride, int64_t out_len,
+                   int64_t batch, int64_t up, int64_t down, int64_t Lo, int64_t c, int precision, double *partial,
+                   size_t partial_bytes, int64_t *nparts, cudaStream_t s) {
+  TdPlan pl = plan_tc_dh(up, down, Lo, c, out_len, batch, precision);
+  if (!pl.ok) return GBFIR_ERR_NOT_SUPPORTED;
+  TdParams &p = pl.p;
+  p.x = x;
+  p.x_bstride = batch > 1 ? x_bstride : 0;
+  p.N = N;
+  p.gy = gy;
+  p.gy_bstride = batch > 1 ? gy_bstride : 0;
+  p.out_len = out_len;
+  p.partial = partial;
+  if ((size_t)pl.grid * Lo * sizeof(double) > partial_bytes)
+    GBFIR_FAIL(GBFIR_ERR_WORKSPACE, "backward dh (tensor cores): needs %zu B of workspace, got %zu",
+               (size_t)pl.grid * Lo * sizeof(double), partial_bytes);
+  int rc = ensure_smem((const void *)tc_dh_kernel, pl.smem, "backward dh (tensor cores)");
+  if (rc) return rc;
+  tc_dh_kernel<<<(unsigned)pl.grid, kTdThreads, pl.smem, s>>>(p);
+  rc = check_launch("backward dh (tensor cores)");
+  if (rc) return rc;
+  *nparts = pl.grid;
+  return GBFIR_SUCCESS;
+}
+
+}  // namespace gbfir

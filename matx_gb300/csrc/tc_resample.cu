@@ -968,6 +968,7 @@ int adjoint_rowtile_status();
 int tc_wide_status_take();
 int tc_channelize_status_take();
 int tc_blocks_status_take();
+int tc_dh_status_take();
 int iir_status_take();
 }  // namespace gbfir
 
@@ -982,6 +983,7 @@ extern "C" int gbfir_tc_status(void) {
   const int e = gbfir::iir_status_take();
   const int f = gbfir::tc_channelize_status_take();
   const int g = gbfir::tc_blocks_status_take();
-  if (a < 0 || b < 0 || c < 0 || d < 0 || e < 0 || f < 0 || g < 0) return -1;
-  return (a | b | c | d | e | f | g) ? 1 : 0;
+  const int k = gbfir::tc_dh_status_take();
+  if (a < 0 || b < 0 || c < 0 || d < 0 || e < 0 || f < 0 || g < 0 || k < 0) return -1;
+  return (a | b | c | d | e | f | g | k) ? 1 : 0;
 }

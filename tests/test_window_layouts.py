@@ -1,8 +1,9 @@
 """The row tile's shared-memory window layouts, restated from matx_gb300/csrc/rowtile.cuh
 (smem_idx, unit_idx): each is a permutation inside its block, and the row-strided reads of a
 warp hit distinct banks.  Lanes read rows q*S + k of the window: 8-byte loads are served per
-half-warp (16 lanes, 16 slots of 8 bytes per 128-byte wavefront), the paired form's 16-byte
-loads per quarter-warp (8 lanes, 8 units of 16 bytes)."""
+half-warp (16 lanes, 16 slots of 8 bytes per 128-byte wavefront), 4-byte loads of real
+samples per warp (32 lanes, 32 banks), the paired form's 16-byte loads per quarter-warp (8
+lanes, 8 units of 16 bytes)."""
 import pytest
 
 
@@ -17,6 +18,13 @@ def smem_idx(p, pad):
     """Element XOR layout for an even row stride S, pad = 10 + ctz(S)."""
     t = pad - 10
     sh, m = max(t, 4), (1 << min(t, 4)) - 1
+    return p ^ ((p >> sh) & m)
+
+
+def smem_idx_real(p, pad):
+    """Element XOR layout of real float samples for an even row stride S, pad = 30 + ctz(S)."""
+    t = pad - 30
+    sh, m = max(t, 5), (1 << min(t, 5)) - 1
     return p ^ ((p >> sh) & m)
 
 
@@ -64,3 +72,18 @@ def test_unit_layout_conflict_free():
             for q in range(0, 32, 8):
                 slots = {unit_idx(c + (q + lane) * s2, pad) % 8 for lane in range(8)}
                 assert len(slots) == 8, (s2, c, q)
+
+
+@pytest.mark.parametrize("pad", list(range(31, 38)))
+def test_real_layout_is_a_block_permutation(pad):
+    for base in (0, 32, 8192):
+        block = [smem_idx_real(base + i, pad) for i in range(32)]
+        assert sorted(block) == list(range(base, base + 32))
+
+
+def test_real_layout_conflict_free():
+    for S in range(2, 256, 2):
+        pad = 30 + min(ctz(S), 7)
+        for c in range(64):
+            banks = {smem_idx_real(c + lane * S, pad) % 32 for lane in range(32)}
+            assert len(banks) == 32, (S, c)
