@@ -1239,9 +1239,10 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
                          int64_t c_override, bool odd_extend, int rev, double scale, TileChoice tc, cudaStream_t s) {
   using XT = typename val_of<T, XC>::type;
   using HT = typename val_of<T, HC>::type;
-  // real float rows: Nt a multiple of 8, so every thread's 8-phase super-groups are whole
+  // real float rows: at least 8 phases, so a thread's 8-phase super-group is not half empty
   constexpr bool kReal32 = std::is_same<T, float>::value && !XC && !HC;
-  const int64_t G = tc.group > 0 ? tc.group : kReal32 ? 8 / gcd64(upk, 8) : 4 / gcd64(upk, 4);
+  int64_t G = tc.group > 0 ? tc.group : 4 / gcd64(upk, 4);
+  if (tc.group <= 0 && kReal32 && upk * G < 8) G = 8 / gcd64(upk, 8);
   RsGeom geo = plan_geometry(upk, dn, L, out_len, G, c_override, odd_extend);
   const int nsg = (geo.ncg + 1) / 2;
   int wc = 1;
@@ -1302,7 +1303,9 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
     const int64_t alloc = window_alloc(win);
     return tap_table_bytes<T, XC, HC>(geo.ncg, geo.span) + (size_t)nbuf * (size_t)alloc * sizeof(XT) + stg_bytes;
   };
-  int rq = tc.rq > 0 ? tc.rq : 2;
+  // four rows per thread for real float rows: the f32x2 FMAs of a sample need one 16-byte
+  // tap load per band and k, shared by the thread's rows
+  int rq = tc.rq > 0 ? tc.rq : kReal32 ? 4 : 2;
   int nbuf = tc.nbuf > 0 ? tc.nbuf : 2;
   if (ring) {
     // one CTA per SM of up to 18 warps (112 registers a thread: one or two rows per thread); four
