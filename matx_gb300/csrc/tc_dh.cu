@@ -20,7 +20,8 @@
 //
 // Pipeline (384 threads): warps 1-11 materialise each stage's operands straight from global
 // memory — the X Hankel slab and the GY slab, split into the operand terms, in the
-// no-swizzle K-major layout — into a 2-slot ring; warp 0 lane 0 issues the MMAs.  bf16x3
+// no-swizzle K-major layout — into a ring of 2 to 4 slots, each warp arriving on the slot's
+// barrier when its own items are stored (no CTA-wide barrier); warp 0 lane 0 issues the MMAs.  bf16x3
 // keeps the leading product x0*g0 in its own accumulator and the five smaller products in a
 // second one (every MMA costs about one FP32 rounding of its accumulator).  At the end warps
 // 0-3 drain TMEM through shared memory and every thread folds taps.  Every mbarrier wait is
@@ -46,6 +47,7 @@ constexpr int kTdProd0 = 1, kTdProdWarps = 11;
 constexpr int kTdNProd = kTdProdWarps * 32;
 constexpr int kTdBatch = 4;     // producer items whose loads are in flight together
 constexpr int kTdMaxItems = 8;  // producer items per thread and stage (planner bound)
+constexpr int kTdMaxSlots = 4;  // operand ring slots
 
 struct TdParams {
   const float *x;
@@ -55,19 +57,17 @@ struct TdParams {
   int64_t up, down, Lo, c, kmin, inv_down;
   int64_t Nt, S;
   int32_t NP, MT, KR, terms, fp16;
+  int32_t nslot;  // operand ring slots (2..4)
   int64_t tiles_per_row, ntiles;
   double *partial;  // [gridDim.x][Lo]
 };
 
-__device__ __forceinline__ void td_sync(int id, int nthreads) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
-}
 
 __global__ void __launch_bounds__(kTdThreads, 1) tc_dh_kernel(const TdParams p) {
   extern __shared__ __align__(1024) unsigned char smem_dyn[];
-  __shared__ uint64_t op_full[2], op_empty[2], acc_full;
+  __shared__ uint64_t op_full[kTdMaxSlots], op_empty[kTdMaxSlots], acc_full;
   __shared__ uint32_t tmem_slot;
-  __shared__ int s_fail, s_pok, s_aok;
+  __shared__ int s_fail, s_aok;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   // ring slot: X tiles [terms][MT][128 x KR] then GY tiles [terms][NP x KR], bf16/fp16
@@ -85,8 +85,8 @@ __global__ void __launch_bounds__(kTdThreads, 1) tc_dh_kernel(const TdParams p) 
   const uint32_t tcols = need <= 32 ? 32u : need <= 64 ? 64u : need <= 128 ? 128u : need <= 256 ? 256u : 512u;
   if (warp == 0) tc::tmem_alloc(&tmem_slot, tcols);
   if (tid == 0) {
-    for (int i = 0; i < 2; i++) {
-      tc::mbar_init(&op_full[i], 1);
+    for (int i = 0; i < p.nslot; i++) {
+      tc::mbar_init(&op_full[i], kTdProdWarps);
       tc::mbar_init(&op_empty[i], 1);
     }
     tc::mbar_init(&acc_full, 1);
@@ -130,10 +130,11 @@ __global__ void __launch_bounds__(kTdThreads, 1) tc_dh_kernel(const TdParams p) 
     }
     const uint32_t tstride_a = (uint32_t)p.MT * abytes;
     for (int64_t i = 0; i < my_tiles; ++i) {
-      const int slot = (int)(i & 1);
-      if (ptid == 0) s_pok = i < 2 ? 1 : (tc::mbar_wait(&op_empty[slot], (uint32_t)(((i - 2) >> 1) & 1)) ? 1 : 0);
-      td_sync(1, kTdNProd);
-      if (!s_pok) {
+      const int slot = (int)(i % p.nslot);
+      const int64_t round = i / p.nslot;
+      int ok = 1;
+      if (lane == 0 && round > 0) ok = tc::mbar_wait(&op_empty[slot], (uint32_t)((round - 1) & 1)) ? 1 : 0;
+      if (!__shfl_sync(0xffffffffu, ok, 0)) {
         s_fail = 1;
         break;
       }
@@ -212,8 +213,8 @@ __global__ void __launch_bounds__(kTdThreads, 1) tc_dh_kernel(const TdParams p) 
         }
       }
       tc::fence_async_smem();
-      td_sync(1, kTdNProd);
-      if (ptid == 0) tc::mbar_arrive_plain(&op_full[slot]);
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive_plain(&op_full[slot]);
     }
   } else if (lane == 0) {
     // ================= MMA issuer (warp 0, one thread) =================
@@ -224,8 +225,8 @@ __global__ void __launch_bounds__(kTdThreads, 1) tc_dh_kernel(const TdParams p) 
     constexpr uint32_t kTx = 0x001021u, kTg = 0x010201u;
     const int npairs = split ? 6 : 1;
     for (int64_t i = 0; i < my_tiles; ++i) {
-      const int slot = (int)(i & 1);
-      if (!tc::mbar_wait(&op_full[slot], (uint32_t)((i >> 1) & 1))) {
+      const int slot = (int)(i % p.nslot);
+      if (!tc::mbar_wait(&op_full[slot], (uint32_t)((i / p.nslot) & 1))) {
         s_fail = 1;
         break;
       }
@@ -324,8 +325,7 @@ static int64_t td_inverse(int64_t a, int64_t m) {
 
 // Rows of Nt = up*G phases: the G with the least MMA and operand work per output
 // ((MT*NP + MT*128 + NP) / Nt), NP = Nt padded to 16 <= 256 and MT*NP <= 256 (two FP32
-// accumulators within the 512 TMEM columns; the FP32 staging of dB within the ring); rows
-// per stage KR = 64, 32 or 16, the largest whose two ring slots fit.
+// accumulators within the 512 TMEM columns; the FP32 staging of dB within the ring).
 static TdPlan plan_tc_dh(int64_t up, int64_t down, int64_t Lo, int64_t c, int64_t out_len, int64_t batch,
                          int precision) {
   TdPlan pl{};
@@ -334,14 +334,14 @@ static TdPlan plan_tc_dh(int64_t up, int64_t down, int64_t Lo, int64_t c, int64_
   p.fp16 = precision == GBFIR_PREC_FP16;
   const int64_t kmin = ceil_div(c - Lo + 1, up);
   const size_t budget = 200 * 1024;
-  auto ring_bytes = [&](int64_t MT, int64_t NP, int kr) { return 2 * ((size_t)MT * 128 + NP) * kr * 2 * p.terms; };
+  auto slot_bytes = [&](int64_t MT, int64_t NP, int kr) { return ((size_t)MT * 128 + NP) * kr * 2 * p.terms; };
   double best = 0.0;
   int64_t bestG = 0;
   for (int64_t G = 1; up * G <= 256; G++) {
     const int64_t Nt = up * G, NP = (Nt + 15) / 16 * 16;
     const int64_t W = floor_div(c + (Nt - 1) * down, up) - kmin + 1;
     const int64_t MT = (W + 127) / 128;
-    if (MT * NP > 256 || ring_bytes(MT, NP, 16) > budget || (MT * 128 + NP) * 2 > (int64_t)kTdMaxItems * kTdNProd)
+    if (MT * NP > 256 || 2 * slot_bytes(MT, NP, 16) > budget || (MT * 128 + NP) * 2 > (int64_t)kTdMaxItems * kTdNProd)
       continue;
     const double cost = (double)(MT * NP + MT * 128 + NP) / (double)Nt;
     if (bestG == 0 || cost < best - 1e-9) {
@@ -360,18 +360,21 @@ static TdPlan plan_tc_dh(int64_t up, int64_t down, int64_t Lo, int64_t c, int64_
   p.S = down * bestG;
   p.NP = (int32_t)((p.Nt + 15) / 16 * 16);
   p.MT = (int32_t)((floor_div(c + (p.Nt - 1) * down, up) - kmin + 1 + 127) / 128);
-  // rows per stage: the ring's two slots fit, and each producer thread has at most
-  // kTdMaxItems items (8-row chunks of an X row or a GY phase) per stage
+  // rows per stage and ring slots: stages of 32 rows in up to four slots (the producers run
+  // up to three stages ahead of the MMAs), else 64 or 16 rows in at least two; each producer
+  // thread has at most kTdMaxItems items (8-row chunks of an X row or a GY phase) per stage
   auto items = [&](int kr) { return ((int64_t)p.MT * 128 + p.NP) * (kr / 8); };
   p.KR = 0;
-  for (int kr : {64, 32, 16}) {
-    if (ring_bytes(p.MT, p.NP, kr) <= budget && items(kr) <= (int64_t)kTdMaxItems * kTdNProd) {
+  for (int kr : {32, 64, 16}) {
+    const int ns = (int)std::min<size_t>(kTdMaxSlots, budget / slot_bytes(p.MT, p.NP, kr));
+    if (ns >= 2 && items(kr) <= (int64_t)kTdMaxItems * kTdNProd) {
       p.KR = kr;
+      p.nslot = ns;
       break;
     }
   }
   if (p.KR == 0) return pl;
-  const size_t ring = ring_bytes(p.MT, p.NP, p.KR);
+  const size_t ring = (size_t)p.nslot * slot_bytes(p.MT, p.NP, p.KR);
   const size_t staging = (size_t)p.MT * 128 * (p.NP + 4) * 4;
   pl.smem = 1024 + std::max(ring, staging);
   const int64_t rows = (out_len + p.Nt - 1) / p.Nt;
