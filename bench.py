@@ -723,7 +723,7 @@ def measure_fwdbwd(args, rank, world, dev, steps=None):
                 res[key]["rel_l2_vs_fp64"] = _fwdbwd_errors(x, h, up, down, "fp32", oracle_res)
             except Exception as e:  # noqa: BLE001
                 res[key]["rel_l2_vs_fp64"] = {"unavailable": str(e)[:160]}
-            # tensor-core forms of the forward and dL/dx (dL/dh stays FP32 with FP64 sums)
+            # tensor-core forms of the forward, dL/dx and dL/dh (FP64 sums across CTAs)
             forms = {}
             for form in ("bf16x3", "bf16", "fp16"):
                 def step_f():
