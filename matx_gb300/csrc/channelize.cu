@@ -120,6 +120,21 @@ __device__ __forceinline__ void twiddle_of<double>(int64_t m, int64_t M, double 
 }
 
 // DFT kind: (M1, M2) with M = M1*M2; M1 == 0 selects the direct DFT.
+// The 8 taps th[0..7] of one channel row.  Float rows are 16-byte aligned (the table's row
+// stride is a multiple of 4 and blocks start at multiples of 8), so they come in as two
+// 16-byte loads: lanes of a quarter warp read rows 16*stride bytes apart, distinct 16-byte
+// bank groups, where eight 4-byte loads per lane would hit the same bank four times.
+template <typename HT, int E>
+__device__ __forceinline__ void load_tap_block(const HT *th, HT (&t)[E]) {
+  if constexpr (std::is_same<HT, float>::value && E == 8) {
+    const float4 a = *reinterpret_cast<const float4 *>(th), b = *reinterpret_cast<const float4 *>(th + 4);
+    t[0] = a.x, t[1] = a.y, t[2] = a.z, t[3] = a.w, t[4] = b.x, t[5] = b.y, t[6] = b.z, t[7] = b.w;
+  } else {
+#pragma unroll
+    for (int kk = 0; kk < E; kk++) t[kk] = th[kk];
+  }
+}
+
 template <typename T, bool XC, bool HC, int M1, int M2>
 __global__ void __launch_bounds__(kChThreads) channelize_fused(const ChParams p) {
   using XT = typename val_of<T, XC>::type;
@@ -201,8 +216,7 @@ __global__ void __launch_bounds__(kChThreads) channelize_fused(const ChParams p)
 #pragma unroll
           for (int e = 0; e < E; e++) prv[e] = win[(rowi + e) * M + sc];
           HT t[E];
-#pragma unroll
-          for (int kk = 0; kk < E; kk++) t[kk] = th[kb + kk];
+          load_tap_block<HT, E>(th + kb, t);
 #pragma unroll
           for (int kk = 0; kk < E; kk++) {
 #pragma unroll
@@ -430,8 +444,7 @@ __global__ void __launch_bounds__(kChThreads) channelize_warpfft(const ChParams 
 #pragma unroll
           for (int e = 0; e < E; e++) prv[e] = win[(rowi + e) * M + sc];
           float tv[E];
-#pragma unroll
-          for (int kk = 0; kk < E; kk++) tv[kk] = th[kb + kk];
+          load_tap_block<float, E>(th + kb, tv);
 #pragma unroll
           for (int kk = 0; kk < E; kk++) {
 #pragma unroll
