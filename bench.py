@@ -641,16 +641,20 @@ def run_channelize(args, rank, world, dev):
     return 0
 
 
-def _fwdbwd_errors(x, h, up, down, form, oracle_res):
+def _fwdbwd_errors(x, h, up, down, form, oracle_res, conv=False):
     """rel-L2 of y, dL/dx and dL/dh of one form against the FP64 oracle for a fixed upstream
-    gradient (untimed)."""
+    gradient (untimed); conv: conv1d SAME instead of resample_poly."""
     import torch
     import matx_gb300 as mx
     from matx_gb300 import autograd as ag
     xs, hs, gy, y64, dx64, dh64 = oracle_res
     with torch.no_grad():
-        y = mx.resample_poly(xs, hs, up, down, precision=form)
-        dx, dh = ag.resample_poly_bwd(gy, xs, hs, up, down, precision=form)
+        if conv:
+            y = mx.conv1d(xs, hs, "same", precision=form)
+            dx, dh = ag.conv1d_bwd(gy, xs, hs, "same", precision=form)
+        else:
+            y = mx.resample_poly(xs, hs, up, down, precision=form)
+            dx, dh = ag.resample_poly_bwd(gy, xs, hs, up, down, precision=form)
     rel = lambda a, b: float(np.linalg.norm(a.cpu().numpy().astype(np.float64) - b) / np.linalg.norm(b))
     return {"y": rel(y, y64), "dx": rel(dx, dx64), "dh": rel(dh, dh64)}
 
@@ -708,45 +712,50 @@ def measure_fwdbwd(args, rank, world, dev, steps=None):
         total_macs += macs
         total_ms += ms
         total_gms = total_gms + gms if isinstance(gms, float) and isinstance(total_gms, float) else None
-        if (up, down) == (3, 2):
-            oracle_res = None
-            try:
-                import oracle
-                oracle.build()
-                xs, hs = x.detach(), h.detach()
+        oracle_res = None
+        try:
+            import oracle
+            oracle.build()
+            xs, hs = x.detach(), h.detach()
+            nthr = os.cpu_count() or 1
+            xn, hn = xs.cpu().numpy(), hs.cpu().numpy()
+            if conv:
+                gy = torch.randn(B, N, device=dev, generator=g)
+                y64 = oracle.conv1d(xn, hn, 1, double=True, nthreads=nthr)
+                dx64, dh64 = oracle.conv1d_bwd(gy.cpu().numpy(), xn, hn, 1, nthreads=nthr)
+            else:
                 gy = torch.randn(B, mx.resample_out_len(N, up, down), device=dev, generator=g)
-                nthr = os.cpu_count() or 1
-                y64 = oracle.resample_poly(xs.cpu().numpy(), hs.cpu().numpy(), up, down, double=True, nthreads=nthr)
-                dx64, dh64 = oracle.resample_poly_bwd(gy.cpu().numpy(), xs.cpu().numpy(), hs.cpu().numpy(), up, down,
-                                                      nthreads=nthr)
-                oracle_res = (xs, hs, gy, y64, dx64, dh64)
-                res[key]["rel_l2_vs_fp64"] = _fwdbwd_errors(x, h, up, down, "fp32", oracle_res)
-            except Exception as e:  # noqa: BLE001
-                res[key]["rel_l2_vs_fp64"] = {"unavailable": str(e)[:160]}
-            # tensor-core forms of the forward, dL/dx and dL/dh (FP64 sums across CTAs)
-            forms = {}
-            for form in ("bf16x3", "bf16", "fp16"):
-                def step_f():
-                    x.grad = None
-                    h.grad = None
-                    y = ag.resample_poly(x, h, up, down, precision=form)
-                    torch.mean((y - target) ** 2).backward()
-                try:
-                    step_f()
-                except mx.GbfirError as ge:
-                    forms[form] = {"unavailable": str(ge)[:140]}
-                    continue
-                for _ in range(args.warmup):
-                    step_f()
-                msf = _timed(step_f, steps, lambda: _flush_l2(flushbuf), stream)
-                forms[form] = {"ms": msf, "gmacs": macs / (msf * 1e-3) / 1e9, "vs_fp32": ms / msf}
-                gmsf = _graphed_timed(step_f, steps, lambda: _flush_l2(flushbuf), stream)
-                forms[form]["graph_ms"] = gmsf
-                if isinstance(gmsf, float) and isinstance(gms, float):
-                    forms[form]["graph_vs_fp32"] = gms / gmsf
-                if oracle_res is not None:
-                    forms[form]["rel_l2_vs_fp64"] = _fwdbwd_errors(x, h, up, down, form, oracle_res)
-            res["3/2"]["forms"] = forms
+                y64 = oracle.resample_poly(xn, hn, up, down, double=True, nthreads=nthr)
+                dx64, dh64 = oracle.resample_poly_bwd(gy.cpu().numpy(), xn, hn, up, down, nthreads=nthr)
+            oracle_res = (xs, hs, gy, y64, dx64, dh64)
+            res[key]["rel_l2_vs_fp64"] = _fwdbwd_errors(x, h, up, down, "fp32", oracle_res, conv)
+        except Exception as e:  # noqa: BLE001
+            res[key]["rel_l2_vs_fp64"] = {"unavailable": str(e)[:160]}
+        # tensor-core forms of the forward, dL/dx and dL/dh (FP64 sums across CTAs)
+        forms = {}
+        for form in ("bf16x3", "bf16", "fp16"):
+            def step_f():
+                x.grad = None
+                h.grad = None
+                y = (ag.conv1d(x, h, "same", precision=form) if conv
+                     else ag.resample_poly(x, h, up, down, precision=form))
+                torch.mean((y - target) ** 2).backward()
+            try:
+                step_f()
+            except mx.GbfirError as ge:
+                forms[form] = {"unavailable": str(ge)[:140]}
+                continue
+            for _ in range(args.warmup):
+                step_f()
+            msf = _timed(step_f, steps, lambda: _flush_l2(flushbuf), stream)
+            forms[form] = {"ms": msf, "gmacs": macs / (msf * 1e-3) / 1e9, "vs_fp32": ms / msf}
+            gmsf = _graphed_timed(step_f, steps, lambda: _flush_l2(flushbuf), stream)
+            forms[form]["graph_ms"] = gmsf
+            if isinstance(gmsf, float) and isinstance(gms, float):
+                forms[form]["graph_vs_fp32"] = gms / gmsf
+            if oracle_res is not None:
+                forms[form]["rel_l2_vs_fp64"] = _fwdbwd_errors(x, h, up, down, form, oracle_res, conv)
+        res[key]["forms"] = forms
     return {"metric": "FIR GMAC/s (resample_poly fp32 forward + backward, dL/dx and dL/dh)",
             "value": total_macs / (total_ms * 1e-3) / 1e9, "unit": "GMAC/s", "n_gpus": world, "steps": steps,
             "warmup": args.warmup, "ms_per_step": total_ms, "higher_is_better": True, "scaling": "weak",

@@ -246,6 +246,15 @@ GBFIR_API int gbfir_conv1d_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_b
                      gbfir_buf h, int32_t mode, void *workspace,
                      size_t workspace_bytes, gbfir_stream_t stream);
 
+/* gbfir_conv1d_bwd with a choice of arithmetic: precision != FP32 computes dx on the tensor
+ * cores (the forward Toeplitz-MMA pass over gy with the taps reversed; NOT_SUPPORTED where no
+ * tile fits) and dh as the tensor-core GEMM over the signal rows described for
+ * gbfir_resample_poly_bwd_prec (the FP32 reduction where its tile does not fit).  Other
+ * arguments and results are those of gbfir_conv1d_bwd. */
+GBFIR_API int gbfir_conv1d_bwd_prec(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x,
+                                    gbfir_buf h, int32_t mode, int32_t precision, void *workspace,
+                                    size_t workspace_bytes, gbfir_stream_t stream);
+
 /* gbfir_resample_poly_bwd with a choice of arithmetic: precision != FP32 computes dx on the
  * tensor cores as a Toeplitz MMA pass over gy (the transposed resampler, taps reversed,
  * rates swapped; same coverage rules as the forward forms, NOT_SUPPORTED otherwise), and dh

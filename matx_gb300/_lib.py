@@ -73,6 +73,7 @@ SIGNATURES = [
     ("gbfir_resample_poly_bwd_noalloc", ctypes.c_int, [_B, _B, _B, _B, _B, _i64, _i64, _p]),
     ("gbfir_conv1d_bwd_workspace_size", _sz, [_i64, _i64, _i64, _i32]),
     ("gbfir_conv1d_bwd", ctypes.c_int, [_B, _B, _B, _B, _B, _i32, _p, _sz, _p]),
+    ("gbfir_conv1d_bwd_prec", ctypes.c_int, [_B, _B, _B, _B, _B, _i32, _i32, _p, _sz, _p]),
     ("gbfir_ragged_workspace_size", _sz, [_i64, _i64]),
     ("gbfir_ragged_plan", _i64, [_p, _i64, _p, _p]),
     ("gbfir_ragged_plan_prec", _i64, [_p, _i64, _i32, _p, _p]),

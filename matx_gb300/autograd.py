@@ -2,7 +2,7 @@
 
 ``resample_poly(x, h, up, down)`` and ``conv1d(x, h, mode)`` here are
 torch.autograd.Function wrappers over the forward kernels and the hand-written
-adjoints of libgbfir (gbfir_resample_poly_bwd / gbfir_conv1d_bwd):
+adjoints of libgbfir (gbfir_resample_poly_bwd_prec / gbfir_conv1d_bwd_prec):
 
   dL/dx = the transposed resampler applied to dL/dy (correlation with the taps,
           up and down swapped; for conv1d, corr(dL/dy, h) cropped to the signal),
@@ -64,8 +64,12 @@ def resample_poly_bwd(gy: torch.Tensor, x: torch.Tensor, h: torch.Tensor, up: in
 
 
 def conv1d_bwd(gy: torch.Tensor, x: torch.Tensor, h: torch.Tensor, mode, need_dx: bool = True,
-               need_dh: bool = True):
-    """(dx, dh) of y = conv1d(x, h, mode) for upstream gradient gy."""
+               need_dh: bool = True, precision="fp32"):
+    """(dx, dh) of y = conv1d(x, h, mode) for upstream gradient gy.
+
+    ``precision`` other than "fp32" computes dx (the reversed-tap Toeplitz MMA pass over gy)
+    and dh (the GEMM over the signal rows) on the tensor cores.
+    """
     lib = _lib.load()
     m = _mode(mode)
     gy = gy.contiguous()
@@ -76,9 +80,9 @@ def conv1d_bwd(gy: torch.Tensor, x: torch.Tensor, h: torch.Tensor, mode, need_dx
     B = x.numel() // x.shape[-1]
     nb = lib.gbfir_conv1d_bwd_workspace_size(B, x.shape[-1], h.shape[-1], m)
     ws = _workspace(nb, x.device)
-    _lib.check(lib.gbfir_conv1d_bwd(
+    _lib.check(lib.gbfir_conv1d_bwd_prec(
         _buf(dx, "dx") if need_dx else _null_buf(), _buf(dh, "dh") if need_dh else _null_buf(),
-        _buf(gy, "gy"), _buf(x, "x"), _buf(h, "h"), m,
+        _buf(gy, "gy"), _buf(x, "x"), _buf(h, "h"), m, _prec(precision),
         ctypes.c_void_p(ws.data_ptr()), ws.numel(), _stream()))
     return dx, dh
 
@@ -100,16 +104,17 @@ class ResamplePolyFn(torch.autograd.Function):
 
 class Conv1dFn(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, x, h, mode):
+    def forward(ctx, x, h, mode, precision="fp32"):
         ctx.save_for_backward(x, h)
-        ctx.mode = _mode(mode)
-        return _conv1d_fwd(x, h, mode)
+        ctx.mode, ctx.precision = _mode(mode), precision
+        return _conv1d_fwd(x, h, mode, precision=precision)
 
     @staticmethod
     def backward(ctx, gy):
         x, h = ctx.saved_tensors
-        dx, dh = conv1d_bwd(gy, x, h, ctx.mode, ctx.needs_input_grad[0], ctx.needs_input_grad[1])
-        return dx, dh, None
+        dx, dh = conv1d_bwd(gy, x, h, ctx.mode, ctx.needs_input_grad[0], ctx.needs_input_grad[1],
+                            precision=ctx.precision)
+        return dx, dh, None, None
 
 
 def resample_poly(x: torch.Tensor, h: torch.Tensor, up: int, down: int, precision="fp32") -> torch.Tensor:
@@ -119,7 +124,8 @@ def resample_poly(x: torch.Tensor, h: torch.Tensor, up: int, down: int, precisio
     return ResamplePolyFn.apply(x, h, up, down, precision)
 
 
-def conv1d(x: torch.Tensor, h: torch.Tensor, mode=0) -> torch.Tensor:
+def conv1d(x: torch.Tensor, h: torch.Tensor, mode=0, precision="fp32") -> torch.Tensor:
+    """Differentiable conv1d; ``precision`` selects the forward, dL/dx and dL/dh arithmetic."""
     if x.dtype != torch.float32 or h.dtype != torch.float32 or h.dim() != 1:
         raise TypeError("matx_gb300.autograd.conv1d: real float32 x and a 1-D float32 filter")
-    return Conv1dFn.apply(x, h, mode)
+    return Conv1dFn.apply(x, h, mode, precision)

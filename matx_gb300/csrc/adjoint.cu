@@ -413,6 +413,8 @@ int adjoint_rowtile_status() { return rowtile_status_take(); }
 using namespace gbfir;
 
 namespace gbfir {
+int conv1d_bwd_dx_tc(const gbfir_buf &dx, const gbfir_buf &gy, const gbfir_buf &h, int64_t start, int precision,
+                     cudaStream_t s);
 int resample_poly_bwd_dx_tc(const gbfir_buf &dx, const gbfir_buf &gy, const gbfir_buf &h, int64_t up, int64_t down,
                             int precision, cudaStream_t s);
 }  // namespace gbfir
@@ -590,8 +592,8 @@ size_t gbfir_conv1d_bwd_workspace_size(int64_t batch, int64_t in_len, int64_t h_
   return (size_t)max_parts() * (size_t)h_len * sizeof(double);
 }
 
-int gbfir_conv1d_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x, gbfir_buf h, int32_t mode,
-                     void *workspace, size_t workspace_bytes, gbfir_stream_t stream) {
+static int conv_bwd_impl(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x, gbfir_buf h, int32_t mode,
+                         int32_t precision, void *workspace, size_t workspace_bytes, gbfir_stream_t stream) {
   try {
     int rc;
     if ((rc = check_real(gy, "conv1d_bwd gy", false))) return rc;
@@ -616,7 +618,10 @@ int gbfir_conv1d_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x, gbfi
     const int64_t start = mode == GBFIR_MODE_SAME ? ((mn & 1) ? (mn - 1) / 2 : mn / 2 - 1)
                         : mode == GBFIR_MODE_VALID ? mn - 1 : 0;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    if (dx.ptr) {
+    if (dx.ptr && precision != GBFIR_PREC_FP32) {
+      rc = conv1d_bwd_dx_tc(dx, gy, h, start, precision, s);
+      if (rc) return rc;
+    } else if (dx.ptr) {
       TileChoice tc;
       rc = resample_pass<float, false, false>(gy.ptr, gy.batch_stride, gy.len, h.ptr, L, dx.ptr, dx.batch_stride, N,
                                               x.batch, 1, 1, L - 1 - start, false, 1, 1.0, tc, s);
@@ -625,12 +630,24 @@ int gbfir_conv1d_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x, gbfi
     if (dh.ptr) {
       DhPlan pl = plan_dh((const float *)x.ptr, x.batch_stride, N, (const float *)gy.ptr, gy.batch_stride, gy.len,
                           x.batch, L, 1, 1, start, false);
-      return run_dh(pl, x.batch, L, 0, 1.0, (float *)dh.ptr, workspace, workspace_bytes, s);
+      return run_dh_prec(pl, precision, x.batch, L, 0, 1.0, (float *)dh.ptr, workspace, workspace_bytes, s);
     }
     return GBFIR_SUCCESS;
   } catch (...) {
     GBFIR_FAIL(GBFIR_ERR_CUDA, "conv1d_bwd: internal exception");
   }
+}
+
+int gbfir_conv1d_bwd(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x, gbfir_buf h, int32_t mode,
+                     void *workspace, size_t workspace_bytes, gbfir_stream_t stream) {
+  return conv_bwd_impl(dx, dh, gy, x, h, mode, GBFIR_PREC_FP32, workspace, workspace_bytes, stream);
+}
+
+int gbfir_conv1d_bwd_prec(gbfir_buf dx, gbfir_buf dh, gbfir_buf gy, gbfir_buf x, gbfir_buf h, int32_t mode,
+                          int32_t precision, void *workspace, size_t workspace_bytes, gbfir_stream_t stream) {
+  if (precision < GBFIR_PREC_FP32 || precision > GBFIR_PREC_BF16X3)
+    GBFIR_FAIL(GBFIR_ERR_INVALID_PARAMETER, "conv1d_bwd: unknown precision %d", (int)precision);
+  return conv_bwd_impl(dx, dh, gy, x, h, mode, precision, workspace, workspace_bytes, stream);
 }
 
 }  // extern "C"

@@ -929,6 +929,22 @@ int conv1d_tc(const gbfir_buf &out, const gbfir_buf &in, const gbfir_buf &h, int
   return launch_tc(pl, out, in, h, xc, "conv1d (tensor cores)", s);
 }
 
+// dL/dx of conv1d on the tensor cores: dx[i] = sum_n gy[n] * h[start + n - i] is the forward
+// pass over gy with the taps read reversed about the centre L - 1 - start (the FP32 adjoint
+// runs the same pass on the CUDA cores).  Real float32 operands.
+int conv1d_bwd_dx_tc(const gbfir_buf &dx, const gbfir_buf &gy, const gbfir_buf &h, int64_t start, int precision,
+                     cudaStream_t s) {
+  TcTaps t{};
+  t.Lo = h.len;
+  t.even = 0;
+  t.rev = 1;
+  t.scale = 1.0;
+  t.c = h.len - 1 - start;
+  TcPlan pl = plan_tc_rows(1, 1, t, gy.len, dx.len, dx.batch, 0, precision, tc_rows_pref());
+  if (!pl.ok) GBFIR_FAIL(GBFIR_ERR_NOT_SUPPORTED, "conv1d_bwd: tensor-core dx unavailable: %s", pl.why);
+  return launch_tc(pl, dx, gy, h, false, "conv1d_bwd dx (tensor cores)", s);
+}
+
 // dL/dx of resample_poly on the tensor cores: the transposed resampler
 //   dx[m] = up * sum_k gy[k] * he(Lo - 1 - (c + m*up - k*down))
 // is the forward pass with the rates swapped and the taps read reversed (the FP32 adjoint

@@ -93,3 +93,43 @@ def test_tc_fwd_bwd_autograd_bf16x3(ag, orc):
     assert rel_l2(h.grad.cpu().numpy(), rdh) < 1e-6
     ry = orc.resample_poly(xs[rows], hs, 3, 2)
     assert rel_l2(y[rows].detach().cpu().numpy(), ry) < 1e-6
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("form", ["bf16x3", "bf16", "fp16"])
+def test_tc_conv_bwd_vs_fp64(ag, orc, mode, form):
+    """conv1d's dL/dx and dL/dh on the tensor cores (gbfir_conv1d_bwd_prec), FULL / SAME / VALID."""
+    import torch
+    rng = np.random.default_rng(17 + mode)
+    B, N, L = 3, 9001, 127
+    x = rng.uniform(-1, 1, (B, N)).astype(np.float32)
+    h = (rng.standard_normal(L) / np.sqrt(L)).astype(np.float32)
+    olen = {0: N + L - 1, 1: N, 2: N - L + 1}[mode]
+    gy = rng.standard_normal((B, olen)).astype(np.float32)
+    dev = lambda a: torch.from_numpy(a).cuda()
+    dx, dh = ag.conv1d_bwd(dev(gy), dev(x), dev(h), mode, precision=form)
+    _, dh2 = ag.conv1d_bwd(dev(gy), dev(x), dev(h), mode, False, True, precision=form)
+    torch.cuda.synchronize()
+    rdx, rdh = orc.conv1d_bwd(gy.astype(np.float64), x.astype(np.float64), h.astype(np.float64), mode)
+    ex, eh = rel_l2(dx.cpu().numpy(), rdx), rel_l2(dh.cpu().numpy(), rdh)
+    assert ex < TOL[form] and eh < TOL[form], (mode, form, ex, eh)
+    assert torch.equal(dh, dh2)
+    if form != "bf16x3":
+        assert ex > 1e-5 and eh > 1e-5, (mode, form, ex, eh)
+
+
+def test_tc_conv_fwd_bwd_autograd_bf16x3(ag, orc):
+    """The differentiable conv1d SAME case (256 x 16384, 127 taps) end to end in bf16x3."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(9)
+    x = (torch.rand(256, 16384, device="cuda", generator=g) * 2 - 1).requires_grad_(True)
+    h = (torch.randn(127, device="cuda", generator=g) / 127 ** 0.5).requires_grad_(True)
+    y = ag.conv1d(x, h, "same", precision="bf16x3")
+    gy = torch.randn(y.shape, device="cuda", generator=g)
+    y.backward(gy)
+    xs, hs, gs = (t.detach().cpu().numpy().astype(np.float64) for t in (x, h, gy))
+    rows = slice(0, 8)
+    rdx, _ = orc.conv1d_bwd(gs[rows], xs[rows], hs, 1)
+    assert rel_l2(x.grad[rows].cpu().numpy(), rdx) < 1e-6
+    _, rdh = orc.conv1d_bwd(gs, xs, hs, 1, nthreads=8)
+    assert rel_l2(h.grad.cpu().numpy(), rdh) < 1e-6
