@@ -19,13 +19,17 @@
 // adds the CTAs' partials in a fixed order.  The result is deterministic.
 //
 // Pipeline (384 threads): warps 1-11 materialise each stage's operands straight from global
-// memory — the X Hankel slab and the GY slab, split into the operand terms, in the
-// no-swizzle K-major layout — into a ring of 2 to 4 slots, each warp arriving on the slot's
-// barrier when its own items are stored (no CTA-wide barrier); warp 0 lane 0 issues the MMAs.  bf16x3
-// keeps the leading product x0*g0 in its own accumulator and the five smaller products in a
-// second one (every MMA costs about one FP32 rounding of its accumulator).  At the end warps
-// 0-3 drain TMEM through shared memory and every thread folds taps.  Every mbarrier wait is
-// bounded: one that gives up sets the status word read by gbfir_tc_status().
+// memory — the X Hankel slab and the GY slab, split into the operand terms — into a ring of
+// 2 to 4 slots, each warp arriving on the slot's barrier when its own items are stored (no
+// CTA-wide barrier); warp 0 lane 0 issues the MMAs.  Stages of 64 rows use the 128-byte
+// swizzled K-major layout (the tensor core reads it at about twice the rate of the
+// no-swizzle layout at N = 128), with the no-swizzle layout and 32- or 16-row stages where
+// those do not fit.  bf16x3 keeps the leading product x0*g0 in its own accumulator (every MMA
+// costs about one FP32 rounding of its accumulator): where two gradient terms fit one MMA
+// (N = 2*NP <= 256) it issues four MMAs a K-step into [x0*g0 | x0*g1 + x1*g0 | x1*g1 + x2*g0
+// + x0*g2] (B = [g0 | g1] for two of them), else six into x0*g0 and the rest.  At the end
+// warps 0-3 drain TMEM through shared memory and every thread folds taps.  Every mbarrier
+// wait is bounded: one that gives up sets the status word read by gbfir_tc_status().
 #include <algorithm>
 
 #include "common.cuh"
@@ -45,7 +49,7 @@ int tc_dh_status_take() {
 constexpr int kTdThreads = 384;
 constexpr int kTdProd0 = 1, kTdProdWarps = 11;
 constexpr int kTdNProd = kTdProdWarps * 32;
-constexpr int kTdBatch = 4;     // producer items whose loads are in flight together
+constexpr int kTdBatch = 8;     // producer items whose loads are in flight together
 constexpr int kTdMaxItems = 8;  // producer items per thread and stage (planner bound)
 constexpr int kTdMaxSlots = 4;  // operand ring slots
 
@@ -58,10 +62,28 @@ struct TdParams {
   int64_t Nt, S;
   int32_t NP, MT, KR, terms, fp16;
   int32_t nslot;  // operand ring slots (2..4)
+  int32_t sw;     // 1: 128-byte-swizzled K-major operands (KR = 64: a row of a tile is 128 bytes)
+  int32_t cat;    // bf16x3 with the gradient terms concatenated along N: 4 MMAs a K-step into
+                  // three accumulators [x0*g0 | x0*g1 + x1*g0 | x1*g1 + x2*g0 + x0*g2]
   int64_t tiles_per_row, ntiles;
   double *partial;  // [gridDim.x][Lo]
 };
 
+
+// Timing hooks of the pipeline roles (role, stage, event); they compile to nothing unless a
+// tracing build defines them.
+#ifndef GBFIR_TC_TRACE
+#define GBFIR_TC_TRACE(role, stage, event) \
+  do {                                     \
+  } while (0)
+#endif
+
+// Byte offset of the 16-byte chunk (row, 8-wide K chunk kc) in a tile of KR-wide K-major rows:
+// the no-swizzle core-matrix layout, or with sw the 128-byte swizzle (rows of 128 bytes, the
+// chunk index XORed with the row's position in its 8-row, 1024-byte group; tiles 1024-aligned).
+__device__ __forceinline__ uint32_t td_chunk_offset(uint32_t row, uint32_t kc, uint32_t KR, bool sw) {
+  return sw ? (row << 7) + ((kc ^ (row & 7u)) << 4) : tc::kmajor_offset(row, 8u * kc, KR);
+}
 
 __global__ void __launch_bounds__(kTdThreads, 1) tc_dh_kernel(const TdParams p) {
   extern __shared__ __align__(1024) unsigned char smem_dyn[];
@@ -69,6 +91,7 @@ __global__ void __launch_bounds__(kTdThreads, 1) tc_dh_kernel(const TdParams p) 
   __shared__ uint32_t tmem_slot;
   __shared__ int s_fail, s_aok;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) GBFIR_TC_TRACE(3, 0, 1);
 
   // ring slot: X tiles [terms][MT][128 x KR] then GY tiles [terms][NP x KR], bf16/fp16
   unsigned char *smem = smem_dyn + ((1024u - (tc::smem_u32(smem_dyn) & 1023u)) & 1023u);
@@ -79,9 +102,9 @@ __global__ void __launch_bounds__(kTdThreads, 1) tc_dh_kernel(const TdParams p) 
   auto bmat = [&](int slot, int t) {
     return smem + slot * slot_bytes + (size_t)p.terms * p.MT * abytes + (size_t)t * bbytes;
   };
-  const bool split = p.terms == 3;
-  const int acc_cols = p.MT * p.NP;  // M-tile mt in columns [mt*NP, mt*NP + NP)
-  const int need = split ? 2 * acc_cols : acc_cols;
+  const bool split = p.terms == 3 && !p.cat;
+  const int acc_cols = p.MT * p.NP;  // M-tile mt in columns [mt*NP, mt*NP + NP) (cat: [mt*3*NP, +3*NP))
+  const int need = p.cat ? 3 * acc_cols : split ? 2 * acc_cols : acc_cols;
   const uint32_t tcols = need <= 32 ? 32u : need <= 64 ? 64u : need <= 128 ? 128u : need <= 256 ? 256u : 512u;
   if (warp == 0) tc::tmem_alloc(&tmem_slot, tcols);
   if (tid == 0) {
@@ -119,25 +142,27 @@ __global__ void __launch_bounds__(kTdThreads, 1) tc_dh_kernel(const TdParams p) 
       if (itm < nA) {
         const int kc = itm / mrows, m = itm - kc * mrows;
         it_g[j] = 8 * kc * Si + m;
-        it_s[j] = (uint32_t)(m >> 7) * abytes + tc::kmajor_offset((uint32_t)(m & 127), 8u * kc, (uint32_t)KR);
+        it_s[j] = (uint32_t)(m >> 7) * abytes + td_chunk_offset((uint32_t)(m & 127), (uint32_t)kc, (uint32_t)KR, p.sw);
       } else if (itm < nitems) {
         const int i2 = itm - nA;
         const int kc = i2 / p.NP, n = i2 - kc * p.NP;
         it_g[j] = 8 * kc * Nti + n;
         it_s[j] = (1u << 31) | (n < Nti ? 0u : 1u << 30) |
-                  ((uint32_t)p.terms * p.MT * abytes + tc::kmajor_offset((uint32_t)n, 8u * kc, (uint32_t)KR));
+                  ((uint32_t)p.terms * p.MT * abytes + td_chunk_offset((uint32_t)n, (uint32_t)kc, (uint32_t)KR, p.sw));
       }
     }
     const uint32_t tstride_a = (uint32_t)p.MT * abytes;
     for (int64_t i = 0; i < my_tiles; ++i) {
       const int slot = (int)(i % p.nslot);
       const int64_t round = i / p.nslot;
+      if (ptid == 0) GBFIR_TC_TRACE(0, (int)i, 0);
       int ok = 1;
       if (lane == 0 && round > 0) ok = tc::mbar_wait(&op_empty[slot], (uint32_t)((round - 1) & 1)) ? 1 : 0;
       if (!__shfl_sync(0xffffffffu, ok, 0)) {
         s_fail = 1;
         break;
       }
+      if (ptid == 0) GBFIR_TC_TRACE(0, (int)i, 1);
       const int64_t t = blockIdx.x + i * (int64_t)gridDim.x;
       const int64_t b = t / p.tiles_per_row;
       const int64_t q0 = (t - b * p.tiles_per_row) * KR;
@@ -215,47 +240,80 @@ __global__ void __launch_bounds__(kTdThreads, 1) tc_dh_kernel(const TdParams p) 
       tc::fence_async_smem();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive_plain(&op_full[slot]);
+      if (ptid == 0) GBFIR_TC_TRACE(0, (int)i, 2);
     }
   } else if (lane == 0) {
     // ================= MMA issuer (warp 0, one thread) =================
     const uint32_t idesc = tc::idesc_f16(128, (uint32_t)p.NP, p.fp16 ? 0u : 1u);
+    const uint32_t idesc2 = tc::idesc_f16(128, 2u * (uint32_t)p.NP, 1u);
     const uint32_t sbo = (uint32_t)(KR / 8) * 128u;
+    // no swizzle: K-adjacent core matrices 128 bytes apart, row groups sbo apart; 128-byte
+    // swizzle (layout type 2): row groups 1024 bytes apart, K-step s starting 32*s bytes in
+    auto desc = [&](const unsigned char *tile) -> uint64_t {
+      return p.sw ? (tc::smem_desc(tc::smem_u32(tile), 16u, 1024u) | ((uint64_t)2 << 61))
+                  : tc::smem_desc(tc::smem_u32(tile), 128u, sbo);
+    };
+    const uint64_t kstep = p.sw ? 2 : 16;  // in 16-byte units
     // products of order <= 2 (signal term tx, gradient term tg), smallest first; the last,
     // x0*g0, goes to the leading accumulator
     constexpr uint32_t kTx = 0x001021u, kTg = 0x010201u;
     const int npairs = split ? 6 : 1;
     for (int64_t i = 0; i < my_tiles; ++i) {
       const int slot = (int)(i % p.nslot);
+      GBFIR_TC_TRACE(1, (int)i, 0);
       if (!tc::mbar_wait(&op_full[slot], (uint32_t)((i / p.nslot) & 1))) {
         s_fail = 1;
         break;
       }
+      GBFIR_TC_TRACE(1, (int)i, 1);
       tc::tc_fence_after();
-      for (int mt = 0; mt < p.MT; mt++) {
+      for (int mt = 0; p.cat && mt < p.MT; mt++) {
+        // C2 is initialised first (x0*g2), so the x1*[g0|g1] MMA, which spans C1 and C2, only
+        // ever accumulates; B = [g0 | g1] is the two term tiles back to back (N = 2*NP)
+        const uint32_t L = tmem + (uint32_t)(mt * 3 * p.NP), C1 = L + (uint32_t)p.NP, C2 = L + 2u * p.NP;
+        uint64_t a0 = desc(amat(slot, mt, 0)), a1 = desc(amat(slot, mt, 1)), a2 = desc(amat(slot, mt, 2));
+        uint64_t g01 = desc(bmat(slot, 0)), g2 = desc(bmat(slot, 2));
+        for (int ks = 0; ks < KR / 16; ks++) {
+          const uint32_t acc = (i > 0 || ks > 0) ? 1u : 0u;
+          tc::mma_f16(C2, a0, g2, idesc, acc);
+          tc::mma_f16(C2, a2, g01, idesc, 1u);
+          tc::mma_f16(L, a0, g01, idesc2, acc);
+          tc::mma_f16(C1, a1, g01, idesc2, 1u);
+          a0 += kstep;
+          a1 += kstep;
+          a2 += kstep;
+          g01 += kstep;
+          g2 += kstep;
+        }
+      }
+      for (int mt = 0; !p.cat && mt < p.MT; mt++) {
         for (int pr = 0; pr < npairs; pr++) {
           const int tx = split ? (int)((kTx >> (4 * pr)) & 15u) : 0;
           const int tg = split ? (int)((kTg >> (4 * pr)) & 15u) : 0;
           const bool lead = pr == npairs - 1;
           const uint32_t d = tmem + (uint32_t)(mt * p.NP) + (split && !lead ? (uint32_t)acc_cols : 0u);
           const bool first_pair = lead || pr == 0;
-          uint64_t ad = tc::smem_desc(tc::smem_u32(amat(slot, mt, tx)), 128u, sbo);
-          uint64_t bd = tc::smem_desc(tc::smem_u32(bmat(slot, tg)), 128u, sbo);
+          uint64_t ad = desc(amat(slot, mt, tx));
+          uint64_t bd = desc(bmat(slot, tg));
           for (int ks = 0; ks < KR / 16; ks++) {
             tc::mma_f16(d, ad, bd, idesc, (i > 0 || !first_pair || ks > 0) ? 1u : 0u);
-            ad += 16;  // +256 B: two core matrices along K
-            bd += 16;
+            ad += kstep;
+            bd += kstep;
           }
         }
       }
       tc::mma_commit(&op_empty[slot]);
+      GBFIR_TC_TRACE(1, (int)i, 2);
     }
     // arrives once every MMA issued above has completed (at once if there were none)
     tc::mma_commit(&acc_full);
   }
 
   // ================= drain and fold =================
+  if (tid == 0) GBFIR_TC_TRACE(2, 0, 0);
   if (tid == 0) s_aok = tc::mbar_wait(&acc_full, 0u) ? 1 : 0;
   __syncthreads();
+  if (tid == 0) GBFIR_TC_TRACE(2, 0, 1);
   const bool have = my_tiles > 0 && s_aok && !s_fail;
   const int sstride = p.NP + 4;
   float *stage = reinterpret_cast<float *>(smem);  // [MT*128][NP + 4] FP32, over the idle ring
@@ -265,11 +323,22 @@ __global__ void __launch_bounds__(kTdThreads, 1) tc_dh_kernel(const TdParams p) 
     for (int mt = 0; mt < p.MT; mt++) {
       float *srow = stage + (size_t)(mt * 128 + 32 * warp + lane) * sstride;
       for (int col = 0; col < p.NP; col += 16) {
-        uint32_t r[16], rc[16];
-        tc::tmem_ld16(tmem + lane_base + (uint32_t)(mt * p.NP + col), r);
-        if (split) tc::tmem_ld16(tmem + lane_base + (uint32_t)(acc_cols + mt * p.NP + col), rc);
+        uint32_t r[16], rc[16], rd[16];
+        if (p.cat) {
+          const uint32_t base = lane_base + (uint32_t)(mt * 3 * p.NP + col);
+          tc::tmem_ld16(tmem + base, r);
+          tc::tmem_ld16(tmem + base + (uint32_t)p.NP, rc);
+          tc::tmem_ld16(tmem + base + 2u * p.NP, rd);
+        } else {
+          tc::tmem_ld16(tmem + lane_base + (uint32_t)(mt * p.NP + col), r);
+          if (split) tc::tmem_ld16(tmem + lane_base + (uint32_t)(acc_cols + mt * p.NP + col), rc);
+        }
         tc::tmem_ld_wait();
-        if (split) {
+        if (p.cat) {
+#pragma unroll
+          for (int q = 0; q < 16; q++)
+            r[q] = __float_as_uint(__uint_as_float(r[q]) + (__uint_as_float(rc[q]) + __uint_as_float(rd[q])));
+        } else if (split) {
 #pragma unroll
           for (int q = 0; q < 16; q++) r[q] = __float_as_uint(__uint_as_float(r[q]) + __uint_as_float(rc[q]));
         }
@@ -291,13 +360,16 @@ __global__ void __launch_bounds__(kTdThreads, 1) tc_dh_kernel(const TdParams p) 
     if (have) {
       int64_t res = (tp - p.c) % p.up;
       if (res < 0) res += p.up;
-      for (int64_t j = (res * p.inv_down) % p.up; j < p.Nt; j += p.up) {
-        const int64_t k = (p.c + j * p.down - tp) / p.up - p.kmin;
+      const int j0 = (int)((res * p.inv_down) % p.up);
+      // along the phases j0, j0 + up, ... the input position k steps by down
+      int k = (int)((p.c + j0 * p.down - tp) / p.up - p.kmin);
+      const int Nti = (int)p.Nt, upi = (int)p.up, dni = (int)p.down;
+      for (int j = j0; j < Nti; j += upi, k += dni)
         if (k >= 0 && k < mrows) s += (double)stage[(size_t)k * sstride + j];
-      }
     }
     part[tp] = s;
   }
+  if (tid == 0) GBFIR_TC_TRACE(2, 0, 2);
   if ((s_fail || !s_aok) && tid == 0 && my_tiles > 0) atomicExch(&g_tcd_status, 1);
   tc::tc_fence_before();
   __syncthreads();
@@ -364,8 +436,20 @@ static TdPlan plan_tc_dh(int64_t up, int64_t down, int64_t Lo, int64_t c, int64_
   // up to three stages ahead of the MMAs), else 64 or 16 rows in at least two; each producer
   // thread has at most kTdMaxItems items (8-row chunks of an X row or a GY phase) per stage
   auto items = [&](int kr) { return ((int64_t)p.MT * 128 + p.NP) * (kr / 8); };
+  // 64-row stages in the 128-byte-swizzled layout where two slots fit (the tensor core reads
+  // those operands faster than the no-swizzle ones), else the no-swizzle layout
   p.KR = 0;
+  p.sw = 0;
+  {
+    const int ns = (int)std::min<size_t>(kTdMaxSlots, budget / slot_bytes(p.MT, p.NP, 64));
+    if (ns >= 2 && items(64) <= (int64_t)kTdMaxItems * kTdNProd) {
+      p.KR = 64;
+      p.nslot = ns;
+      p.sw = 1;
+    }
+  }
   for (int kr : {32, 64, 16}) {
+    if (p.KR) break;
     const int ns = (int)std::min<size_t>(kTdMaxSlots, budget / slot_bytes(p.MT, p.NP, kr));
     if (ns >= 2 && items(kr) <= (int64_t)kTdMaxItems * kTdNProd) {
       p.KR = kr;
@@ -374,6 +458,7 @@ static TdPlan plan_tc_dh(int64_t up, int64_t down, int64_t Lo, int64_t c, int64_
     }
   }
   if (p.KR == 0) return pl;
+  p.cat = (p.terms == 3 && 2 * p.NP <= 256 && 3 * p.MT * p.NP <= 512) ? 1 : 0;
   const size_t ring = (size_t)p.nslot * slot_bytes(p.MT, p.NP, p.KR);
   const size_t staging = (size_t)p.MT * 128 * (p.NP + 4) * 4;
   pl.smem = 1024 + std::max(ring, staging);
