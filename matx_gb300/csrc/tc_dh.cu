@@ -28,7 +28,7 @@
 // costs about one FP32 rounding of its accumulator): where two gradient terms fit one MMA
 // (N = 2*NP <= 256) it issues four MMAs a K-step into [x0*g0 | x0*g1 + x1*g0 | x1*g1 + x2*g0
 // + x0*g2] (B = [g0 | g1] for two of them), else six into x0*g0 and the rest.  At the end
-// warps 0-3 drain TMEM through shared memory and every thread folds taps.  Every mbarrier
+// every warp drains part of TMEM through shared memory and every thread folds taps.  Every mbarrier
 // wait is bounded: one that gives up sets the status word read by gbfir_tc_status().
 #include <algorithm>
 
@@ -63,6 +63,7 @@ struct TdParams {
   int32_t NP, MT, KR, terms, fp16;
   int32_t nslot;  // operand ring slots (2..4)
   int32_t sw;     // 1: 128-byte-swizzled K-major operands (KR = 64: a row of a tile is 128 bytes)
+  int32_t nsub, fold_off;  // threads per tap in the fold; byte offset of its FP64 sums
   int32_t cat;    // bf16x3 with the gradient terms concatenated along N: 4 MMAs a K-step into
                   // three accumulators [x0*g0 | x0*g1 + x1*g0 | x1*g1 + x2*g0 + x0*g2]
   int64_t tiles_per_row, ntiles;
@@ -318,11 +319,13 @@ __global__ void __launch_bounds__(kTdThreads, 1) tc_dh_kernel(const TdParams p) 
   const int sstride = p.NP + 4;
   float *stage = reinterpret_cast<float *>(smem);  // [MT*128][NP + 4] FP32, over the idle ring
   tc::tc_fence_after();
-  if (have && warp < 4) {
-    const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+  if (have) {
+    // every warp drains: warp w reads TMEM lane quarter w % 4, column chunks w / 4, + 3, ...
+    const int quarter = warp & 3, cset = warp >> 2;
+    const uint32_t lane_base = (uint32_t)(32 * quarter) << 16;
     for (int mt = 0; mt < p.MT; mt++) {
-      float *srow = stage + (size_t)(mt * 128 + 32 * warp + lane) * sstride;
-      for (int col = 0; col < p.NP; col += 16) {
+      float *srow = stage + (size_t)(mt * 128 + 32 * quarter + lane) * sstride;
+      for (int col = 16 * cset; col < p.NP; col += 16 * (kTdThreads / 128)) {
         uint32_t r[16], rc[16], rd[16];
         if (p.cat) {
           const uint32_t base = lane_base + (uint32_t)(mt * 3 * p.NP + col);
@@ -351,23 +354,49 @@ __global__ void __launch_bounds__(kTdThreads, 1) tc_dh_kernel(const TdParams p) 
   }
   tc::tc_fence_before();
   __syncthreads();
+  if (tid == 0) GBFIR_TC_TRACE(2, 1, 0);
   // tap t collects dB[k][j] over the phases j = j0, j0 + up, ... (j*down = t - c mod up),
-  // k = (c + j*down - t)/up - kmin, in increasing j: a fixed order
+  // k = (c + j*down - t)/up - kmin.  With nsub > 1 threads per tap (few taps), thread sub
+  // sums the phases j0 + up*(sub + nsub*m) in increasing m, and the nsub sums are added in
+  // sub order: a fixed order either way.  A thread's sum is compensated FP32 (Kahan: the
+  // rounding error of each addition carried into the next), as exact as an FP64 sum of these
+  // few FP32 terms while staying off the FP64 pipe; the sums are combined in FP64.
   double *part = p.partial + (size_t)blockIdx.x * p.Lo;
   const int mrows = p.MT * 128;
-  for (int64_t tp = tid; tp < p.Lo; tp += kTdThreads) {
+  const int nsub = p.nsub;
+  double *fsum = reinterpret_cast<double *>(smem + p.fold_off);  // [Lo][nsub] when nsub > 1
+  for (int64_t e = tid; e < p.Lo * nsub; e += kTdThreads) {
+    const int64_t tp = e / nsub;
+    const int sub = (int)(e - tp * nsub);
     double s = 0.0;
     if (have) {
       int64_t res = (tp - p.c) % p.up;
       if (res < 0) res += p.up;
       const int j0 = (int)((res * p.inv_down) % p.up);
       // along the phases j0, j0 + up, ... the input position k steps by down
-      int k = (int)((p.c + j0 * p.down - tp) / p.up - p.kmin);
-      const int Nti = (int)p.Nt, upi = (int)p.up, dni = (int)p.down;
-      for (int j = j0; j < Nti; j += upi, k += dni)
-        if (k >= 0 && k < mrows) s += (double)stage[(size_t)k * sstride + j];
+      int k = (int)((p.c + j0 * p.down - tp) / p.up - p.kmin) + sub * (int)p.down;
+      const int Nti = (int)p.Nt, ustep = (int)p.up * nsub, dstep = (int)p.down * nsub;
+      float sf = 0.f, cf = 0.f;
+      for (int j = j0 + sub * (int)p.up; j < Nti; j += ustep, k += dstep) {
+        if (k >= 0 && k < mrows) {
+          const float y = __fsub_rn(stage[(size_t)k * sstride + j], cf);
+          const float t = __fadd_rn(sf, y);
+          cf = __fsub_rn(__fsub_rn(t, sf), y);
+          sf = t;
+        }
+      }
+      s = (double)sf - (double)cf;
     }
-    part[tp] = s;
+    if (nsub == 1) part[tp] = s;
+    else fsum[e] = s;
+  }
+  if (nsub > 1) {
+    __syncthreads();
+    for (int64_t tp = tid; tp < p.Lo; tp += kTdThreads) {
+      double s = fsum[tp * nsub];
+      for (int sub = 1; sub < nsub; sub++) s += fsum[tp * nsub + sub];
+      part[tp] = s;
+    }
   }
   if (tid == 0) GBFIR_TC_TRACE(2, 0, 2);
   if ((s_fail || !s_aok) && tid == 0 && my_tiles > 0) atomicExch(&g_tcd_status, 1);
@@ -461,7 +490,11 @@ static TdPlan plan_tc_dh(int64_t up, int64_t down, int64_t Lo, int64_t c, int64_
   p.cat = (p.terms == 3 && 2 * p.NP <= 256 && 3 * p.MT * p.NP <= 512) ? 1 : 0;
   const size_t ring = (size_t)p.nslot * slot_bytes(p.MT, p.NP, p.KR);
   const size_t staging = (size_t)p.MT * 128 * (p.NP + 4) * 4;
-  pl.smem = 1024 + std::max(ring, staging);
+  // the fold: up to four threads per tap where taps are few, their FP64 sums after the staging
+  p.nsub = Lo >= kTdThreads ? 1 : (int32_t)std::min<int64_t>(4, kTdThreads / Lo);
+  p.fold_off = (int32_t)((staging + 15) / 16 * 16);
+  const size_t fold = p.nsub > 1 ? (size_t)p.fold_off + (size_t)Lo * p.nsub * 8 : staging;
+  pl.smem = 1024 + std::max(ring, fold);
   const int64_t rows = (out_len + p.Nt - 1) / p.Nt;
   p.tiles_per_row = (rows + p.KR - 1) / p.KR;
   p.ntiles = p.tiles_per_row * batch;
