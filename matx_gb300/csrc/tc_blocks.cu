@@ -222,7 +222,9 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_blocks_kernel(const TbParams
     }
     __syncthreads();
     if (s_item < 0 || s_fail) break;
-    const TbGeom &g = sg;
+    // a private copy: read through the shared struct, every field would be reloaded after each
+    // store the compiler cannot prove does not alias it (a dependent shared load per element)
+    const TbGeom g = sg;
     const int64_t row0 = s_row0, ntl = s_ntiles;
     if (g.identity) {
       // rates that reduce to 1/1: MatX's resample_poly copies the input (the taps are ignored);
@@ -477,20 +479,27 @@ __global__ void __launch_bounds__(kTbThreads, 1) tc_blocks_kernel(const TbParams
         tc::tc_fence_before();
         tb_sync(2, 128);
         if (quarter == 0 && lane == 0) tc::mbar_arrive_plain(&tm_empty[set]);
+        if (quarter == 0 && lane == 0) GBFIR_TC_TRACE(2, (int)e, 3);
         // whole outputs, a warp per row at a time: lanes take consecutive phases (coalesced)
         int64_t bb, q0;
         tile_of(i, bb, q0);
         XT *orow = reinterpret_cast<XT *>(g.out) + bb * g.out_bstride;
         const int64_t j0 = (int64_t)b * g.NB;
+        // the row's valid phases of this block, worked out once per row; the loop body is two
+        // shared loads and one store, two phases a lane in flight
+        const int64_t cols = std::min<int64_t>(g.NB, g.Nt - j0);
         for (int q = quarter; q < p.RT; q += 4) {
           const int64_t n0 = (q0 + q) * g.Nt + j0;
-          for (int n = lane; n < g.NB; n += 32) {
-            if (j0 + n >= g.Nt || n0 + n >= g.out_len) continue;
-            if constexpr (XC) {
-              orow[n0 + n] = make_float2(stage[(size_t)q * sstride + n], stage[(size_t)(64 + q) * sstride + n]);
-            } else {
-              orow[n0 + n] = stage[(size_t)q * sstride + n];
-            }
+          const int lim = (int)std::max<int64_t>(0, std::min<int64_t>(cols, g.out_len - n0));
+          const float *sr = stage + (size_t)q * sstride;
+          XT *dst = orow + n0;
+          if constexpr (XC) {
+            const float *si = stage + (size_t)(64 + q) * sstride;
+#pragma unroll 2
+            for (int n = lane; n < lim; n += 32) dst[n] = make_float2(sr[n], si[n]);
+          } else {
+#pragma unroll 2
+            for (int n = lane; n < lim; n += 32) dst[n] = sr[n];
           }
         }
         tb_sync(2, 128);  // the staging tile is read before the next stage overwrites it
