@@ -265,7 +265,9 @@ __global__ void __launch_bounds__(kRgThreads) ragged_rowtile(const RgParams rp) 
       }
     }
     __syncthreads();
-    const RsParams &p = s_p;
+    // a private copy: read through the shared struct, the fields would be reloaded after every
+    // store the compiler cannot prove does not alias it
+    const RsParams p = s_p;
     if (s_identity) {
       const float2 *xi = reinterpret_cast<const float2 *>(d.in);
       float2 *yo = reinterpret_cast<float2 *>(d.out);
