@@ -34,10 +34,18 @@ struct DhParams {
   int32_t QC, win, win_alloc;
   int32_t U, RS;      // work units (g, 4 k) and row slices
   int64_t G, inv_down;
+  int32_t gal;        // 1: gradient rows 16-byte aligned (16-byte tile copies)
   double *partial;    // [gridDim.x][Lo]
 };
 
 constexpr int kDhThreads = 256;
+
+// Timing hooks (role, stage, event); they compile to nothing unless a tracing build defines them.
+#ifndef GBFIR_TC_TRACE
+#define GBFIR_TC_TRACE(role, stage, event) \
+  do {                                     \
+  } while (0)
+#endif
 
 template <bool PAD, int UPT>
 __global__ void __launch_bounds__(kDhThreads) rowtile_dh(const DhParams p) {
@@ -56,17 +64,29 @@ __global__ void __launch_bounds__(kDhThreads) rowtile_dh(const DhParams p) {
     const int64_t q0 = (tile - b * p.tiles_per_row) * p.QC;
     const float *xr = p.x + b * p.x_bstride;
     const int64_t xs0 = q0 * p.S + p.kmin;
-    for (int e = tid; e < p.win; e += kDhThreads) {
-      const int64_t gi = xs0 + e;
-      const bool ok = gi >= 0 && gi < p.N;
-      cp_async_zfill<4>(&xb[smem_idx<PAD ? 4 : 0>(e)], ok ? (const void *)(xr + gi) : (const void *)xr, ok);
+    if (xs0 >= 0 && xs0 + p.win <= p.N) {
+      // interior window: no range checks
+      const float *src = xr + xs0;
+      for (int e = tid; e < p.win; e += kDhThreads) cp_async_zfill<4>(&xb[smem_idx<PAD ? 4 : 0>(e)], src + e, true);
+    } else {
+      for (int e = tid; e < p.win; e += kDhThreads) {
+        const int64_t gi = xs0 + e;
+        const bool ok = gi >= 0 && gi < p.N;
+        cp_async_zfill<4>(&xb[smem_idx<PAD ? 4 : 0>(e)], ok ? (const void *)(xr + gi) : (const void *)xr, ok);
+      }
     }
     const float *gr = p.gy + b * p.gy_bstride;
     const int64_t g0 = q0 * p.Nt;
-    for (int e = tid; e < gyn; e += kDhThreads) {
-      const int64_t gi = g0 + e;
-      const bool ok = gi < p.out_len;
-      cp_async_zfill<4>(&gb[e], ok ? (const void *)(gr + gi) : (const void *)gr, ok);
+    if (p.gal && g0 + gyn <= p.out_len) {
+      // a whole tile of 16-byte aligned gradient rows: 16-byte copies
+      const float *src = gr + g0;
+      for (int e4 = tid; e4 < gyn / 4; e4 += kDhThreads) cp_async_zfill<16>(&gb[4 * e4], src + 4 * e4, true);
+    } else {
+      for (int e = tid; e < gyn; e += kDhThreads) {
+        const int64_t gi = g0 + e;
+        const bool ok = gi < p.out_len;
+        cp_async_zfill<4>(&gb[e], ok ? (const void *)(gr + gi) : (const void *)gr, ok);
+      }
     }
   };
 
@@ -93,6 +113,7 @@ __global__ void __launch_bounds__(kDhThreads) rowtile_dh(const DhParams p) {
 #pragma unroll
     for (int e = 0; e < 16; e++) acc[m][e] = 0.f;
 
+  if (tid == 0) GBFIR_TC_TRACE(3, 0, 1);
   int64_t tile = blockIdx.x;
   if (tile < p.ntiles) issue(tile, xb0, gb0);
   cp_async_commit();
@@ -100,10 +121,13 @@ __global__ void __launch_bounds__(kDhThreads) rowtile_dh(const DhParams p) {
     float *xc = (it & 1) ? xb1 : xb0;
     float *gc = (it & 1) ? gb1 : gb0;
     const int64_t next = tile + gridDim.x;
+    if (tid == 0) GBFIR_TC_TRACE(0, it, 0);
     if (next < p.ntiles) issue(next, (it & 1) ? xb0 : xb1, (it & 1) ? gb0 : gb1);
     cp_async_commit();
+    if (tid == 0) GBFIR_TC_TRACE(0, it, 1);
     cp_async_wait<1>();
     __syncthreads();
+    if (tid == 0) GBFIR_TC_TRACE(0, it, 2);
     if (active) {
       for (int q = r; q < p.QC; q += p.RS) {
         const int xq = q * (int)p.S;
@@ -128,6 +152,7 @@ __global__ void __launch_bounds__(kDhThreads) rowtile_dh(const DhParams p) {
     __syncthreads();
   }
   cp_async_wait<0>();
+  if (tid == 0) GBFIR_TC_TRACE(2, 0, 0);
 
   // ---- deterministic reduction: row slices, then taps -------------------------------
 #pragma unroll
@@ -138,31 +163,44 @@ __global__ void __launch_bounds__(kDhThreads) rowtile_dh(const DhParams p) {
     for (int e = 0; e < 16; e++) red[((size_t)r * p.U + u) * 16 + e] = acc[m][e];
   }
   __syncthreads();
+  if (tid == 0) GBFIR_TC_TRACE(2, 0, 1);
   double *dred = reinterpret_cast<double *>(xb0);  // window buffers are free now: [U][16] doubles
+  // the row slices' sums: compensated FP32 (the rounding error of each addition carried into
+  // the next, in slice order), kept as a double — as exact as FP64 additions of these few
+  // FP32 terms, without the slow FP64 pipe
   for (int e = tid; e < p.U * 16; e += kDhThreads) {
-    double s = 0.0;
-    for (int rr = 0; rr < p.RS; rr++) s += (double)red[(size_t)rr * p.U * 16 + e];
-    dred[e] = s;
+    float sf = 0.f, cf = 0.f;
+    for (int rr = 0; rr < p.RS; rr++) {
+      const float y = __fsub_rn(red[(size_t)rr * p.U * 16 + e], cf);
+      const float t = __fadd_rn(sf, y);
+      cf = __fsub_rn(__fsub_rn(t, sf), y);
+      sf = t;
+    }
+    dred[e] = (double)sf - (double)cf;
   }
   __syncthreads();
+  if (tid == 0) GBFIR_TC_TRACE(2, 0, 3);
   double *part = p.partial + (size_t)blockIdx.x * p.Lo;
-  for (int64_t tp = tid; tp < p.Lo; tp += kDhThreads) {
-    int64_t res = (tp - p.c) % p.up;
-    if (res < 0) res += p.up;
-    const int64_t j0 = (res * p.inv_down) % p.up;
+  // 32-bit index arithmetic (tile-local quantities); along the phases j0, j0 + up, ... the
+  // input position k steps by down
+  const int upi = (int)p.up, dni = (int)p.down, ci = (int)p.c, Loi = (int)p.Lo, Nti = (int)p.Nt;
+  for (int tp = tid; tp < Loi; tp += kDhThreads) {
+    int res = (tp - ci) % upi;
+    if (res < 0) res += upi;
+    const int j0 = (int)(((int64_t)res * p.inv_down) % upi);
+    int k = (ci + j0 * dni - tp) / upi;
     double s = 0.0;
-    for (int64_t mm = 0; mm < p.G; mm++) {
-      const int64_t j = j0 + p.up * mm;
-      if (j >= p.Nt) break;
-      const int64_t g = j >> 2, jj = j & 3;
-      const int64_t k = (p.c + j * p.down - tp) / p.up;
-      const int64_t kl0 = ceil_div(p.c + 4 * g * p.down - p.Lo + 1, p.up);
-      const int64_t kk = k - kl0;
+    for (int mm = 0, j = j0; mm < (int)p.G && j < Nti; mm++, j += upi, k += dni) {
+      const int g = j >> 2, jj = j & 3;
+      const int num = ci + 4 * g * dni - Loi + 1;  // kl0 = ceil(num / up)
+      const int kl0 = num >= 0 ? (num + upi - 1) / upi : -((-num) / upi);
+      const int kk = k - kl0;
       if (kk < 0 || kk >= p.span) continue;
       s += dred[((g * units_per_g + kk / 4) * 16) + (kk % 4) * 4 + jj];
     }
     part[tp] = s;
   }
+  if (tid == 0) GBFIR_TC_TRACE(2, 0, 2);
 }
 
 // dh[m] = scale * sum_p partial[p][m + off]  (fixed order over the partial rows)
@@ -255,6 +293,7 @@ static DhPlan plan_dh(const float *x, int64_t x_bstride, int64_t N, const float 
   p.gy = gy;
   p.gy_bstride = batch > 1 ? gy_bstride : 0;
   p.out_len = out_len;
+  p.gal = (reinterpret_cast<uintptr_t>(gy) % 16 == 0 && p.gy_bstride % 4 == 0) ? 1 : 0;
   p.up = upk;
   p.down = dn;
   p.Lo = geo.Lo;
