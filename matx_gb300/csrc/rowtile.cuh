@@ -72,10 +72,19 @@ struct RsParams {
   int32_t stg_off;   // byte offset of the store staging area in dynamic shared memory
   int64_t rows_full; // rows holding Nt outputs (the tensor map's row count)
   int32_t pair;      // 1: bands start at even k and rows read two samples per 16-byte load
+  int32_t ost_single; // 1: one staging buffer per warp instead of two (one row per thread)
 };
 
+// Batch row of tile t: a 32-bit division wherever the tile count allows it (the 64-bit one
+// is a long instruction sequence, on the path between two tiles).
+__device__ __forceinline__ int64_t tile_row(const RsParams &p, int64_t t) {
+  if (p.ntiles <= 0x7fffffffLL) return (int64_t)((uint32_t)t / (uint32_t)p.tiles_per_row);
+  return t / p.tiles_per_row;
+}
+
 // Output staging of one warp for the TMA-store epilogue: two buffers of 32 rows x ost_rb
-// bytes, alternating; `n` counts the boxes this warp has stored.
+// bytes, alternating (or one, reused once its previous box has been read); `n` counts the
+// boxes this warp has stored.
 struct OutStage {
   const void *map;  // CUtensorMap over (2*Nt floats, rows_full, batch)
   unsigned char *buf;
@@ -150,19 +159,36 @@ __device__ __forceinline__ void build_tap_table(const RsParams &p, const typenam
   TE *table = reinterpret_cast<TE *>(table_raw);
   int *goff = reinterpret_cast<int *>(table_raw + (((size_t)p.ncg * p.span * sizeof(TE) + 15) & ~(size_t)15));
   const int nent = p.ncg * p.span * 4;
-  for (int e = tid; e < nent; e += nthreads) {
-    const int g = e / (p.span * 4);
-    const int rem = e - g * (p.span * 4);
-    const int kk = rem >> 2, jj = rem & 3;
-    const int64_t j = 4 * (int64_t)g + jj;
-    const int64_t kl0 = band_start(p.c, g, p.down, p.Lo, p.up, p.pair != 0);
-    const int64_t tp = p.c + j * p.down - (kl0 + kk) * p.up;
-    HT v = zero_val<HT>();
-    if (j < p.Nt && tp >= 0 && tp < p.Lo) {
-      const int64_t te = p.rev ? p.Lo - 1 - tp : tp;  // index into he
-      if (!(p.even && te == 0)) v = hp[te - p.even];
+  // four entries a thread per pass, their tap loads all in flight before the stores
+  constexpr int U = 4;
+  for (int e0 = tid; e0 < nent; e0 += U * nthreads) {
+    HT v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int e = e0 + u * nthreads;
+      v[u] = zero_val<HT>();
+      if (e < nent) {
+        const int g = e / (p.span * 4);
+        const int rem = e - g * (p.span * 4);
+        const int kk = rem >> 2, jj = rem & 3;
+        const int64_t j = 4 * (int64_t)g + jj;
+        const int64_t kl0 = band_start(p.c, g, p.down, p.Lo, p.up, p.pair != 0);
+        const int64_t tp = p.c + j * p.down - (kl0 + kk) * p.up;
+        if (j < p.Nt && tp >= 0 && tp < p.Lo) {
+          const int64_t te = p.rev ? p.Lo - 1 - tp : tp;  // index into he
+          if (!(p.even && te == 0)) v[u] = hp[te - p.even];
+        }
+      }
     }
-    table[g * p.span + kk].v[jj] = v;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int e = e0 + u * nthreads;
+      if (e < nent) {
+        const int g = e / (p.span * 4);
+        const int rem = e - g * (p.span * 4);
+        table[g * p.span + (rem >> 2)].v[rem & 3] = v[u];
+      }
+    }
   }
   for (int g = tid; g < p.ncg; g += nthreads)
     goff[g] = (int)(band_start(p.c, g, p.down, p.Lo, p.up, p.pair != 0) - p.kmin);
@@ -196,8 +222,11 @@ __device__ __forceinline__ void c2_store_rows(const RsParams &p, const float2 (&
       // stage the warp's 32 rows x 8 phases (swizzled like the tensor map: 16-byte chunk
       // u of row r at chunk u ^ f(r), conflict-free), then one lane stores the box; rows
       // past rows_full are clipped by the map and the one partial row is stored here
-      unsigned char *buf = os.buf + (os.n & 1) * 2048;
-      if (lane == 0 && os.n >= 2) tc::bulk_wait_read<1>();
+      unsigned char *buf = os.buf + (p.ost_single ? 0 : (os.n & 1) * 2048);
+      if (lane == 0 && os.n >= 1) {
+        if (p.ost_single) tc::bulk_wait_read<0>();
+        else if (os.n >= 2) tc::bulk_wait_read<1>();
+      }
       __syncwarp();
       const int rb = p.ost_rb;
       const int sw = rb == 64 ? ((lane >> 1) & 3) : rb == 32 ? ((lane >> 2) & 1) : 0;
@@ -338,6 +367,12 @@ __device__ __forceinline__ void cp_async16_part(void *smem_dst, const void *gmem
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(tc::smem_u32(smem_dst)), "l"(gmem_src),
                "r"(src_bytes)
                : "memory");
+}
+
+// cp.async completion on an mbarrier: the barrier's pending count is raised by one now and
+// lowered again once every cp.async this thread issued before it has landed.
+__device__ __forceinline__ void cp_async_mbar_arrive_inc(uint64_t *bar) {
+  asm volatile("cp.async.mbarrier.arrive.shared::cta.b64 [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
 }
 
 // The paired walk of rowtile_compute_c2: every band starts at an even k and the row stride is
@@ -658,7 +693,9 @@ __global__ void __launch_bounds__(RQ <= 2 ? 512 : 256)
   const XT *xp = reinterpret_cast<const XT *>(p.x);
   OT *op = reinterpret_cast<OT *>(p.out);
 
-  build_tap_table<T, XC, HC>(p, hp, table, tid, blockDim.x);
+  if (tid == 0) GBFIR_TC_TRACE(3, 0, 1);
+  // (odd row strides build the table after issuing the first window copy)
+  if constexpr (PAD > 0 && PAD != 20) build_tap_table<T, XC, HC>(p, hp, table, tid, blockDim.x);
 
   const int wid = tid >> 5, lane = tid & 31;
   const int wr = wid / p.WC, wc = wid - wr * p.WC;
@@ -671,7 +708,7 @@ __global__ void __launch_bounds__(RQ <= 2 ? 512 : 256)
     if (p.ostore) {
       unsigned char *base = smem_raw + p.stg_off;
       base += (1024 - (tc::smem_u32(base) & 1023)) & 1023;
-      ostage.buf = base + wid * 4096;
+      ostage.buf = base + wid * (p.ost_single ? 2048 : 4096);
     }
   }
 
@@ -681,7 +718,7 @@ __global__ void __launch_bounds__(RQ <= 2 ? 512 : 256)
     // 16), which a bulk copy cannot produce; stage it with cp.async (zero-filled outside the
     // signal).
     auto issue_loads = [&](int64_t tile, XT *buf) {
-      const int64_t b = tile / p.tiles_per_row;
+      const int64_t b = tile_row(p, tile);
       const int64_t q0 = (tile - b * p.tiles_per_row) * p.QC;
       const int64_t xs0 = q0 * p.S + p.kmin;
       const XT *row = xp + b * p.x_bstride;
@@ -721,7 +758,7 @@ __global__ void __launch_bounds__(RQ <= 2 ? 512 : 256)
       }
       __syncthreads();
 
-      const int64_t b = tile / p.tiles_per_row;
+      const int64_t b = tile_row(p, tile);
       const int64_t q0 = (tile - b * p.tiles_per_row) * p.QC;
       OT *orow = op + b * p.out_bstride;
       ostage.b = b;
@@ -738,7 +775,7 @@ __global__ void __launch_bounds__(RQ <= 2 ? 512 : 256)
     // TMA bulk copy (thread 0) that completes on an mbarrier.  The copy starts at the
     // 16-byte boundary at or below the window start (`a` elements early) and covers a
     // multiple of 16 bytes; windows that reach past either end of the signal are staged
-    // element by element with zeros outside instead.
+    // element by element (cp.async, zeros outside) on the same barrier instead.
     constexpr int ES = (int)sizeof(XT), G = 16 / ES;
     __shared__ uint64_t s_bar[2];
     __shared__ int s_ok;
@@ -748,50 +785,77 @@ __global__ void __launch_bounds__(RQ <= 2 ? 512 : 256)
       tc::mbar_fence_init();
     }
     __syncthreads();
-    // every thread computes the same origin offset of tile t
-    auto origin = [&](int64_t t, int64_t &b, int64_t &w0) -> int {
-      b = t / p.tiles_per_row;
-      const int64_t q0 = (t - b * p.tiles_per_row) * p.QC;
-      const int64_t xs0 = q0 * p.S + p.kmin;
-      const int a = (int)((reinterpret_cast<uintptr_t>(xp + b * p.x_bstride + xs0) & 15) / ES);
-      w0 = xs0 - a;
-      return a;
+    // tile t: its batch row, first row, and the elements its window copy starts early; every
+    // thread computes the same values once per tile (for the copy one tile ahead, then the
+    // compute)
+    struct Origin {
+      int64_t b, q0, w0;
+      int a;
     };
-    auto issue_window = [&](int64_t t, XT *buf, uint64_t *bar) {
-      int64_t b, w0;
-      const int a = origin(t, b, w0);
-      const int64_t wl = (p.win + a + G - 1) / G * G;
-      const XT *row = xp + b * p.x_bstride;
+    auto origin = [&](int64_t t) -> Origin {
+      Origin o;
+      o.b = tile_row(p, t);
+      o.q0 = (t - o.b * p.tiles_per_row) * p.QC;
+      const int64_t xs0 = o.q0 * p.S + p.kmin;
+      o.a = (int)((reinterpret_cast<uintptr_t>(xp + o.b * p.x_bstride + xs0) & 15) / ES);
+      o.w0 = xs0 - o.a;
+      return o;
+    };
+    auto issue_window = [&](const Origin &o, XT *buf, uint64_t *bar, int ts) {
+      const int64_t w0 = o.w0;
+      const int64_t wl = (p.win + o.a + G - 1) / G * G;
+      const XT *row = xp + o.b * p.x_bstride;
       // the bulk copy's alignment rules hold by construction; check them anyway and take
       // the element path if they do not
       const bool aligned = ((reinterpret_cast<uintptr_t>(row + w0) | (uintptr_t)tc::smem_u32(buf)) & 15) == 0;
       if (aligned && w0 >= 0 && w0 + wl <= p.N) {
         if (tid == 0) {
           const uint32_t bytes = (uint32_t)(wl * ES);
+          GBFIR_TC_TRACE(2, ts, 1);
           tc::fence_async_smem();
+          GBFIR_TC_TRACE(2, ts, 2);
           tc::mbar_arrive_expect_tx(bar, bytes);
           tc::bulk_copy_g2s(buf, row + w0, bytes, bar);
+          GBFIR_TC_TRACE(2, ts, 3);
         }
       } else {
+        // one cp.async per sample (zeros outside the signal), each thread's copies completing
+        // on the barrier; the barrier's one expected arrival comes from thread 0 once every
+        // thread has registered its copies, so the window lands while the CTA computes
         for (int64_t e = tid; e < wl; e += blockDim.x) {
           const int64_t gi = w0 + e;
-          buf[e] = (gi >= 0 && gi < p.N) ? row[gi] : zero_val<XT>();
+          const bool ok = gi >= 0 && gi < p.N;
+          cp_async_zfill<ES>(&buf[e], ok ? (const void *)(row + gi) : (const void *)row, ok);
         }
+        cp_async_mbar_arrive_inc(bar);
+        __syncthreads();
         if (tid == 0) tc::mbar_arrive_plain(bar);
       }
     };
 
     int64_t tile = blockIdx.x;
-    if (tile < p.ntiles) issue_window(tile, xbuf0, &s_bar[0]);
+    if (tid == 0) GBFIR_TC_TRACE(3, 0, 0);
+    Origin oc{};
+    if (tile < p.ntiles) {
+      oc = origin(tile);
+      issue_window(oc, xbuf0, &s_bar[0], 16);
+    }
+    // the table is complete before any thread reads it: the loop's first barrier follows
+    build_tap_table<T, XC, HC>(p, hp, table, tid, blockDim.x);
     for (int it = 0; tile < p.ntiles; tile += gridDim.x, ++it) {
+      if (tid == 0) GBFIR_TC_TRACE(2, it, 0);
       const int k = dbuf ? (it & 1) : 0;
       XT *cur = k ? xbuf1 : xbuf0;
       const uint32_t parity = dbuf ? ((it >> 1) & 1) : (it & 1);
       const int64_t next = tile + gridDim.x;
+      Origin on{};
+      if (next < p.ntiles) on = origin(next);
       // the other buffer was released by the barrier that ended the previous tile
-      if (dbuf && next < p.ntiles) issue_window(next, k ? xbuf0 : xbuf1, &s_bar[k ^ 1]);
+      if (dbuf && next < p.ntiles) issue_window(on, k ? xbuf0 : xbuf1, &s_bar[k ^ 1], it);
+      if (tid == 0) GBFIR_TC_TRACE(0, it, 0);
       if (tid == 0) s_ok = tc::mbar_wait(&s_bar[k], parity) ? 1 : 0;
       __syncthreads();
+      if (tid == 0) GBFIR_TC_TRACE(0, it, 1);
       if (!s_ok) {
         // a copy that never completed: record it and stop; give the copies in flight a
         // bounded chance to land before the CTA (and its shared memory) goes away
@@ -803,14 +867,15 @@ __global__ void __launch_bounds__(RQ <= 2 ? 512 : 256)
         __syncthreads();
         break;
       }
-      int64_t b, w0;
-      const int a = origin(tile, b, w0);
-      const int64_t q0 = (tile - b * p.tiles_per_row) * p.QC;
-      OT *orow = op + b * p.out_bstride;
-      ostage.b = b;
-      rowtile_compute<T, XC, HC, RQ, PAD>(p, cur, table, orow, q0, wr, wc, lane, scale, a, ostage);
+      OT *orow = op + oc.b * p.out_bstride;
+      ostage.b = oc.b;
+      rowtile_compute<T, XC, HC, RQ, PAD>(p, cur, table, orow, oc.q0, wr, wc, lane, scale, oc.a, ostage);
+      if (tid == 0) GBFIR_TC_TRACE(0, it, 2);
+      if (lane == 0 && wid == (int)(blockDim.x >> 5) - 1) GBFIR_TC_TRACE(1, it, 2);
       __syncthreads();
-      if (!dbuf && next < p.ntiles) issue_window(next, xbuf0, &s_bar[0]);
+      if (tid == 0) GBFIR_TC_TRACE(0, it, 3);
+      if (!dbuf && next < p.ntiles) issue_window(on, xbuf0, &s_bar[0], it);
+      oc = on;
     }
   }
   // the staged boxes are read and written before the CTA's shared memory goes away
@@ -871,7 +936,7 @@ __global__ void __launch_bounds__(kRingThreads, 1)
   // tile t: its batch row, first row, and (odd strides) the elements its window copy starts
   // early so that the bulk copy is 16-byte aligned
   auto origin = [&](int64_t t, int64_t &b, int64_t &q0, int64_t &w0) -> int {
-    b = t / p.tiles_per_row;
+    b = tile_row(p, t);
     q0 = (t - b * p.tiles_per_row) * p.QC;
     const int64_t xs0 = q0 * p.S + p.kmin;
     int a = 0;
@@ -1297,6 +1362,7 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
                       ost_rb > 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0 &&
                       (batch == 1 || out_bstride % 2 == 0) && rows_full >= 1;
   size_t stg_bytes = ostore ? 1024 + (size_t)(threads / 32 - (ring ? nstage : 0)) * 4096 : 0;
+  bool ost_single = false;
   auto smem_for = [&](int rq, int nbuf) -> size_t {
     const int64_t QC = 32LL * rq * wr;
     const int64_t win = (QC - 1) * geo.S + (geo.kmax - geo.kmin) + 1;
@@ -1333,11 +1399,25 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
     if (nbuf > 2) nbuf = 2;
     if (sizeof(T) == 8) rq = 1;
     else if (threads > 256 && rq > 2) rq = 2;  // CTAs of 9-16 column warps: 1 or 2 rows per thread
-    // two CTAs per SM: prefer double buffering, then fewer rows, then a single buffer
-    while (smem_for(rq, nbuf) > 110 * 1024 && (rq > 1 || nbuf > 1)) {
-      if (nbuf == 2 && rq == 1) nbuf = 1;
-      else if (rq > 1) rq /= 2;
-      else nbuf = 1;
+    // two CTAs per SM (228 KB per SM, 1 KB of it reserved per CTA): prefer double buffering,
+    // then fewer rows, then (one row per thread, whose warps compute a whole super-group
+    // between two boxes) one staging buffer per warp, then a single window buffer
+    const size_t stg_two = stg_bytes;
+    while (smem_for(rq, nbuf) > 112 * 1024 && (rq > 1 || nbuf > 1)) {
+      if (nbuf == 2 && rq == 1 && ostore && !ost_single) {
+        ost_single = true;
+        stg_bytes = 1024 + (size_t)(threads / 32) * 2048;
+      } else if (nbuf == 2 && rq == 1) {
+        nbuf = 1;
+      } else if (rq > 1) {
+        rq /= 2;
+      } else {
+        nbuf = 1;
+      }
+    }
+    if (nbuf == 1 && ost_single) {
+      ost_single = false;
+      stg_bytes = stg_two;
     }
   }
   const size_t smem = smem_for(rq, nbuf);
@@ -1393,6 +1473,7 @@ inline int resample_pass(const void *in, int64_t in_bstride, int64_t N_in, const
         p.ost_rb = ost_rb;
         p.rows_full = rows_full;
         p.stg_off = (int32_t)(smem - stg_bytes);
+        p.ost_single = ost_single ? 1 : 0;
       }
     }
     if constexpr (kRingType) {
