@@ -262,6 +262,11 @@ def test_resample_tile_overrides_agree(mx, orc):
     (3, 2, 2, 20001, (4, 2, 8, 1)), (3, 2, 3, 20000, (2, 1, 8, 2)), (4, 5, 1, 20003, (2, 1, 1, 2)),
     (4, 5, 2, 20000, (4, 1, 1, 1)), (1, 2, 2, 9999, (2, 2, 2, 2)), (160, 147, 2, 20000, (1, 10, 1, 1)),
     (160, 147, 1, 20011, (1, 8, 1, 2)), (5, 4, 2, 20002, (2, 2, 0, 1)), (2, 1, 3, 7777, (4, 1, 0, 2)),
+    # odd row stride, double-buffered windows with one staging buffer per warp (two CTAs per
+    # SM): long rows, rows of one or two tiles (every window reaches past a signal end and is
+    # staged by cp.async), and signals shorter than one window
+    (160, 147, 2, 20000, (1, 10, 1, 2)), (160, 147, 8, 3001, (1, 10, 1, 2)),
+    (160, 147, 16, 500, (1, 10, 1, 2)), (160, 147, 6, 7003, (1, 10, 1, 1)),
 ])
 def test_resample_tma_store_epilogue(mx, orc, case):
     """Buffers + 4 sends the outputs through shared memory and TMA tensor stores: the result
