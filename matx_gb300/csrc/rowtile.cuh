@@ -1003,19 +1003,20 @@ __global__ void __launch_bounds__(kRingThreads, 1)
             tc::mbar_arrive_plain(&full[slot]);
           }
         } else {
+          // one cp.async per sample (zeros outside the signal), each lane's arrival made when
+          // its copies have landed, so the staging warps go on to the next slot at once
           for (int64_t e = sl; e < wl; e += nsl) {
             const int64_t gi = w0 + e;
-            buf[e] = (gi >= 0 && gi < p.N) ? row[gi] : make_float2(0.f, 0.f);
+            const bool ok = gi >= 0 && gi < p.N;
+            cp_async_zfill<8>(&buf[e], ok ? (const void *)(row + gi) : (const void *)row, ok);
           }
-          tc::mbar_arrive_plain(&full[slot]);  // each lane's stores are ordered before its arrival
+          cp_async_mbar_arrive(&full[slot]);
         }
       }
       if (sl == 0) GBFIR_TC_TRACE(0, (int)n, 1);
     }
-    if constexpr (PAD != 0 && PAD != 20) {
-      cp_async_commit();  // the copies were never grouped: group them, then wait for all
-      cp_async_wait<0>();
-    }
+    cp_async_commit();  // the copies were never grouped: group them, then wait for all
+    cp_async_wait<0>();
   } else {
     // ================= compute warps =================
     const int cw = wid - nstage;
