@@ -279,7 +279,6 @@ __device__ __forceinline__ void rowtile_compute_c2(const RsParams &p, const floa
   const int nsg = (p.ncg + 1) / 2;
   const int rbase = wr * 32 * RQ + lane;
   const float2 sc = make_float2(scale, scale);
-  const int Nt = (int)p.Nt;
   for (int sg = wc; sg < nsg; sg += p.WC) {
     const int gA = 2 * sg, gB = 2 * sg + 1;
     const bool hasB = gB < p.ncg;
@@ -681,7 +680,6 @@ __global__ void __launch_bounds__(RQ <= 2 ? 512 : 256)
   using XT = typename val_of<T, XC>::type;
   using HT = typename val_of<T, HC>::type;
   using OT = typename val_of<T, XC || HC>::type;
-  constexpr bool OC = XC || HC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned char *table = smem_raw;
   const size_t table_bytes = tap_table_bytes<T, XC, HC>(p.ncg, p.span);
